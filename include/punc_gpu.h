@@ -1,0 +1,259 @@
+/*
+ * punc_gpu.h - C ABI of the GB300 particle-in-cell engine.
+ *
+ * Each entry point replaces one PUNC++ function or method on the
+ * per-timestep particle path (paths are relative to the PUNC++ tree).
+ * The engine owns every device buffer; host pointers passed in are
+ * borrowed for the duration of the call only.  Every function returns a
+ * pg_status; no function aborts, traps or exits.  A handle is not
+ * thread-safe: calls on one handle are ordered on the handle's own CUDA
+ * stream.
+ */
+#ifndef PUNC_GPU_H
+#define PUNC_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PG_ABI_VERSION 1
+
+typedef enum pg_status {
+    PG_OK = 0,
+    PG_ERR_ARG = 1,            /* invalid argument or size */
+    PG_ERR_CUDA = 2,           /* a CUDA runtime call failed */
+    PG_ERR_MESH = 3,           /* inconsistent mesh: non-manifold facet, untagged boundary facet, degenerate cell */
+    PG_ERR_CAPACITY = 4,       /* particle store full */
+    PG_ERR_WALK_LIMIT = 5,     /* a relocation walk hit its step limit (cycle or non-finite position) */
+    PG_ERR_NOT_CONVERGED = 6,  /* PCG reached its iteration cap */
+    PG_ERR_STATE = 7,          /* call out of order (e.g. circuit or flux not set up) */
+    PG_ERR_SINGULAR = 8        /* circuit matrix could not be inverted */
+} pg_status;
+
+typedef enum pg_precision {
+    PG_FP64 = 0,   /* all particle arithmetic in FP64, reference rounding order */
+    PG_MIXED = 1   /* FP32 particles, FP64 facet re-test, int64 fixed-point deposit */
+} pg_precision;
+
+/* Opaque handles. */
+typedef struct pg_mesh pg_mesh;   /* host-side mesh tables */
+typedef struct pg_sim pg_sim;     /* device-resident mesh, particles and solver */
+
+/* Mesh as plain arrays, the content of a DOLFIN Mesh plus its facet
+ * MeshFunction after Mesh::Mesh relabelled the tags
+ * (punc/src/mesh.cpp:41-60): tag 1 = exterior boundary, 2.. = objects.
+ * Every boundary facet must be listed with a tag >= 1. */
+typedef struct pg_mesh_desc {
+    int64_t n_vertices;
+    const double *coords;            /* [n_vertices][3] */
+    int64_t n_cells;
+    const int64_t *cells;            /* [n_cells][4] vertex ids, any order */
+    int64_t n_boundary_facets;
+    const int64_t *bfacet_vertices;  /* [n_boundary_facets][3] */
+    const int32_t *bfacet_tags;      /* [n_boundary_facets] */
+    int64_t n_dofs;                  /* CG1 dofs; = n_vertices unless periodic */
+    const int64_t *vertex_to_dof;    /* [n_vertices] or NULL (identity) */
+} pg_mesh_desc;
+
+/* Which host table pg_mesh_array returns. */
+typedef enum pg_mesh_table {
+    PG_T_CELL_VERTICES = 0,  /* int64 [Nc][4], ascending vertex ids (UFC order) */
+    PG_T_BARYCENTRIC = 1,    /* double [Nc][12], rows 0-2 of the barycentric matrix */
+    PG_T_PLANES = 2,         /* double [Nc][16], per facet i: -n.m, n_x, n_y, n_z */
+    PG_T_NEIGHBOURS = 3,     /* int64 [Nc][4], neighbour across facet i or -tag */
+    PG_T_CELL_DOFS = 4,      /* int64 [Nc][4] */
+    PG_T_VOLUME = 5,         /* double [Nc] */
+    PG_T_DV_INV = 6,         /* double [Ndof], (d+1) / patch volume */
+    PG_T_CSR_ROWPTR = 7,     /* int64 [Ndof+1] */
+    PG_T_CSR_COL = 8,        /* int64 [nnz] */
+    PG_T_STIFFNESS = 9,      /* double [nnz], eps0 * P1 stiffness, no boundary conditions */
+    PG_T_MASS = 10,          /* double [nnz], consistent P1 mass */
+    PG_T_EXT_FACETS = 11,    /* double [Nf][14]: area, 9 vertex coords, 3 inward normal, cell */
+    PG_T_BC_KIND = 12,       /* int64 [Ndof]: -1 free, 0 exterior, k>=1 object k (tag k+1) */
+    PG_T_OBJ_FACETS = 13     /* double [No][7]: cell, object index, area, 3 outward normal, local facet */
+} pg_mesh_table;
+
+typedef struct pg_config {
+    int32_t precision;          /* pg_precision */
+    int32_t periodic;           /* 1: remove the constant null space (no Dirichlet BC) */
+    double eps0;                /* vacuum permittivity in simulation units */
+    int64_t particle_capacity;  /* particle slots to allocate (0: automatic) */
+    int32_t max_walk_steps;     /* relocation walk step limit (0: 100000) */
+    int32_t sort_interval;      /* cell-sort period in steps of pg_step (0: 20) */
+    double pcg_rtol;            /* 0: 1e-12, PoissonSolver default (punc/src/poisson.cpp:326-328) */
+    double pcg_atol;            /* 0: 1e-14 */
+    int32_t pcg_max_iter;       /* 0: 1000 */
+    int32_t pcg_warm_start;     /* 1: start PCG from the previous potential */
+    double ext_E[3];            /* exterior Dirichlet value phi = x . ext_E (PhiBoundary) */
+} pg_config;
+
+/* Reference Object (punc/include/punc/object.h:80-130). */
+typedef struct pg_object {
+    int64_t bnd_id;     /* boundary tag, 2 = first object */
+    double charge;
+    double current;
+    double potential;
+} pg_object;
+
+/* Reference VSource / ISource (punc/include/punc/object.h:45-71). */
+typedef struct pg_source {
+    int32_t node_a;     /* -1 = ground */
+    int32_t node_b;
+    double value;
+} pg_source;
+
+/* Species with a Maxwellian velocity distribution
+ * (punc/src/population.cpp:41-70, punc/src/distributions.cpp:23-77). */
+typedef struct pg_species {
+    double q;           /* charge of a simulation particle */
+    double m;           /* mass of a simulation particle */
+    double n;           /* number density of simulation particles */
+    double vth;         /* thermal speed */
+    double vd[3];       /* drift velocity */
+    double vdf_range;   /* rejection box half-width in vth (0: 5) */
+} pg_species;
+
+typedef struct pg_solve_info {
+    int32_t iterations;
+    int32_t solves;
+    double residual;    /* final ||r||_2 of the last solve */
+    double rhs_norm;    /* ||b||_2 of the last solve */
+} pg_solve_info;
+
+/* One fused timestep in the order of the time loop of
+ * interaction/interaction.cpp:342-480. */
+typedef struct pg_step_args {
+    double dt;
+    double B[3];             /* uniform magnetic field */
+    int32_t first_step;      /* 1: push with dt/2 (leapfrog start) */
+    int32_t use_accel;       /* 1: accel() instead of boris() */
+    int32_t periodic_move;   /* 1: move_periodic with Ld */
+    double Ld[3];
+    int32_t inject;          /* 1: flux injection after update */
+    uint64_t seed;           /* injection RNG key */
+    uint64_t step;           /* injection RNG counter (time step number) */
+    double E0[3];            /* uniform external field added to the cell field */
+} pg_step_args;
+
+typedef struct pg_step_result {
+    double KE;               /* kinetic energy at mid-step (returned by the push) */
+    int64_t n_particles;     /* after injection */
+    int64_t n_absorbed;
+    int64_t n_injected;
+    int32_t pcg_iterations;  /* summed over the step's solves */
+    double pcg_residual;
+} pg_step_result;
+
+/* ---- library ---------------------------------------------------------- */
+int32_t pg_abi_version(void);
+const char *pg_last_error(void);       /* thread-local text of the last failure */
+/* One block of the Philox4x32-10 generator behind pg_inject (the reference's
+ * std::mt19937_64, punc/include/punc/injector.h:161, is unseeded and cannot be
+ * reproduced; this stream can).  No GPU needed. */
+int pg_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+/* ---- mesh tables (host only, no GPU needed) ---------------------------- */
+/* Population<3>::Population + init_localizer + Cell::init_barycentric_matrix
+ * (punc/include/punc/population.h:310-389, punc/src/population.cpp:181-240),
+ * element_volume (punc/src/distributor.cpp:35-69), P1 stiffness and mass
+ * (punc/ufl/Potential3D.ufl), Mesh::exterior_boundaries
+ * (punc/src/mesh.cpp:166-236). */
+int pg_mesh_build(const pg_mesh_desc *desc, double eps0, pg_mesh **out);
+int pg_mesh_array(const pg_mesh *mesh, int32_t which, const void **data, int64_t *count);
+int pg_mesh_free(pg_mesh *mesh);
+
+/* ---- engine ------------------------------------------------------------ */
+int pg_create(const pg_mesh *mesh, const pg_config *cfg, pg_sim **out);
+int pg_destroy(pg_sim *sim);
+int pg_status_detail(pg_sim *sim, int32_t *code, int64_t *index);
+
+/* Population::add_particles(xs, vs, q, m) (punc/include/punc/population.h:411-435):
+ * locate each point and keep those inside the mesh. */
+int pg_add_particles(pg_sim *sim, const double *xs, const double *vs, int64_t n,
+                     double q, double m, int64_t *n_added);
+/* num_of_particles / num_of_negatives / num_of_positives
+ * (punc/include/punc/population.h:701-744). */
+int pg_num_particles(pg_sim *sim, int64_t *total, int64_t *negatives, int64_t *positives);
+/* Download live particles ordered by (cell, particle id).  Any output may be NULL. */
+int pg_get_particles(pg_sim *sim, int64_t capacity, double *x, double *v, double *q,
+                     double *m, int64_t *cell, int64_t *pid, int64_t *n_out);
+/* Population::locate (punc/src/population.cpp:24-39), for n points. */
+int pg_locate(pg_sim *sim, const double *xs, int64_t n, int64_t *cells);
+
+/* EFieldDG0::solve (punc/src/efield.cpp:95-99): E = -grad(phi) per cell.
+ * phi may be NULL (use the device potential). */
+int pg_efield_dg0(pg_sim *sim, const double *phi);
+int pg_set_efield(pg_sim *sim, const double *E_cells);   /* [Nc][3] */
+int pg_get_efield(pg_sim *sim, double *E_cells);         /* [Nc][3] */
+
+/* accel with a DG0 field (punc/include/punc/pusher.h:66-130). */
+int pg_accel(pg_sim *sim, double dt, double *KE);
+/* boris with a DG0 field and uniform B (punc/include/punc/pusher.h:397-510). */
+int pg_boris(pg_sim *sim, const double B[3], double dt, double *KE);
+/* move / move_periodic (punc/include/punc/pusher.h:648-681). */
+int pg_move(pg_sim *sim, double dt);
+int pg_move_periodic(pg_sim *sim, double dt, const double Ld[3]);
+/* Population::update (punc/include/punc/population.h:641-699): relocate every
+ * particle by the facet walk of relocate_fast (539-569), absorb at boundaries,
+ * zero then tally object currents, charge += current, current /= dt. */
+int pg_update(pg_sim *sim, pg_object *objects, int32_t n_objects, double dt);
+/* kinetic_energy (punc/include/punc/diagnostics.h:248-265). */
+int pg_kinetic_energy(pg_sim *sim, double *KE);
+
+/* distribute_cg1 (punc/include/punc/distributor.h:168-210): rho = dv_inv * sum q lambda.
+ * rho may be NULL (keep it on the device only). */
+int pg_distribute_cg1(pg_sim *sim, double *rho);
+int pg_set_rho(pg_sim *sim, const double *rho);
+
+/* PoissonSolver::solve (punc/src/poisson.cpp:343-362) with object potentials
+ * as Dirichlet values; phi may be NULL. */
+int pg_poisson_solve(pg_sim *sim, const pg_object *objects, int32_t n_objects,
+                     double *phi, pg_solve_info *info);
+/* CircuitCM::CircuitCM (punc/src/object_CM.cpp:135-197): capacitance matrix
+ * by one Laplace solve per object, then the circuit matrix. */
+int pg_circuit_cm_setup(pg_sim *sim, const pg_source *vsources, int32_t n_vsources,
+                        const pg_source *isources, int32_t n_isources, double dt);
+/* PoissonSolver::solve_circuit (punc/src/poisson.cpp:364-376) with CircuitCM
+ * pre_solve / post_solve (punc/src/object_CM.cpp:53-60, 328-357). */
+int pg_solve_circuit(pg_sim *sim, pg_object *objects, int32_t n_objects,
+                     double *phi, pg_solve_info *info);
+int pg_get_phi(pg_sim *sim, double *phi);
+int pg_get_rho(pg_sim *sim, double *rho);
+int pg_get_capacitance(pg_sim *sim, double *inv_capacitance);  /* [n_obj][n_obj] */
+
+/* create_flux (punc/src/injector.cpp:104-171) for Maxwellian species. */
+int pg_create_flux(pg_sim *sim, const pg_species *species, int32_t n_species);
+/* inject_particles (punc/include/punc/injector.h:157-232) with a counter-based
+ * Philox4x32-10 stream keyed by (seed, step, species, facet). */
+int pg_inject(pg_sim *sim, double dt, uint64_t seed, uint64_t step, int64_t *n_injected);
+
+/* One fused timestep: push, move, update, inject, deposit, Poisson with the
+ * circuit, E field (interaction/interaction.cpp:342-480). */
+int pg_step(pg_sim *sim, const pg_step_args *args, pg_object *objects, int32_t n_objects,
+            pg_step_result *result);
+/* Sort particles by cell and drop absorbed slots. */
+int pg_sort(pg_sim *sim);
+
+/* Per-stage device times in ms of pg_step accumulated since the last call
+ * (CUDA events on the engine stream, recorded while profiling is on), like
+ * the reference Timer (punc/include/punc/diagnostics.h:171-234). */
+int pg_stage_times(pg_sim *sim, double *ms, int32_t capacity, int32_t *n_stages);
+const char *pg_stage_name(pg_sim *sim, int32_t index);   /* NULL if out of range */
+int pg_set_profiling(pg_sim *sim, int32_t on);
+/* CUDA events on the engine stream, for timing a span of calls on the device:
+ * record into slot 0..15, then the elapsed ms between two recorded slots
+ * (waits for the later one). */
+int pg_event_record(pg_sim *sim, int32_t slot);
+int pg_event_elapsed(pg_sim *sim, int32_t from_slot, int32_t to_slot, double *ms);
+/* Wait until all work queued on the engine stream has finished. */
+int pg_synchronize(pg_sim *sim);
+/* Number of kernels this library has launched in this process. */
+int pg_launch_count(int64_t *n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PUNC_GPU_H */

@@ -1,0 +1,941 @@
+// ORACLE - test infrastructure only.  A CPU restatement of the PUNC++
+// per-timestep particle path, used by tests/, the smoke check and bench.py's
+// CPU-baseline leg to check and time the GPU engine.  Never part of the
+// product path.
+//
+// It keeps the reference's data model: AoS particles {x, v, q, m} bucketed in
+// per-cell std::vectors, cells visited in id order, particles in vector
+// order, Population::update's push_back / swap-with-back bookkeeping.  Each
+// function cites the reference file:line it restates (paths relative to the
+// PUNC++ tree).
+//
+// Parity status: the reference cannot be built here (DOLFIN 2019.1, FFC,
+// PETSc and Boost are absent) and ships no golden vectors, so parity with the
+// reference binary is UNPINNED.  The arithmetic of DOLFIN's
+// TetrahedronCell::normal and MeshEntity::midpoint is restated from the
+// published DOLFIN 2019.1.0 source; the cell volume, facet area, P1 element
+// matrices (FFC for punc/ufl/Potential3D.ufl) and the DG0 gradient are
+// restated from the mathematics.  The analytic known answers of the
+// reference's demos (capacitance, Langmuir frequency, orbit, flux count) are
+// checked against this oracle in tests/test_oracle_known_answers.py.
+//
+// Compile with -ffp-contract=off and without -march (the reference's Release
+// build, punc/CMakeLists.txt).
+#include <algorithm>
+#include <array>
+#include <climits>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <thread>
+#include <vector>
+
+namespace {
+
+struct Particle {            // punc/include/punc/population.h:74-94 (+ a test id)
+    double x[3];
+    double v[3];
+    double q;
+    double m;
+    int64_t id;
+};
+
+struct Cell {                // punc/include/punc/population.h:179-231
+    int64_t id;
+    int64_t vertices[4];     // ascending global index (DOLFIN ordered mesh)
+    std::array<double, 12> vertex_coordinates;
+    double barycentric_matrix[12];
+    std::vector<long> facet_adjacents;
+    std::vector<double> facet_plane_coeffs;
+    std::vector<Particle> particles;
+    int64_t dofs[4];
+    double volume;
+
+    // Cell<3>::init_barycentric_matrix (punc/src/population.cpp:181-240)
+    void init_barycentric_matrix() {
+        double x1 = vertex_coordinates[0], y1 = vertex_coordinates[1], z1 = vertex_coordinates[2];
+        double x2 = vertex_coordinates[3], y2 = vertex_coordinates[4], z2 = vertex_coordinates[5];
+        double x3 = vertex_coordinates[6], y3 = vertex_coordinates[7], z3 = vertex_coordinates[8];
+        double x4 = vertex_coordinates[9], y4 = vertex_coordinates[10], z4 = vertex_coordinates[11];
+        double x13 = x1 - x3; double y13 = y1 - y3; double z13 = z1 - z3;
+        double x14 = x1 - x4; double y14 = y1 - y4; double z14 = z1 - z4;
+        double x24 = x2 - x4; double y24 = y2 - y4; double z24 = z2 - z4;
+        double x31 = x3 - x1; double y31 = y3 - y1; double z31 = z3 - z1;
+        double x32 = x3 - x2; double y32 = y3 - y2; double z32 = z3 - z2;
+        double x34 = x3 - x4; double y34 = y3 - y4; double z34 = z3 - z4;
+        double x42 = x4 - x2; double y42 = y4 - y2; double z42 = z4 - z2;
+        double x43 = x4 - x3; double y43 = y4 - y3; double z43 = z4 - z3;
+        double V01 = (x2 * (y3 * z4 - y4 * z3) + x3 * (y4 * z2 - y2 * z4) + x4 * (y2 * z3 - y3 * z2)) / 6.0;
+        double V02 = (x1 * (y4 * z3 - y3 * z4) + x3 * (y1 * z4 - y4 * z1) + x4 * (y3 * z1 - y1 * z3)) / 6.0;
+        double V03 = (x1 * (y2 * z4 - y4 * z2) + x2 * (y4 * z1 - y1 * z4) + x4 * (y1 * z2 - y2 * z1)) / 6.0;
+        double V04 = (x1 * (y3 * z2 - y2 * z3) + x2 * (y1 * z3 - y3 * z1) + x3 * (y2 * z1 - y1 * z2)) / 6.0;
+        double V = V01 + V02 + V03 + V04;
+        double V6 = 6 * V;
+        double *A = barycentric_matrix;
+        A[0] = V01 / V; A[4] = V02 / V; A[8] = V03 / V;
+        A[1] = (y42 * z32 - y32 * z42) / V6;
+        A[5] = (y31 * z43 - y34 * z13) / V6;
+        A[9] = (y24 * z14 - y14 * z24) / V6;
+        A[2] = (x32 * z42 - x42 * z32) / V6;
+        A[6] = (x43 * z31 - x13 * z34) / V6;
+        A[10] = (x14 * z24 - x24 * z14) / V6;
+        A[3] = (x42 * y32 - x32 * y42) / V6;
+        A[7] = (x31 * y43 - x34 * y13) / V6;
+        A[11] = (x24 * y14 - x14 * y24) / V6;
+    }
+
+    // Cell<3>::barycentric (punc/include/punc/population.h:885-893)
+    void barycentric(const double *x, double *y) const {
+        const double *A = barycentric_matrix;
+        y[0] = A[0] + A[1] * x[0] + A[2] * x[1] + A[3] * x[2];
+        y[1] = A[4] + A[5] * x[0] + A[6] * x[1] + A[7] * x[2];
+        y[2] = A[8] + A[9] * x[0] + A[10] * x[1] + A[11] * x[2];
+        y[3] = 1 - y[0] - y[1] - y[2];
+    }
+
+    // DOLFIN 2019.1.0 TetrahedronCell::normal(cell, facet): cross product of
+    // the facet's edge vectors from its first vertex, normalised, flipped to
+    // point away from the opposite vertex.
+    std::array<double, 3> normal(int facet) const {
+        int f[3], k = 0;
+        for (int i = 0; i < 4; ++i) if (i != facet) f[k++] = i;
+        const double *P0 = &vertex_coordinates[3 * facet];
+        const double *P1 = &vertex_coordinates[3 * f[0]];
+        const double *P2 = &vertex_coordinates[3 * f[1]];
+        const double *P3 = &vertex_coordinates[3 * f[2]];
+        double V0[3], V1[3], V2[3];
+        for (int j = 0; j < 3; ++j) { V0[j] = P0[j] - P1[j]; V1[j] = P2[j] - P1[j]; V2[j] = P3[j] - P1[j]; }
+        double n[3] = {V1[1] * V2[2] - V1[2] * V2[1], V1[2] * V2[0] - V1[0] * V2[2], V1[0] * V2[1] - V1[1] * V2[0]};
+        double norm = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        for (int j = 0; j < 3; ++j) n[j] /= norm;
+        if (n[0] * V0[0] + n[1] * V0[1] + n[2] * V0[2] > 0)
+            for (int j = 0; j < 3; ++j) n[j] *= -1.0;
+        return {n[0], n[1], n[2]};
+    }
+
+    // DOLFIN 2019.1.0 MeshEntity::midpoint: running vertex sum / vertex count.
+    std::array<double, 3> facet_midpoint(int facet) const {
+        double x = 0.0, y = 0.0, z = 0.0;
+        std::size_t num_vertices = 0;
+        for (int i = 0; i < 4; ++i) {
+            if (i == facet) continue;
+            x += vertex_coordinates[3 * i];
+            y += vertex_coordinates[3 * i + 1];
+            z += vertex_coordinates[3 * i + 2];
+            num_vertices++;
+        }
+        x /= double(num_vertices); y /= double(num_vertices); z /= double(num_vertices);
+        return {x, y, z};
+    }
+};
+
+// Portable Philox4x32-10 (Salmon et al., SC'11) and the stream layout of the
+// engine's injection: key = seed, counter = (block, facet, species, step).
+struct Philox {
+    static void round10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+        for (int r = 0; r < 10; ++r) {
+            const uint64_t p0 = uint64_t(0xD2511F53u) * c[0];
+            const uint64_t p1 = uint64_t(0xCD9E8D57u) * c[2];
+            const uint32_t hi0 = uint32_t(p0 >> 32), lo0 = uint32_t(p0);
+            const uint32_t hi1 = uint32_t(p1 >> 32), lo1 = uint32_t(p1);
+            const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+            c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+            k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+        }
+    }
+};
+
+struct Stream {
+    uint32_t k0, k1, c1, c2, c3, block = 0;
+    bool have = false;
+    double cached = 0;
+    Stream(uint64_t seed, uint32_t a, uint32_t b, uint32_t c) : k0(uint32_t(seed)), k1(uint32_t(seed >> 32)), c1(a), c2(b), c3(c) {}
+    static double res53(uint32_t a, uint32_t b) {
+        return (double(a >> 5) * 67108864.0 + double(b >> 6)) * (1.0 / 9007199254740992.0);
+    }
+    double operator()() {
+        if (have) { have = false; return cached; }
+        uint32_t c[4] = {block, c1, c2, c3};
+        Philox::round10(c, k0, k1);
+        ++block;
+        cached = res53(c[2], c[3]);
+        have = true;
+        return res53(c[0], c[1]);
+    }
+};
+
+// exp from Cody-Waite reduction by ln2 (24-bit head) and the degree-13
+// Taylor polynomial, so CPU and GPU accept/reject identically.
+double exp_series(double x) {
+    if (x != x) return x;
+    if (x > 709.5) return HUGE_VAL;
+    if (x < -745.0) return 0.0;
+    const double kf = std::floor(x * 0x1.71547652b82fep+0 + 0.5);
+    const double r = (x - kf * 0x1.62e4300000000p-1) - kf * -0x1.05c610ca86c39p-29;
+    static const double c[14] = {0x1.6124613a86d09p-33, 0x1.1eed8eff8d898p-29, 0x1.ae64567f544e4p-26,
+                                 0x1.27e4fb7789f5cp-22, 0x1.71de3a556c734p-19, 0x1.a01a01a01a01ap-16,
+                                 0x1.a01a01a01a01ap-13, 0x1.6c16c16c16c17p-10, 0x1.1111111111111p-7,
+                                 0x1.5555555555555p-5, 0x1.5555555555555p-3, 0.5, 1.0, 1.0};
+    double p = c[0];
+    for (int i = 1; i < 14; ++i) p = p * r + c[i];
+    int k = int(kf);
+    double extra = 1.0;
+    if (k < -1020) { k += 1000; extra = 0x1p-1000; }
+    const uint64_t bits = uint64_t(int64_t(k) + 1023) << 52;
+    double two_k;
+    std::memcpy(&two_k, &bits, 8);
+    return (p * two_k) * extra;
+}
+
+struct ExtFacet {            // punc/include/punc/mesh.h:38-44
+    double area;
+    double vertices[9];
+    double normal[3];        // inward
+    int64_t cell;
+};
+
+struct SpeciesFlux {         // Maxwellian part of punc/include/punc/distributions.h:52-249
+    double q, m, n, vth, vd[3], vdf_range;
+    double vth2, factor;
+    double domain[6];
+    std::vector<double> num_particles, pdf_max;
+};
+
+struct Oracle {
+    int64_t nv = 0, nc = 0, ndof = 0;
+    std::vector<double> coords;
+    std::vector<int64_t> v2d;
+    std::vector<Cell> cells;
+    std::vector<double> dv_inv;
+    std::vector<int64_t> rowptr, col;
+    std::vector<double> K, M;
+    std::vector<ExtFacet> ext;
+    std::vector<double> ofac;   // cell, object, area, n(3), facet
+    std::vector<int64_t> bc_kind;
+    double eps0 = 1.0;
+    // locate acceleration: uniform grid of cell lists
+    double glo[3], gh[3];
+    int gn[3];
+    std::vector<std::vector<int64_t>> grid;
+    std::vector<SpeciesFlux> flux;
+    int64_t next_id = 0;
+};
+
+// ---- setup -------------------------------------------------------------------
+
+int build(Oracle &o, const double *coords, int64_t nv, const int64_t *cells, int64_t nc, const int64_t *bfv,
+          const int32_t *btag, int64_t nb, const int64_t *v2d, int64_t ndof, double eps0) {
+    o.nv = nv; o.nc = nc; o.eps0 = eps0;
+    o.coords.assign(coords, coords + 3 * nv);
+    o.ndof = v2d ? ndof : nv;
+    o.v2d.resize(nv);
+    for (int64_t v = 0; v < nv; ++v) o.v2d[v] = v2d ? v2d[v] : v;
+    std::map<std::array<int64_t, 3>, int32_t> tags;
+    for (int64_t k = 0; k < nb; ++k) {
+        std::array<int64_t, 3> t = {bfv[3 * k], bfv[3 * k + 1], bfv[3 * k + 2]};
+        std::sort(t.begin(), t.end());
+        tags[t] = btag[k];
+    }
+    o.cells.resize(nc);
+    // facets sorted by vertex triple to find neighbours
+    std::vector<std::pair<std::array<int64_t, 3>, int64_t>> fl(4 * nc);
+    for (int64_t c = 0; c < nc; ++c) {
+        Cell &cell = o.cells[c];
+        cell.id = c;
+        int64_t v[4] = {cells[4 * c], cells[4 * c + 1], cells[4 * c + 2], cells[4 * c + 3]};
+        std::sort(v, v + 4);
+        for (int i = 0; i < 4; ++i) {
+            cell.vertices[i] = v[i];
+            cell.dofs[i] = o.v2d[v[i]];
+            for (int j = 0; j < 3; ++j) cell.vertex_coordinates[3 * i + j] = coords[3 * v[i] + j];
+        }
+        cell.init_barycentric_matrix();
+        for (int f = 0; f < 4; ++f) {
+            std::array<int64_t, 3> t;
+            int k = 0;
+            for (int i = 0; i < 4; ++i) if (i != f) t[k++] = v[i];
+            fl[4 * c + f] = {t, 4 * c + f};
+        }
+    }
+    std::sort(fl.begin(), fl.end());
+    std::vector<long> adj(4 * nc, 0);
+    for (size_t k = 0; k < fl.size();) {
+        size_t e = k + 1;
+        while (e < fl.size() && fl[e].first == fl[k].first) ++e;
+        if (e - k == 2) {
+            adj[fl[k].second] = fl[k + 1].second / 4;
+            adj[fl[k + 1].second] = fl[k].second / 4;
+        } else if (e - k == 1) {
+            auto it = tags.find(fl[k].first);
+            if (it == tags.end()) return 3;
+            adj[fl[k].second] = -1 * (long)it->second;
+        } else {
+            return 3;
+        }
+        k = e;
+    }
+    // Population::init_localizer (punc/include/punc/population.h:345-389)
+    for (auto &cell : o.cells) {
+        cell.facet_adjacents.clear();
+        cell.facet_plane_coeffs.clear();
+        for (int i = 0; i < 4; ++i) {
+            cell.facet_adjacents.push_back(adj[4 * cell.id + i]);
+            double dot_product = 0;
+            for (int j = 0; j < 3; ++j) dot_product += cell.facet_midpoint(i)[j] * cell.normal(i)[j];
+            cell.facet_plane_coeffs.push_back(-dot_product);
+            for (int j = 0; j < 3; ++j) cell.facet_plane_coeffs.push_back(cell.normal(i)[j]);
+        }
+        const double *p = cell.vertex_coordinates.data();
+        double a[3], b[3], d[3];
+        for (int j = 0; j < 3; ++j) { a[j] = p[3 + j] - p[j]; b[j] = p[6 + j] - p[j]; d[j] = p[9 + j] - p[j]; }
+        const double det = a[0] * (b[1] * d[2] - b[2] * d[1]) - a[1] * (b[0] * d[2] - b[2] * d[0]) + a[2] * (b[0] * d[1] - b[1] * d[0]);
+        cell.volume = std::fabs(det) / 6.0;
+    }
+    // element_volume (punc/src/distributor.cpp:35-69): per vertex in order, the
+    // volumes of its cells in ascending cell order, into the vertex's dof.
+    {
+        std::vector<std::vector<int64_t>> vc(nv);
+        for (int64_t c = 0; c < nc; ++c)
+            for (int i = 0; i < 4; ++i) vc[o.cells[c].vertices[i]].push_back(c);
+        std::vector<double> volumes(o.ndof, 0.0);
+        for (int64_t v = 0; v < nv; ++v)
+            for (int64_t c : vc[v]) volumes[o.v2d[v]] += o.cells[c].volume;
+        o.dv_inv.resize(o.ndof);
+        for (int64_t i = 0; i < o.ndof; ++i) o.dv_inv[i] = (3 + 1.0) / volumes[i];
+    }
+    // P1 stiffness eps0*grad.grad and consistent mass (punc/ufl/Potential3D.ufl)
+    {
+        struct Entry { int64_t col; double k, m; };
+        std::vector<std::vector<Entry>> rows(o.ndof);
+        for (auto &cell : o.cells) {
+            const double *A = cell.barycentric_matrix;
+            double g[4][3];
+            for (int k = 0; k < 3; ++k) for (int j = 0; j < 3; ++j) g[k][j] = A[4 * k + 1 + j];
+            for (int j = 0; j < 3; ++j) g[3][j] = -(g[0][j] + g[1][j] + g[2][j]);
+            for (int i = 0; i < 4; ++i)
+                for (int j = 0; j < 4; ++j) {
+                    auto &row = rows[cell.dofs[i]];
+                    Entry *e = nullptr;
+                    for (auto &x : row) if (x.col == cell.dofs[j]) { e = &x; break; }
+                    if (!e) { row.push_back(Entry{cell.dofs[j], 0.0, 0.0}); e = &row.back(); }
+                    const double gg = g[i][0] * g[j][0] + g[i][1] * g[j][1] + g[i][2] * g[j][2];
+                    e->k += eps0 * cell.volume * gg;
+                    e->m += cell.volume / 20.0 * (i == j ? 2.0 : 1.0);
+                }
+        }
+        o.rowptr.assign(o.ndof + 1, 0);
+        for (int64_t r = 0; r < o.ndof; ++r) {
+            std::sort(rows[r].begin(), rows[r].end(), [](const Entry &a, const Entry &b) { return a.col < b.col; });
+            for (auto &e : rows[r]) { o.col.push_back(e.col); o.K.push_back(e.k); o.M.push_back(e.m); }
+            o.rowptr[r + 1] = (int64_t)o.col.size();
+        }
+    }
+    // Mesh::exterior_boundaries (punc/src/mesh.cpp:166-236) and object facets
+    o.bc_kind.assign(o.ndof, -1);
+    for (auto &cell : o.cells)
+        for (int f = 0; f < 4; ++f) {
+            const long t = cell.facet_adjacents[f];
+            if (t >= 0) continue;
+            const double *p = cell.vertex_coordinates.data();
+            int q[3], k = 0;
+            for (int i = 0; i < 4; ++i) if (i != f) q[k++] = i;
+            double b[3], d[3];
+            for (int j = 0; j < 3; ++j) { b[j] = p[3 * q[1] + j] - p[3 * q[0] + j]; d[j] = p[3 * q[2] + j] - p[3 * q[0] + j]; }
+            const double cx = b[1] * d[2] - b[2] * d[1], cy = b[2] * d[0] - b[0] * d[2], cz = b[0] * d[1] - b[1] * d[0];
+            const double area = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+            const auto n = cell.normal(f);
+            if (t == -1) {
+                ExtFacet e;
+                e.area = area;
+                for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) e.vertices[3 * i + j] = p[3 * q[i] + j];
+                for (int j = 0; j < 3; ++j) e.normal[j] = -1 * n[j];
+                e.cell = cell.id;
+                o.ext.push_back(e);
+            } else {
+                const double rec[7] = {double(cell.id), double(-t - 2), area, n[0], n[1], n[2], double(f)};
+                o.ofac.insert(o.ofac.end(), rec, rec + 7);
+            }
+        }
+    for (int pass = 0; pass < 2; ++pass)
+        for (auto &cell : o.cells)
+            for (int f = 0; f < 4; ++f) {
+                const long t = cell.facet_adjacents[f];
+                if (t >= 0 || (pass == 0) != (t == -1)) continue;
+                for (int i = 0; i < 4; ++i) if (i != f) o.bc_kind[cell.dofs[i]] = (t == -1) ? 0 : -t - 1;
+            }
+    // locate grid
+    for (int j = 0; j < 3; ++j) { o.glo[j] = 1e300; double hi = -1e300; for (int64_t v = 0; v < nv; ++v) { o.glo[j] = std::min(o.glo[j], coords[3 * v + j]); hi = std::max(hi, coords[3 * v + j]); } o.gn[j] = std::max<int>(1, (int)std::cbrt((double)nc / 6.0)); o.gh[j] = std::max(hi - o.glo[j], 1e-300) / o.gn[j]; }
+    o.grid.assign((size_t)o.gn[0] * o.gn[1] * o.gn[2], {});
+    for (auto &cell : o.cells) {
+        int lo[3], hi[3];
+        for (int j = 0; j < 3; ++j) {
+            double mn = 1e300, mx = -1e300;
+            for (int i = 0; i < 4; ++i) { mn = std::min(mn, cell.vertex_coordinates[3 * i + j]); mx = std::max(mx, cell.vertex_coordinates[3 * i + j]); }
+            lo[j] = std::max(0, std::min(o.gn[j] - 1, (int)std::floor((mn - o.glo[j]) / o.gh[j])));
+            hi[j] = std::max(0, std::min(o.gn[j] - 1, (int)std::floor((mx - o.glo[j]) / o.gh[j])));
+        }
+        for (int a = lo[0]; a <= hi[0]; ++a) for (int b = lo[1]; b <= hi[1]; ++b) for (int e = lo[2]; e <= hi[2]; ++e)
+            o.grid[((size_t)a * o.gn[1] + b) * o.gn[2] + e].push_back(cell.id);
+    }
+    return 0;
+}
+
+// The lowest-index cell whose four plane values are all <= 0, or -1.
+// (Stands in for the BoundingBoxTree query of locate, punc/src/population.cpp:24-39;
+// the two agree for every point strictly inside a cell.)
+long locate(const Oracle &o, const double *x) {
+    int b[3];
+    for (int j = 0; j < 3; ++j) {
+        const double f = std::floor((x[j] - o.glo[j]) / o.gh[j]);
+        if (!(f >= -1.0 && f <= (double)o.gn[j])) return -1;
+        b[j] = f < 0 ? 0 : (f >= o.gn[j] ? o.gn[j] - 1 : (int)f);
+    }
+    const auto &lst = o.grid[((size_t)b[0] * o.gn[1] + b[1]) * o.gn[2] + b[2]];
+    long best = -1;
+    for (int64_t c : lst) {
+        const double *co = o.cells[c].facet_plane_coeffs.data();
+        bool in = true;
+        for (int i = 0; i < 4 && in; ++i) {
+            double proj = co[4 * i];
+            for (int j = 0; j < 3; ++j) proj += co[4 * i + 1 + j] * x[j];
+            if (proj > 0) in = false;
+        }
+        if (in && (best < 0 || c < best)) best = (long)c;
+    }
+    return best;
+}
+
+// Population::relocate_fast (punc/include/punc/population.h:539-569).  The
+// tail recursion is a loop here, with a step limit (LONG_MIN when reached).
+long relocate_fast(const Oracle &o, const double *p, long cell_id) {
+    for (int depth = 0; depth <= 100000; ++depth) {
+        const double *coeffs = o.cells[cell_id].facet_plane_coeffs.data();
+        long next = cell_id;
+        for (int i = 0; i < 4; ++i) {
+            double proj = *coeffs++;
+            for (int j = 0; j < 3; j++) proj += *coeffs++ * p[j];
+            if (proj > 0) { next = o.cells[cell_id].facet_adjacents[i]; break; }
+        }
+        if (next == cell_id || next < 0) return next;
+        cell_id = next;
+    }
+    return LONG_MIN;
+}
+
+// Range split for the threaded variants (cells are the unit of work).
+template <class F>
+void for_cells(int64_t nc, int nthreads, F f) {
+    if (nthreads <= 1) { f(0, nc, 0); return; }
+    std::vector<std::thread> ts;
+    const int64_t chunk = (nc + nthreads - 1) / nthreads;
+    for (int t = 0; t < nthreads; ++t) {
+        const int64_t b = t * chunk, e = std::min(nc, b + chunk);
+        if (b >= e) break;
+        ts.emplace_back([=] { f(b, e, t); });
+    }
+    for (auto &t : ts) t.join();
+}
+
+}  // namespace
+
+extern "C" {
+
+void *or_create(const double *coords, int64_t nv, const int64_t *cells, int64_t nc, const int64_t *bfv,
+                const int32_t *btag, int64_t nb, const int64_t *v2d, int64_t ndof, double eps0, int32_t *status) {
+    Oracle *o = new Oracle;
+    const int rc = build(*o, coords, nv, cells, nc, bfv, btag, nb, v2d, ndof, eps0);
+    if (status) *status = rc;
+    if (rc) { delete o; return nullptr; }
+    return o;
+}
+
+void or_free(void *h) { delete static_cast<Oracle *>(h); }
+
+// Table sizes: 0 bary(12) 1 planes(16) 2 nbr(4) 3 dofs(4) 4 volume 5 dv_inv
+// 6 rowptr 7 col 8 K 9 M 10 ext facets(14) 11 bc_kind 12 obj facets(7) 13 cell vertices(4)
+int64_t or_table_size(void *h, int32_t which) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    switch (which) {
+    case 0: return 12 * o.nc;
+    case 1: return 16 * o.nc;
+    case 2: case 3: case 13: return 4 * o.nc;
+    case 4: return o.nc;
+    case 5: return o.ndof;
+    case 6: return o.ndof + 1;
+    case 7: case 8: case 9: return (int64_t)o.col.size();
+    case 10: return 14 * (int64_t)o.ext.size();
+    case 11: return o.ndof;
+    case 12: return (int64_t)o.ofac.size();
+    }
+    return -1;
+}
+
+void or_table(void *h, int32_t which, void *out) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    double *d = static_cast<double *>(out);
+    int64_t *l = static_cast<int64_t *>(out);
+    for (int64_t c = 0; c < o.nc && which <= 4; ++c) {
+        const Cell &cell = o.cells[c];
+        if (which == 0) for (int k = 0; k < 12; ++k) d[12 * c + k] = cell.barycentric_matrix[k];
+        if (which == 1) for (int k = 0; k < 16; ++k) d[16 * c + k] = cell.facet_plane_coeffs[k];
+        if (which == 2) for (int k = 0; k < 4; ++k) l[4 * c + k] = cell.facet_adjacents[k];
+        if (which == 3) for (int k = 0; k < 4; ++k) l[4 * c + k] = cell.dofs[k];
+        if (which == 4) d[c] = cell.volume;
+    }
+    if (which == 13) for (int64_t c = 0; c < o.nc; ++c) for (int k = 0; k < 4; ++k) l[4 * c + k] = o.cells[c].vertices[k];
+    if (which == 5) std::copy(o.dv_inv.begin(), o.dv_inv.end(), d);
+    if (which == 6) std::copy(o.rowptr.begin(), o.rowptr.end(), l);
+    if (which == 7) std::copy(o.col.begin(), o.col.end(), l);
+    if (which == 8) std::copy(o.K.begin(), o.K.end(), d);
+    if (which == 9) std::copy(o.M.begin(), o.M.end(), d);
+    if (which == 10)
+        for (size_t f = 0; f < o.ext.size(); ++f) {
+            const ExtFacet &e = o.ext[f];
+            d[14 * f] = e.area;
+            for (int k = 0; k < 9; ++k) d[14 * f + 1 + k] = e.vertices[k];
+            for (int k = 0; k < 3; ++k) d[14 * f + 10 + k] = e.normal[k];
+            d[14 * f + 13] = (double)e.cell;
+        }
+    if (which == 11) std::copy(o.bc_kind.begin(), o.bc_kind.end(), l);
+    if (which == 12) std::copy(o.ofac.begin(), o.ofac.end(), d);
+}
+
+void or_locate(void *h, const double *xs, int64_t n, int64_t *out) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    for (int64_t i = 0; i < n; ++i) out[i] = locate(o, xs + 3 * i);
+}
+
+// Population::add_particles(xs, vs, q, m) (punc/include/punc/population.h:411-435);
+// points outside the mesh are dropped.  Ids continue a running counter.
+int64_t or_add_particles(void *h, const double *xs, const double *vs, int64_t n, double q, double m) {
+    Oracle &o = *static_cast<Oracle *>(h);
+    int64_t added = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        const long c = locate(o, xs + 3 * i);
+        if (c >= 0) {
+            Particle p;
+            for (int j = 0; j < 3; ++j) { p.x[j] = xs[3 * i + j]; p.v[j] = vs[3 * i + j]; }
+            p.q = q; p.m = m; p.id = o.next_id + i;
+            o.cells[c].particles.push_back(p);
+            ++added;
+        }
+    }
+    o.next_id += n;
+    return added;
+}
+
+int64_t or_num_particles(void *h) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    int64_t n = 0;
+    for (auto &c : o.cells) n += (int64_t)c.particles.size();
+    return n;
+}
+
+// Particles in storage order (cell by cell, vector order).
+void or_get_particles(void *h, double *x, double *v, double *q, double *m, int64_t *cell, int64_t *id) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    int64_t k = 0;
+    for (auto &c : o.cells)
+        for (auto &p : c.particles) {
+            for (int j = 0; j < 3; ++j) { x[3 * k + j] = p.x[j]; v[3 * k + j] = p.v[j]; }
+            q[k] = p.q; m[k] = p.m; cell[k] = c.id; id[k] = p.id;
+            ++k;
+        }
+}
+
+// Replace all particles (cell given), used to resynchronise with the engine.
+void or_set_particles(void *h, const double *x, const double *v, const double *q, const double *m,
+                      const int64_t *cell, const int64_t *id, int64_t n) {
+    Oracle &o = *static_cast<Oracle *>(h);
+    for (auto &c : o.cells) c.particles.clear();
+    for (int64_t k = 0; k < n; ++k) {
+        Particle p;
+        for (int j = 0; j < 3; ++j) { p.x[j] = x[3 * k + j]; p.v[j] = v[3 * k + j]; }
+        p.q = q[k]; p.m = m[k]; p.id = id[k];
+        o.cells[cell[k]].particles.push_back(p);
+        o.next_id = std::max(o.next_id, id[k] + 1);
+    }
+}
+
+// EFieldDG0 (punc/src/efield.cpp:95-99, punc/ufl/EFieldDG03D.ufl): per cell
+// E = -((phi0-phi3) g0 + (phi1-phi3) g1 + (phi2-phi3) g2) + E0.
+void or_efield_dg0(void *h, const double *phi, const double *E0, double *E) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    for (const Cell &c : o.cells) {
+        const double *A = c.barycentric_matrix;
+        const double p3 = phi[c.dofs[3]];
+        const double a = phi[c.dofs[0]] - p3, b = phi[c.dofs[1]] - p3, e = phi[c.dofs[2]] - p3;
+        for (int d = 0; d < 3; ++d) {
+            const double g = a * A[1 + d] + b * A[5 + d] + e * A[9 + d];
+            E[3 * c.id + d] = -g + (E0 ? E0[d] : 0.0);
+        }
+    }
+}
+
+// boris with a DG0 field and uniform B (punc/include/punc/pusher.h:397-510).
+// The DG0 basis is the unit vectors, so the evaluated field is E[cell].
+double or_boris(void *h, const double *E, const double *B, double dt, int32_t nthreads) {
+    Oracle &o = *static_cast<Oracle *>(h);
+    std::vector<double> part(std::max(1, nthreads), 0.0);
+    for_cells(o.nc, nthreads, [&](int64_t cb, int64_t ce, int t) {
+        double KE = 0.0;
+        double v_minus[3], v_prime[3], v_plus[3], tt[3], s[3];
+        for (int64_t cid = cb; cid < ce; ++cid) {
+            Cell &cell = o.cells[cid];
+            const double *Ei = E + 3 * cid;
+            for (auto &particle : cell.particles) {
+                const double m = particle.m, q = particle.q;
+                const double *vel = particle.v;
+                double t_mag2 = 0.0;
+                for (int i = 0; i < 3; ++i) { tt[i] = std::tan((dt * q / (2.0 * m)) * B[i]); t_mag2 += tt[i] * tt[i]; }
+                for (int i = 0; i < 3; ++i) s[i] = 2 * tt[i] / (1 + t_mag2);
+                for (int i = 0; i < 3; ++i) v_minus[i] = vel[i] + 0.5 * dt * (q / m) * Ei[i];
+                for (int i = 0; i < 3; i++) KE += 0.5 * m * v_minus[i] * v_minus[i];
+                const double c1[3] = {v_minus[1] * tt[2] - v_minus[2] * tt[1], -v_minus[0] * tt[2] + v_minus[2] * tt[0],
+                                      v_minus[0] * tt[1] - v_minus[1] * tt[0]};
+                for (int i = 0; i < 3; ++i) v_prime[i] = v_minus[i] + c1[i];
+                const double c2[3] = {v_prime[1] * s[2] - v_prime[2] * s[1], -v_prime[0] * s[2] + v_prime[2] * s[0],
+                                      v_prime[0] * s[1] - v_prime[1] * s[0]};
+                for (int i = 0; i < 3; ++i) v_plus[i] = v_minus[i] + c2[i];
+                for (int i = 0; i < 3; ++i) particle.v[i] = v_plus[i] + 0.5 * dt * (q / m) * Ei[i];
+            }
+        }
+        part[t] = KE;
+    });
+    double KE = 0.0;
+    for (double p : part) KE += p;
+    return KE;
+}
+
+// accel with a DG0 field (punc/include/punc/pusher.h:66-130).
+double or_accel(void *h, const double *E, double dt, int32_t nthreads) {
+    Oracle &o = *static_cast<Oracle *>(h);
+    std::vector<double> part(std::max(1, nthreads), 0.0);
+    for_cells(o.nc, nthreads, [&](int64_t cb, int64_t ce, int t) {
+        double KE = 0.0;
+        for (int64_t cid = cb; cid < ce; ++cid) {
+            Cell &cell = o.cells[cid];
+            for (auto &particle : cell.particles) {
+                double Ei[3] = {E[3 * cid], E[3 * cid + 1], E[3 * cid + 2]};
+                const double m = particle.m, q = particle.q;
+                const double *vel = particle.v;
+                for (int j = 0; j < 3; j++) {
+                    Ei[j] *= dt * (q / m);
+                    KE += 0.5 * m * vel[j] * (vel[j] + Ei[j]);
+                }
+                for (int j = 0; j < 3; j++) particle.v[j] += Ei[j];
+            }
+        }
+        part[t] = KE;
+    });
+    double KE = 0.0;
+    for (double p : part) KE += p;
+    return KE;
+}
+
+// move / move_periodic (punc/include/punc/pusher.h:648-681).
+void or_move(void *h, double dt, const double *Ld, int32_t nthreads) {
+    Oracle &o = *static_cast<Oracle *>(h);
+    for_cells(o.nc, nthreads, [&](int64_t cb, int64_t ce, int) {
+        for (int64_t cid = cb; cid < ce; ++cid)
+            for (auto &particle : o.cells[cid].particles)
+                for (int j = 0; j < 3; ++j) {
+                    particle.x[j] += dt * particle.v[j];
+                    if (Ld) particle.x[j] -= Ld[j] * std::floor(particle.x[j] / Ld[j]);
+                }
+    });
+}
+
+// Population::update (punc/include/punc/population.h:641-699).  objects:
+// [n][4] = {bnd_id, charge, current, potential}.  With nthreads > 1 the walks
+// of a cell range run in parallel first; the bookkeeping that follows is the
+// reference's sequential pass, so the result is the same.  absorbed (may be
+// NULL): [tag] count of absorbed particles.  Returns 0, or -1 on a walk that
+// exceeded the step limit.
+int32_t or_update(void *h, double *objects, int32_t n_obj, double dt, int32_t nthreads, int64_t *absorbed,
+                  int32_t n_tags) {
+    Oracle &o = *static_cast<Oracle *>(h);
+    for (int k = 0; k < n_obj; ++k) objects[4 * k + 2] = 0;
+    std::vector<std::vector<long>> pre;
+    if (nthreads > 1) {
+        pre.resize(o.nc);
+        for_cells(o.nc, nthreads, [&](int64_t cb, int64_t ce, int) {
+            for (int64_t cid = cb; cid < ce; ++cid) {
+                auto &ps = o.cells[cid].particles;
+                pre[cid].resize(ps.size());
+                for (size_t k = 0; k < ps.size(); ++k) pre[cid][k] = relocate_fast(o, ps[k].x, (long)cid);
+            }
+        });
+    }
+    long new_cell_id;
+    for (long cell_id = 0; cell_id < (long)o.nc; ++cell_id) {
+        std::vector<std::size_t> to_delete;
+        std::size_t num_particles = o.cells[cell_id].particles.size();
+        for (std::size_t p_id = 0; p_id < num_particles; ++p_id) {
+            auto particle = o.cells[cell_id].particles[p_id];
+            // a particle appended by a lower cell was already walked to here
+            if (nthreads > 1 && p_id < pre[cell_id].size()) new_cell_id = pre[cell_id][p_id];
+            else new_cell_id = relocate_fast(o, particle.x, cell_id);
+            if (new_cell_id == LONG_MIN) return -1;
+            if (new_cell_id != cell_id) {
+                to_delete.push_back(p_id);
+                if (new_cell_id >= 0) {
+                    o.cells[new_cell_id].particles.push_back(particle);
+                } else {
+                    if (absorbed && -new_cell_id < n_tags) absorbed[-new_cell_id]++;
+                    for (int k = 0; k < n_obj; ++k)
+                        if ((std::size_t)(-new_cell_id) == (std::size_t)objects[4 * k]) objects[4 * k + 2] += particle.q;
+                }
+            }
+        }
+        std::size_t size_to_delete = to_delete.size();
+        for (std::size_t it = size_to_delete; it-- > 0;) {
+            auto p_id = to_delete[it];
+            o.cells[cell_id].particles[p_id] = o.cells[cell_id].particles.back();
+            o.cells[cell_id].particles.pop_back();
+        }
+    }
+    for (int k = 0; k < n_obj; ++k) {
+        objects[4 * k + 1] += objects[4 * k + 2];
+        objects[4 * k + 2] /= dt;
+    }
+    return 0;
+}
+
+// distribute_cg1 (punc/include/punc/distributor.h:168-210).
+void or_distribute_cg1(void *h, double *rho, int32_t nthreads) {
+    Oracle &o = *static_cast<Oracle *>(h);
+    const int nt = std::max(1, nthreads);
+    std::vector<std::vector<double>> part(nt, std::vector<double>(o.ndof, 0.0));
+    for_cells(o.nc, nt, [&](int64_t cb, int64_t ce, int t) {
+        std::vector<double> &rho0 = part[t];
+        double cell_coords[4];
+        for (int64_t cid = cb; cid < ce; ++cid) {
+            const Cell &cell = o.cells[cid];
+            double accum[4] = {0.0, 0.0, 0.0, 0.0};
+            for (auto &particle : cell.particles) {
+                cell.barycentric(particle.x, cell_coords);
+                for (int i = 0; i < 4; ++i) accum[i] += particle.q * cell_coords[i];
+            }
+            for (int i = 0; i < 4; ++i) rho0[cell.dofs[i]] += accum[i];
+        }
+    });
+    for (int64_t i = 0; i < o.ndof; ++i) {
+        double s = part[0][i];
+        for (int t = 1; t < nt; ++t) s += part[t][i];
+        rho[i] = s * o.dv_inv[i];
+    }
+}
+
+// kinetic_energy (punc/include/punc/diagnostics.h:248-265).
+double or_kinetic_energy(void *h) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    double KE = 0.0;
+    for (auto &cell : o.cells)
+        for (auto &particle : cell.particles)
+            for (int i = 0; i < 3; ++i) KE += 0.5 * particle.m * particle.v[i] * particle.v[i];
+    return KE;
+}
+
+// Image charge per object: sum over object facets of eps0*area*(grad phi . n)
+// (Charge.ufl ds-integral used by CircuitCM::post_solve, punc/src/object_CM.cpp:328-337).
+void or_image_charges(void *h, const double *phi, int32_t n_obj, double *out) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    for (int k = 0; k < n_obj; ++k) out[k] = 0.0;
+    for (size_t f = 0; f < o.ofac.size() / 7; ++f) {
+        const double *r = &o.ofac[7 * f];
+        const Cell &c = o.cells[(int64_t)r[0]];
+        const double *A = c.barycentric_matrix;
+        const double p3 = phi[c.dofs[3]];
+        const double a = phi[c.dofs[0]] - p3, b = phi[c.dofs[1]] - p3, e = phi[c.dofs[2]] - p3;
+        double g[3];
+        for (int d = 0; d < 3; ++d) g[d] = a * A[1 + d] + b * A[5 + d] + e * A[9 + d];
+        const int k = (int)r[1];
+        if (k >= 0 && k < n_obj) out[k] += (o.eps0 * r[2]) * (g[0] * r[3] + g[1] * r[4] + g[2] * r[5]);
+    }
+}
+
+// Jacobi-preconditioned CG on the Dirichlet-eliminated system (the same
+// algorithm the engine runs), for the CPU baseline.  x holds the initial
+// guess and receives the solution.  Returns the iteration count, or -1.
+int32_t or_pcg(void *h, const double *b_in, const int64_t *kind, const double *gval, double *x, double rtol,
+               double atol, int32_t max_iter, int32_t remove_mean, int32_t nthreads) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    const int64_t n = o.ndof;
+    std::vector<double> b(b_in, b_in + n), r(n), z(n), p(n, 0.0), Ap(n), dinv(n, 1.0);
+    const int nt = std::max(1, nthreads);
+    auto matvec = [&](const std::vector<double> &v, std::vector<double> &out) {
+        for_cells(n, nt, [&](int64_t rb, int64_t re, int) {
+            for (int64_t i = rb; i < re; ++i) {
+                if (kind[i] >= 0) { out[i] = v[i]; continue; }
+                double s = 0.0;
+                for (int64_t k = o.rowptr[i]; k < o.rowptr[i + 1]; ++k)
+                    if (kind[o.col[k]] < 0) s += o.K[k] * v[o.col[k]];
+                out[i] = s;
+            }
+        });
+    };
+    for (int64_t i = 0; i < n; ++i) {
+        if (kind[i] >= 0) { x[i] = gval[i]; continue; }
+        for (int64_t k = o.rowptr[i]; k < o.rowptr[i + 1]; ++k)
+            if (o.col[k] == i) dinv[i] = 1.0 / o.K[k];
+    }
+    if (remove_mean) {
+        double s = 0.0;
+        for (double v : b) s += v;
+        for (double &v : b) v -= s / n;
+    }
+    std::vector<double> xv(x, x + n);
+    matvec(xv, Ap);
+    double rz = 0, rr = 0, bb = 0;
+    for (int64_t i = 0; i < n; ++i) { r[i] = b[i] - Ap[i]; z[i] = dinv[i] * r[i]; rz += r[i] * z[i]; rr += r[i] * r[i]; bb += b[i] * b[i]; }
+    const double tol = std::max(rtol * std::sqrt(bb), atol);
+    int it = 0;
+    double beta = 0.0;
+    while (std::sqrt(rr) > tol && it < max_iter) {
+        ++it;
+        for (int64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+        matvec(p, Ap);
+        double pap = 0;
+        for (int64_t i = 0; i < n; ++i) pap += p[i] * Ap[i];
+        if (!(pap > 0)) return -1;
+        const double alpha = rz / pap;
+        double rzn = 0;
+        rr = 0;
+        for (int64_t i = 0; i < n; ++i) { xv[i] += alpha * p[i]; r[i] -= alpha * Ap[i]; z[i] = dinv[i] * r[i]; rzn += r[i] * z[i]; rr += r[i] * r[i]; }
+        beta = rzn / rz;
+        rz = rzn;
+    }
+    if (remove_mean) {
+        double s = 0.0;
+        for (double v : xv) s += v;
+        for (double &v : xv) v -= s / n;
+    }
+    std::copy(xv.begin(), xv.end(), x);
+    return std::sqrt(rr) <= tol ? it : -1;
+}
+
+// b = M rho (full mass matrix, no boundary conditions).
+void or_mass_matvec(void *h, const double *rho, double *b) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    for (int64_t i = 0; i < o.ndof; ++i) {
+        double s = 0.0;
+        for (int64_t k = o.rowptr[i]; k < o.rowptr[i + 1]; ++k) s += o.M[k] * rho[o.col[k]];
+        b[i] = s;
+    }
+}
+
+// create_flux (punc/src/injector.cpp:104-171) with the analytic Maxwellian
+// flux count and maximum (punc/src/distributions.cpp:23-77).  sp: [n][9] =
+// {q, m, n, vth, vd0, vd1, vd2, vdf_range, unused}.
+void or_create_flux(void *h, const double *sp, int32_t n_species) {
+    Oracle &o = *static_cast<Oracle *>(h);
+    o.flux.clear();
+    for (int s = 0; s < n_species; ++s) {
+        SpeciesFlux F;
+        const double *r = sp + 9 * s;
+        F.q = r[0]; F.m = r[1]; F.n = r[2]; F.vth = r[3];
+        for (int c = 0; c < 3; ++c) F.vd[c] = r[4 + c];
+        F.vdf_range = r[7] > 0 ? r[7] : 5.0;
+        F.vth2 = F.vth * F.vth;
+        F.factor = (1.0 / (std::pow(std::sqrt(2. * M_PI * F.vth2), 3)));
+        for (int c = 0; c < 3; ++c) { F.domain[c] = F.vd[c] - F.vdf_range * F.vth; F.domain[c + 3] = F.vd[c] + F.vdf_range * F.vth; }
+        for (auto &e : o.ext) {
+            const double *nv = e.normal;
+            double vdn = 0.0;
+            for (int c = 0; c < 3; ++c) vdn += nv[c] * F.vd[c];
+            const double num = e.area * (F.vth / (std::sqrt(2 * M_PI)) * std::exp(-0.5 * (vdn / F.vth) * (vdn / F.vth)) +
+                                         0.5 * vdn * (1. + std::erf(vdn / (std::sqrt(2) * F.vth))));
+            F.num_particles.push_back(num);
+            double tmp[3];
+            for (int c = 0; c < 3; ++c) tmp[c] = F.vd[c] - 0.5 * nv[c] * vdn + 0.5 * nv[c] * std::sqrt(4 * F.vth2 + vdn * vdn);
+            double vn = 0.0;
+            for (int c = 0; c < 3; ++c) vn += tmp[c] * nv[c];
+            double v_sqrt = 0.0;
+            for (int c = 0; c < 3; ++c) v_sqrt += (tmp[c] - F.vd[c]) * (tmp[c] - F.vd[c]);
+            F.pdf_max.push_back((vn > 0.0) * vn * (F.factor * std::exp(-0.5 * v_sqrt / F.vth2)));
+        }
+        o.flux.push_back(F);
+    }
+}
+
+// inject_particles (punc/include/punc/injector.h:157-232) with one Philox
+// stream per (species, facet).  Species slot s of the flux table is the
+// engine's species id s.  Returns the number kept; counts[s] per species.
+int64_t or_inject(void *h, double dt, uint64_t seed, uint64_t step, int64_t *counts) {
+    Oracle &o = *static_cast<Oracle *>(h);
+    int64_t kept_total = 0;
+    int64_t slot = 0;
+    for (size_t s = 0; s < o.flux.size(); ++s) {
+        SpeciesFlux &F = o.flux[s];
+        int64_t kept = 0;
+        for (size_t j = 0; j < o.ext.size(); ++j) {
+            const ExtFacet &e = o.ext[j];
+            Stream rng(seed, (uint32_t)j, (uint32_t)s, (uint32_t)step);
+            const double N_float = F.num_particles[j] * (F.n * dt);
+            std::size_t N = static_cast<std::size_t>(N_float);
+            if (rng() < (N_float - N)) N += 1;
+            std::vector<double> xs(3 * N), vs(3 * N);
+            // random_facet_points (punc/src/injector.cpp:78-102)
+            for (std::size_t i = 0; i < N; ++i) {
+                double r = rng();
+                for (int c = 0; c < 3; ++c) xs[i * 3 + c] = (1.0 - r) * e.vertices[c] + r * e.vertices[c + 3];
+                r = std::sqrt(rng());
+                for (int c = 0; c < 3; ++c) xs[i * 3 + c] = r * xs[i * 3 + c] + (1.0 - r) * e.vertices[2 * 3 + c];
+            }
+            // rejection_sampler with the flux density (punc/src/injector.cpp:51-76)
+            for (std::size_t i = 0; i < N; ++i) {
+                double tmp[3];
+                for (;;) {
+                    for (int c = 0; c < 3; ++c) tmp[c] = F.domain[c] + (F.domain[c + 3] - F.domain[c]) * rng();
+                    const double u = rng();
+                    double vn = 0.0;
+                    for (int c = 0; c < 3; ++c) vn += tmp[c] * e.normal[c];
+                    double v_sqrt = 0.0;
+                    for (int c = 0; c < 3; ++c) v_sqrt += (tmp[c] - F.vd[c]) * (tmp[c] - F.vd[c]);
+                    const double pdf = (vn > 0.0) * vn * (F.factor * exp_series(-0.5 * v_sqrt / F.vth2));
+                    if (u * F.pdf_max[j] < pdf) break;
+                }
+                for (int c = 0; c < 3; ++c) vs[i * 3 + c] = tmp[c];
+            }
+            // x += r dt v, keep if located: the walk from the facet's cell
+            for (std::size_t i = 0; i < N; ++i) {
+                const double r = rng();
+                double x[3];
+                for (int c = 0; c < 3; ++c) x[c] = xs[i * 3 + c] + r * dt * vs[i * 3 + c];
+                const long cell = relocate_fast(o, x, (long)e.cell);
+                const int64_t id = o.next_id + slot + (int64_t)i;
+                if (cell >= 0) {
+                    Particle p;
+                    for (int c = 0; c < 3; ++c) { p.x[c] = x[c]; p.v[c] = vs[i * 3 + c]; }
+                    p.q = F.q; p.m = F.m; p.id = id;
+                    o.cells[cell].particles.push_back(p);
+                    ++kept;
+                }
+            }
+            slot += (int64_t)N;
+        }
+        if (counts) counts[s] = kept;
+        kept_total += kept;
+    }
+    o.next_id += slot;
+    return kept_total;
+}
+
+int64_t or_n_ext_facets(void *h) { return (int64_t) static_cast<Oracle *>(h)->ext.size(); }
+int64_t or_ndof(void *h) { return static_cast<Oracle *>(h)->ndof; }
+int64_t or_next_id(void *h) { return static_cast<Oracle *>(h)->next_id; }
+void or_set_next_id(void *h, int64_t v) { static_cast<Oracle *>(h)->next_id = v; }
+double or_exp_series(double x) { return exp_series(x); }
+void or_philox_block(const uint32_t *ctr, const uint32_t *key, uint32_t *out) {
+    uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+    Philox::round10(c, key[0], key[1]);
+    for (int i = 0; i < 4; ++i) out[i] = c[i];
+}
+void or_philox_uniforms(uint64_t seed, uint32_t a, uint32_t b, uint32_t c, int64_t n, double *out) {
+    Stream s(seed, a, b, c);
+    for (int64_t i = 0; i < n; ++i) out[i] = s();
+}
+
+}  // extern "C"

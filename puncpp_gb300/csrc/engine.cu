@@ -1,0 +1,1298 @@
+// The pg_sim handle: device-resident mesh, particles, fields and solver,
+// and the C ABI entry points of punc_gpu.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pg_device.cuh"
+#include "pg_internal.h"
+
+using namespace pg;
+
+struct pg_sim {
+    pg_config cfg{};
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    std::vector<void *> allocs;  // mesh and solver buffers (freed at destroy)
+
+    // mesh
+    DevMesh dm{};
+    int32_t nc = 0, ndof = 0, n_obj = 0, n_ext = 0, n_ofac = 0;
+    std::vector<double> ext_facets_h, obj_facets_h;
+    double *d_ext_facets = nullptr, *d_ofacets = nullptr;
+
+    // particles (two buffers for the cell sort)
+    DevParticles P[2]{};
+    int cur = 0;
+    int64_t n_slots = 0, next_pid = 0;
+    int n_species = 0;
+    double q[kMaxSpecies]{}, m[kMaxSpecies]{};
+    double *d_q = nullptr;
+
+    // fields
+    double *rho_acc = nullptr, *rho = nullptr, *phi = nullptr, *b = nullptr;
+    bool rho_valid = false;
+
+    // solver
+    int32_t *A_row = nullptr, *A_col = nullptr, *M_row = nullptr, *M_col = nullptr;
+    double *A_val = nullptr, *A_dinv = nullptr, *M_val = nullptr;
+    int32_t *bc_kind = nullptr;
+    double *bc_value = nullptr, *w_ext = nullptr, *w_obj = nullptr;
+    double *r = nullptr, *z = nullptr, *p0 = nullptr, *p1 = nullptr, *Ap = nullptr, *pcg_part = nullptr;
+    int32_t *pcg_out_i = nullptr;
+    double *pcg_out_d = nullptr;
+    double *obj_pot = nullptr, *image = nullptr;
+    bool has_dirichlet = false;
+    bool phi_valid = false;
+
+    // circuit (capacitance-matrix method)
+    bool circuit_ready = false;
+    std::vector<double> inv_cap, inv_circ, circ_vec;  // n x n, 2n x 2n, 2n
+    std::vector<std::vector<int>> groups;
+    std::vector<std::vector<int>> fixed_voltage;
+    std::vector<pg_source> vsrc, isrc;
+    double circ_dt = 0;
+
+    // injection
+    bool flux_ready = false;
+    int n_inj_species = 0;
+    int inj_sp[kMaxSpecies]{};
+    pg_species inj[kMaxSpecies]{};
+    double *flux_num = nullptr, *pdf_max = nullptr;
+    std::vector<double> flux_num_h;
+    int64_t *inj_counts = nullptr, *inj_offsets = nullptr, *scan_tmp = nullptr;
+    int64_t scan_tmp_n = 0;
+
+    // reductions, state
+    DevState *state = nullptr;
+    DevState *state_h = nullptr;   // pinned
+    double *partials = nullptr, *ke_dev = nullptr;
+    int n_part = 0;
+
+    // sort scratch
+    int64_t *sort_hist = nullptr, *sort_cursor = nullptr;
+
+    // profiling
+    bool profiling = false;
+    std::vector<std::string> stage_names;
+    std::vector<double> stage_ms;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
+    cudaEvent_t user_ev[16]{};
+    int64_t step_count = 0;
+};
+
+namespace {
+
+#define PG_CUDA(call)                                                                          \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail(PG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));      \
+    } while (0)
+
+template <class T>
+int dalloc(pg_sim *s, T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, count * sizeof(T));
+    if (e != cudaSuccess) return fail(PG_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    s->allocs.push_back(q);
+    *p = reinterpret_cast<T *>(q);
+    return PG_OK;
+}
+
+template <class T>
+int upload(pg_sim *s, T **p, const std::vector<T> &h) {
+    int rc = dalloc(s, p, h.size());
+    if (rc) return rc;
+    if (!h.empty()) PG_CUDA(cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return PG_OK;
+}
+
+void free_particles(DevParticles &p) {
+    void *ptrs[] = {p.x, p.y, p.z, p.vx, p.vy, p.vz, p.xf, p.yf, p.zf, p.vxf, p.vyf, p.vzf, p.cell, p.sp, p.pid};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    p = DevParticles{};
+}
+
+int alloc_particles(pg_sim *s, DevParticles &p, int64_t cap) {
+    p = DevParticles{};
+    p.capacity = cap;
+    auto al = [&](void **q, size_t bytes) -> bool { return cudaMalloc(q, bytes) == cudaSuccess; };
+    bool ok = true;
+    const size_t n = (size_t)cap;
+    if (s->cfg.precision == PG_MIXED) {
+        ok &= al((void **)&p.xf, n * 4) && al((void **)&p.yf, n * 4) && al((void **)&p.zf, n * 4);
+        ok &= al((void **)&p.vxf, n * 4) && al((void **)&p.vyf, n * 4) && al((void **)&p.vzf, n * 4);
+    } else {
+        ok &= al((void **)&p.x, n * 8) && al((void **)&p.y, n * 8) && al((void **)&p.z, n * 8);
+        ok &= al((void **)&p.vx, n * 8) && al((void **)&p.vy, n * 8) && al((void **)&p.vz, n * 8);
+    }
+    ok &= al((void **)&p.cell, n * 4) && al((void **)&p.sp, n) && al((void **)&p.pid, n * 8);
+    if (!ok) {
+        free_particles(p);
+        return fail(PG_ERR_CUDA, "cudaMalloc: particle store of " + std::to_string(cap) + " slots");
+    }
+    return PG_OK;
+}
+
+int copy_particles(pg_sim *s, const DevParticles &src, const DevParticles &dst, int64_t n) {
+    if (n <= 0) return PG_OK;
+    auto cp = [&](void *d, const void *q, size_t bytes) {
+        return cudaMemcpyAsync(d, q, bytes, cudaMemcpyDeviceToDevice, s->stream);
+    };
+    if (s->cfg.precision == PG_MIXED) {
+        PG_CUDA(cp(dst.xf, src.xf, n * 4)); PG_CUDA(cp(dst.yf, src.yf, n * 4)); PG_CUDA(cp(dst.zf, src.zf, n * 4));
+        PG_CUDA(cp(dst.vxf, src.vxf, n * 4)); PG_CUDA(cp(dst.vyf, src.vyf, n * 4)); PG_CUDA(cp(dst.vzf, src.vzf, n * 4));
+    } else {
+        PG_CUDA(cp(dst.x, src.x, n * 8)); PG_CUDA(cp(dst.y, src.y, n * 8)); PG_CUDA(cp(dst.z, src.z, n * 8));
+        PG_CUDA(cp(dst.vx, src.vx, n * 8)); PG_CUDA(cp(dst.vy, src.vy, n * 8)); PG_CUDA(cp(dst.vz, src.vz, n * 8));
+    }
+    PG_CUDA(cp(dst.cell, src.cell, n * 4));
+    PG_CUDA(cp(dst.sp, src.sp, n));
+    PG_CUDA(cp(dst.pid, src.pid, n * 8));
+    return PG_OK;
+}
+
+// Grow both particle buffers to hold `need` slots.
+int ensure_capacity(pg_sim *s, int64_t need) {
+    if (need <= s->P[0].capacity) return PG_OK;
+    int64_t cap = std::max<int64_t>(need + need / 2, std::max<int64_t>(2 * s->P[0].capacity, 1 << 16));
+    for (int k = 0; k < 2; ++k) {
+        DevParticles np;
+        int rc = alloc_particles(s, np, cap);
+        if (rc) return rc;
+        if (k == s->cur) {
+            rc = copy_particles(s, s->P[k], np, s->n_slots);
+            if (rc) { free_particles(np); return rc; }
+            PG_CUDA(cudaStreamSynchronize(s->stream));
+        }
+        free_particles(s->P[k]);
+        s->P[k] = np;
+    }
+    return PG_OK;
+}
+
+int check_state(pg_sim *s) {
+    PG_CUDA(cudaMemcpyAsync(s->state_h, s->state, sizeof(DevState), cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    if (s->state_h->err_code != 0) {
+        // report once, then clear the device error word so the handle stays usable
+        const int code = s->state_h->err_code;
+        const int64_t idx = s->state_h->err_index;
+        cudaMemsetAsync(s->state, 0, 2 * sizeof(int64_t), s->stream);
+        cudaStreamSynchronize(s->stream);
+        s->state_h->err_code = 0;
+        s->state_h->err_index = 0;
+        return fail(code, "device error " + std::to_string(code) + " at index " + std::to_string(idx));
+    }
+    return PG_OK;
+}
+
+int species_id(pg_sim *s, double q, double m) {
+    for (int k = 0; k < s->n_species; ++k)
+        if (s->q[k] == q && s->m[k] == m) return k;
+    if (s->n_species >= kMaxSpecies) return -1;
+    const int k = s->n_species++;
+    s->q[k] = q;
+    s->m[k] = m;
+    cudaMemcpyAsync(s->d_q, s->q, sizeof(double) * kMaxSpecies, cudaMemcpyHostToDevice, s->stream);
+    return k;
+}
+
+void stage_begin(pg_sim *s, const char *name, cudaEvent_t *out_end) {
+    *out_end = nullptr;
+    if (!s->profiling) return;
+    int id = -1;
+    for (size_t k = 0; k < s->stage_names.size(); ++k)
+        if (s->stage_names[k] == name) id = (int)k;
+    if (id < 0) {
+        s->stage_names.push_back(name);
+        s->stage_ms.push_back(0.0);
+        id = (int)s->stage_names.size() - 1;
+    }
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s->stream);
+    s->ev_pending.push_back({id, {a, b}});
+    *out_end = b;
+}
+
+void stage_end(pg_sim *s, cudaEvent_t end) {
+    if (end) cudaEventRecord(end, s->stream);
+}
+
+void collect_stages(pg_sim *s) {
+    if (s->ev_pending.empty()) return;
+    cudaStreamSynchronize(s->stream);
+    for (auto &e : s->ev_pending) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e.second.first, e.second.second);
+        s->stage_ms[e.first] += ms;
+        cudaEventDestroy(e.second.first);
+        cudaEventDestroy(e.second.second);
+    }
+    s->ev_pending.clear();
+}
+
+struct StageScope {
+    pg_sim *s;
+    cudaEvent_t end;
+    StageScope(pg_sim *s_, const char *n) : s(s_) { stage_begin(s, n, &end); }
+    ~StageScope() { stage_end(s, end); }
+};
+
+// ---- circuit (capacitance-matrix method) ---------------------------------
+
+// In-place inverse by Gauss-Jordan elimination with partial pivoting.
+bool invert(std::vector<double> &a, int n) {
+    std::vector<double> inv(n * n, 0.0);
+    for (int i = 0; i < n; ++i) inv[i * n + i] = 1.0;
+    for (int c = 0; c < n; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < n; ++r)
+            if (std::fabs(a[r * n + c]) > std::fabs(a[piv * n + c])) piv = r;
+        if (a[piv * n + c] == 0.0) return false;
+        if (piv != c)
+            for (int k = 0; k < n; ++k) { std::swap(a[c * n + k], a[piv * n + k]); std::swap(inv[c * n + k], inv[piv * n + k]); }
+        const double d = a[c * n + c];
+        for (int k = 0; k < n; ++k) { a[c * n + k] /= d; inv[c * n + k] /= d; }
+        for (int r = 0; r < n; ++r) {
+            if (r == c) continue;
+            const double f = a[r * n + c];
+            if (f == 0.0) continue;
+            for (int k = 0; k < n; ++k) { a[r * n + k] -= f * a[c * n + k]; inv[r * n + k] -= f * inv[c * n + k]; }
+        }
+    }
+    a = inv;
+    return true;
+}
+
+// Charge-sharing sets: objects joined by voltage sources
+// (get_charge_sharing_sets, punc/src/object.cpp:80-135).
+void collect_group(std::vector<pg_source> &vs, int node, std::vector<int> &group) {
+    group.push_back(node);
+    size_t i = 0;
+    while (i < vs.size()) {
+        const pg_source v = vs[i];
+        if (v.node_a == node) { vs.erase(vs.begin() + i); collect_group(vs, v.node_b, group); }
+        else if (v.node_b == node) { vs.erase(vs.begin() + i); collect_group(vs, v.node_a, group); }
+        else ++i;
+    }
+}
+
+std::vector<std::vector<int>> charge_sharing_sets(std::vector<pg_source> vs, int n_obj) {
+    std::vector<int> nodes(n_obj);
+    for (int i = 0; i < n_obj; ++i) nodes[i] = i;
+    std::vector<std::vector<int>> groups;
+    while (!vs.empty()) {
+        std::vector<int> g;
+        collect_group(vs, vs[0].node_a, g);
+        groups.push_back(g);
+    }
+    for (auto &g : groups)
+        for (int v : g)
+            if (v != -1) nodes.erase(std::remove(nodes.begin(), nodes.end(), v), nodes.end());
+    groups.erase(std::remove_if(groups.begin(), groups.end(),
+                                [](const std::vector<int> &g) { return std::find(g.begin(), g.end(), -1) != g.end(); }),
+                 groups.end());
+    for (int v : nodes) groups.push_back({v});
+    return groups;
+}
+
+}  // namespace
+
+// ---- solver internals ------------------------------------------------------
+
+static int object_index(const pg_sim *s, int64_t bnd_id) {
+    const int64_t k = bnd_id - 2;
+    return (k >= 0 && k < s->n_obj) ? (int)k : -1;
+}
+
+// One Poisson solve with the given object potentials; rho from s->rho or zero.
+static int poisson_solve_internal(pg_sim *s, const double *pot_h, bool zero_rho, bool use_ext, double rtol,
+                                  double atol, pg_solve_info *acc) {
+    if (s->n_obj > 0) PG_CUDA(cudaMemcpyAsync(s->obj_pot, pot_h, sizeof(double) * s->n_obj, cudaMemcpyHostToDevice, s->stream));
+    if (zero_rho) PG_CUDA(cudaMemsetAsync(s->rho_acc, 0, sizeof(double) * s->ndof, s->stream));
+    launch_rhs(s->dm, s->M_row, s->M_col, s->M_val, zero_rho ? s->rho_acc : s->rho, s->bc_kind, s->bc_value, s->w_ext,
+               s->w_obj, s->obj_pot, s->n_obj, use_ext ? 1 : 0, s->b, s->stream);
+    if (zero_rho) s->rho_valid = false;
+    double *x = s->phi;
+    if (!(s->cfg.pcg_warm_start && s->phi_valid) || zero_rho) PG_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * s->ndof, s->stream));
+    launch_set_bc(s->bc_kind, use_ext ? s->bc_value : nullptr, s->obj_pot, s->ndof, x, s->stream);
+    PcgArgs a{};
+    a.n = s->ndof;
+    a.rowptr = s->A_row; a.col = s->A_col; a.val = s->A_val; a.dinv = s->A_dinv;
+    a.b = s->b; a.x = x; a.r = s->r; a.z = s->z; a.p0 = s->p0; a.p1 = s->p1; a.Ap = s->Ap;
+    a.partials = s->pcg_part;
+    a.rtol = rtol; a.atol = atol;
+    a.max_iter = s->cfg.pcg_max_iter;
+    a.remove_mean = s->cfg.periodic ? 1 : 0;
+    a.out_iter = s->pcg_out_i; a.out_status = s->pcg_out_i + 1;
+    a.out_rr = s->pcg_out_d; a.out_bb = s->pcg_out_d + 1;
+    int e;
+    {
+        StageScope t(s, "pcg");
+        e = launch_pcg(a, s->stream);
+    }
+    if (e) return fail(PG_ERR_CUDA, std::string("cooperative PCG launch: ") + cudaGetErrorString((cudaError_t)e));
+    int32_t oi[2];
+    double od[2];
+    PG_CUDA(cudaMemcpyAsync(oi, s->pcg_out_i, sizeof(oi), cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaMemcpyAsync(od, s->pcg_out_d, sizeof(od), cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    s->phi_valid = true;
+    if (acc) {
+        acc->iterations += oi[0];
+        acc->solves += 1;
+        acc->residual = std::sqrt(od[0]);
+        acc->rhs_norm = std::sqrt(od[1]);
+    }
+    if (oi[1] == 1) return fail(PG_ERR_NOT_CONVERGED, "PCG reached " + std::to_string(oi[0]) + " iterations, ||r|| = " + std::to_string(std::sqrt(od[0])));
+    if (oi[1] == 2) return fail(PG_ERR_NOT_CONVERGED, "PCG breakdown (p.Ap <= 0) at iteration " + std::to_string(oi[0]));
+    return PG_OK;
+}
+
+static int image_charges(pg_sim *s, std::vector<double> &out) {
+    out.assign(s->n_obj, 0.0);
+    if (s->n_obj == 0) return PG_OK;
+    launch_image_charge(s->dm, s->phi, s->d_ofacets, s->n_ofac, s->n_obj, s->cfg.eps0, s->image, s->stream);
+    PG_CUDA(cudaMemcpyAsync(out.data(), s->image, sizeof(double) * s->n_obj, cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    return PG_OK;
+}
+
+static int rho_from_acc(pg_sim *s) {
+    launch_scale(s->rho_acc, s->dm.dv_inv, s->rho, s->ndof, s->stream);
+    return PG_OK;
+}
+
+// Deposit the current particles into rho_acc (zeroed first), then rho.
+static int deposit_all(pg_sim *s) {
+    PG_CUDA(cudaMemsetAsync(s->rho_acc, 0, sizeof(double) * s->ndof, s->stream));
+    if (s->n_slots > 0) launch_deposit(s->dm, s->P[s->cur], s->n_slots, s->d_q, s->rho_acc, s->stream);
+    s->rho_valid = true;
+    return rho_from_acc(s);
+}
+
+// CircuitCM::pre_solve + solve + post_solve + correction solve
+// (punc/src/poisson.cpp:364-376, punc/src/object_CM.cpp:53-60, 275-376).
+static int solve_circuit_internal(pg_sim *s, pg_object *objects, int32_t n_objects, pg_solve_info *info) {
+    const int n = s->n_obj;
+    std::vector<pg_object *> obj(n, nullptr);
+    for (int k = 0; k < n_objects; ++k) {
+        const int i = object_index(s, objects[k].bnd_id);
+        if (i < 0) return fail(PG_ERR_ARG, "object bnd_id " + std::to_string(objects[k].bnd_id) + " is not an object tag");
+        obj[i] = &objects[k];
+    }
+    for (int i = 0; i < n; ++i)
+        if (!obj[i]) return fail(PG_ERR_ARG, "solve_circuit needs every object of the mesh");
+    // pre_solve: current sources, potentials to zero
+    for (auto &src : s->isrc) {
+        const double dQ = src.value * s->circ_dt;
+        if (src.node_a != -1) obj[src.node_a]->charge -= dQ;
+        if (src.node_b != -1) obj[src.node_b]->charge += dQ;
+    }
+    std::vector<double> pot(n, 0.0);
+    for (int i = 0; i < n; ++i) obj[i]->potential = 0.0;
+    int rc = poisson_solve_internal(s, pot.data(), false, true, s->cfg.pcg_rtol, s->cfg.pcg_atol, info);
+    if (rc) return rc;
+    // post_solve
+    std::vector<double> img;
+    rc = image_charges(s, img);
+    if (rc) return rc;
+    std::vector<double> &cv = s->circ_vec;
+    for (auto &g : s->groups) {
+        double col = 0.0;
+        for (int v : g) col += obj[v]->charge;
+        cv[n + g[0]] = col;
+    }
+    for (auto &g : s->groups) {
+        double col = 0.0;
+        for (int v : g) col += s->inv_cap[g[0] * n + v] * img[v];
+        cv[g[0]] = col;
+        for (size_t j = 1; j < g.size(); ++j) {
+            col = 0.0;
+            for (int v : g) col += s->inv_cap[g[j] * n + v] * img[v];
+            cv[n + g[j]] = col;
+        }
+    }
+    for (auto &fv : s->fixed_voltage)
+        for (size_t j = 0; j < fv.size(); ++j) {
+            double col = 0.0;
+            for (size_t k = 0; k < fv.size(); ++k) col += s->inv_cap[fv[j] * n + fv[k]] * img[fv[k]];
+            cv[n + fv[j]] = col;
+        }
+    for (int i = 0; i < n; ++i) {
+        double p = 0.0, c = 0.0;
+        for (int j = 0; j < 2 * n; ++j) p += s->inv_circ[i * 2 * n + j] * cv[j];
+        for (int j = 0; j < 2 * n; ++j) c += s->inv_circ[(n + i) * 2 * n + j] * cv[j];
+        obj[i]->potential = p;
+        obj[i]->charge = c;
+        pot[i] = p;
+    }
+    // correction solve with the new potentials
+    return poisson_solve_internal(s, pot.data(), false, true, s->cfg.pcg_rtol, s->cfg.pcg_atol, info);
+}
+
+static void absorbed_to_objects(pg_sim *s, pg_object *objects, int32_t n_objects, double dt, int64_t *n_absorbed) {
+    int64_t tot = 0;
+    for (int t = 0; t < kMaxTags; ++t)
+        for (int sp = 0; sp < s->n_species; ++sp) tot += s->state_h->absorbed[t][sp];
+    if (n_absorbed) *n_absorbed = tot;
+    for (int k = 0; k < n_objects; ++k) objects[k].current = 0;
+    for (int k = 0; k < n_objects; ++k) {
+        const int64_t tag = objects[k].bnd_id;
+        if (tag <= 0 || tag >= kMaxTags) continue;
+        double cur = 0.0;
+        for (int sp = 0; sp < s->n_species; ++sp) cur += (double)s->state_h->absorbed[tag][sp] * s->q[sp];
+        objects[k].current = cur;
+    }
+    for (int k = 0; k < n_objects; ++k) {
+        objects[k].charge += objects[k].current;
+        objects[k].current /= dt;
+    }
+}
+
+static int do_sort(pg_sim *s) {
+    const int other = 1 - s->cur;
+    PG_CUDA(cudaMemsetAsync(s->sort_hist, 0, sizeof(int64_t) * (s->nc + 1), s->stream));
+    launch_sort_hist(s->P[s->cur], s->n_slots, s->sort_hist, s->stream);
+    launch_scan_i64(s->sort_hist, s->sort_cursor, s->nc + 1, s->scan_tmp, s->stream);
+    int64_t total = 0;
+    PG_CUDA(cudaMemcpyAsync(&total, s->sort_cursor + s->nc, sizeof(int64_t), cudaMemcpyDeviceToHost, s->stream));
+    launch_sort_scatter(s->P[s->cur], s->P[other], s->n_slots, s->sort_cursor, s->stream);
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    s->cur = other;
+    s->n_slots = total;
+    return PG_OK;
+}
+
+static int ensure_scan_tmp(pg_sim *s, int64_t n) {
+    const int64_t need = scan_tmp_size(n);
+    if (need <= s->scan_tmp_n) return PG_OK;
+    if (s->scan_tmp) cudaFree(s->scan_tmp);
+    s->scan_tmp = nullptr;
+    PG_CUDA(cudaMalloc(&s->scan_tmp, sizeof(int64_t) * need));
+    s->scan_tmp_n = need;
+    return PG_OK;
+}
+
+// Injection with optional deposit into rho_acc (fused step).
+static int inject_internal(pg_sim *s, double dt, uint64_t seed, uint64_t step, bool deposit, int64_t *n_inj) {
+    if (!s->flux_ready) return fail(PG_ERR_STATE, "pg_inject: call pg_create_flux first");
+    const int total = s->n_inj_species * s->n_ext;
+    if (total == 0) { if (n_inj) *n_inj = 0; return PG_OK; }
+    InjectParams ip{};
+    ip.n_species = s->n_inj_species;
+    ip.n_facets = s->n_ext;
+    ip.seed = seed;
+    ip.step = (uint32_t)step;
+    ip.dt = dt;
+    int64_t bound = 0;
+    for (int k = 0; k < s->n_inj_species; ++k) {
+        const pg_species &S = s->inj[k];
+        InjectSpecies &I = ip.sp[k];
+        I.ndt = S.n * dt;
+        const double range = S.vdf_range > 0 ? S.vdf_range : 5.0;
+        for (int c = 0; c < 3; ++c) {
+            const double lo = S.vd[c] - range * S.vth, hi = S.vd[c] + range * S.vth;
+            I.domain_lo[c] = lo;
+            I.domain_w[c] = hi - lo;
+            I.vd[c] = S.vd[c];
+        }
+        I.vth2 = S.vth * S.vth;
+        I.factor = 1.0 / std::pow(std::sqrt(2. * M_PI * I.vth2), 3);
+        I.q = S.q;
+        for (int j = 0; j < s->n_ext; ++j) bound += (int64_t)(s->flux_num_h[(size_t)k * s->n_ext + j] * I.ndt) + 1;
+    }
+    int rc = ensure_capacity(s, s->n_slots + bound);
+    if (rc) return rc;
+    rc = ensure_scan_tmp(s, total + 1);
+    if (rc) return rc;
+    // the species slots of the injection table are engine species ids
+    InjectParams ipd = ip;
+    for (int k = 0; k < ip.n_species; ++k) ipd.sp[k] = ip.sp[k];
+    ipd.slot_base = s->n_slots;
+    ipd.pid_base = s->next_pid;
+    PG_CUDA(cudaMemsetAsync(s->inj_counts, 0, sizeof(int64_t) * (total + 1), s->stream));
+    PG_CUDA(cudaMemsetAsync(s->state->injected, 0, sizeof(s->state->injected), s->stream));
+    launch_inject_count(s->dm, ipd, s->flux_num, s->inj_counts, s->stream);
+    launch_scan_i64(s->inj_counts, s->inj_offsets, total + 1, s->scan_tmp, s->stream);
+    launch_inject_generate(s->dm, s->P[s->cur], ipd, s->flux_num, s->pdf_max, s->d_ext_facets, s->inj_offsets,
+                           s->cfg.max_walk_steps, deposit ? 1 : 0, s->d_q, s->rho_acc, s->state, s->stream);
+    rc = check_state(s);
+    if (rc) return rc;
+    const int64_t appended = s->state_h->inject_total;
+    s->n_slots += appended;
+    s->next_pid += appended;
+    int64_t kept = 0;
+    for (int k = 0; k < kMaxSpecies; ++k) kept += s->state_h->injected[k];
+    if (n_inj) *n_inj = kept;
+    return PG_OK;
+}
+
+static void fill_push(const pg_sim *s, PushParams &pp, double dt, const double *B, bool accel) {
+    pp = PushParams{};
+    pp.accel = accel ? 1 : 0;
+    pp.has_B = (!accel && B && (B[0] != 0.0 || B[1] != 0.0 || B[2] != 0.0)) ? 1 : 0;
+    for (int k = 0; k < s->n_species; ++k) {
+        const double q = s->q[k], m = s->m[k];
+        pp.coef[k] = accel ? dt * (q / m) : 0.5 * dt * (q / m);
+        pp.half_m[k] = 0.5 * m;
+        if (pp.has_B) {
+            // t = tan((dt q / 2m) B), s = 2t / (1 + |t|^2) (pusher.h:469-479)
+            double t[3], t2 = 0.0;
+            for (int i = 0; i < 3; ++i) { t[i] = std::tan((dt * q / (2.0 * m)) * B[i]); t2 += t[i] * t[i]; }
+            for (int i = 0; i < 3; ++i) { pp.t[k][i] = t[i]; pp.s[k][i] = 2 * t[i] / (1 + t2); }
+        }
+    }
+}
+
+// ---- C ABI -------------------------------------------------------------------
+
+extern "C" {
+
+int pg_create(const pg_mesh *mesh, const pg_config *cfg_in, pg_sim **out) {
+    if (!mesh || !out) return fail(PG_ERR_ARG, "pg_create: NULL argument");
+    *out = nullptr;
+    const HostMesh &h = mesh->h;
+    if (h.n_objects >= kMaxTags - 2) return fail(PG_ERR_ARG, "pg_create: too many object tags");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(PG_ERR_CUDA, "pg_create: no CUDA device");
+    pg_sim *s = new pg_sim;
+    pg_config cfg = cfg_in ? *cfg_in : pg_config{};
+    if (cfg.eps0 == 0) cfg.eps0 = 1.0;
+    if (cfg.max_walk_steps <= 0) cfg.max_walk_steps = 100000;
+    if (cfg.sort_interval <= 0) cfg.sort_interval = 20;
+    if (cfg.pcg_rtol <= 0) cfg.pcg_rtol = 1e-12;
+    if (cfg.pcg_atol <= 0) cfg.pcg_atol = 1e-14;
+    if (cfg.pcg_max_iter <= 0) cfg.pcg_max_iter = 1000;
+    s->cfg = cfg;
+    auto bail = [&](int rc) { pg_destroy(s); return rc; };
+    cudaGetDevice(&s->device);
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(PG_ERR_CUDA, "cudaStreamCreate failed"));
+    s->nc = (int32_t)h.nc;
+    s->ndof = (int32_t)h.ndof;
+    s->n_obj = h.n_objects;
+
+    // mesh tables
+    std::vector<int32_t> nbr32(4 * h.nc), dof32(4 * h.nc);
+    for (int64_t k = 0; k < 4 * h.nc; ++k) { nbr32[k] = (int32_t)h.nbr[k]; dof32[k] = (int32_t)h.cell_dofs[k]; }
+    double *d_planes, *d_bary, *d_E, *d_dvinv;
+    int32_t *d_nbr, *d_dofs;
+    int rc;
+    if ((rc = upload(s, &d_planes, h.planes)) || (rc = upload(s, &d_bary, h.bary)) || (rc = upload(s, &d_nbr, nbr32)) ||
+        (rc = upload(s, &d_dofs, dof32)) || (rc = upload(s, &d_dvinv, h.dv_inv)) || (rc = dalloc(s, &d_E, 4 * h.nc)))
+        return bail(rc);
+    cudaMemset(d_E, 0, sizeof(double) * 4 * h.nc);
+    s->dm.nc = s->nc;
+    s->dm.ndof = s->ndof;
+    s->dm.planes = d_planes;
+    s->dm.bary = d_bary;
+    s->dm.nbr = reinterpret_cast<const int4 *>(d_nbr);
+    s->dm.dofs = reinterpret_cast<const int4 *>(d_dofs);
+    s->dm.E = d_E;
+    s->dm.dv_inv = d_dvinv;
+    for (int j = 0; j < 3; ++j) { s->dm.lo[j] = h.bbox_lo[j]; s->dm.bin_h[j] = h.bin_h[j]; s->dm.nbin[j] = h.nbin[j]; }
+    int64_t *d_binptr;
+    int32_t *d_bincells;
+    if ((rc = upload(s, &d_binptr, h.bin_ptr)) || (rc = upload(s, &d_bincells, h.bin_cells))) return bail(rc);
+    s->dm.bin_ptr = d_binptr;
+    s->dm.bin_cells = d_bincells;
+
+    // fields
+    if ((rc = dalloc(s, &s->rho_acc, h.ndof)) || (rc = dalloc(s, &s->rho, h.ndof)) || (rc = dalloc(s, &s->phi, h.ndof)) ||
+        (rc = dalloc(s, &s->b, h.ndof)))
+        return bail(rc);
+    cudaMemset(s->rho_acc, 0, sizeof(double) * h.ndof);
+    cudaMemset(s->rho, 0, sizeof(double) * h.ndof);
+    cudaMemset(s->phi, 0, sizeof(double) * h.ndof);
+
+    // Poisson: symmetric elimination of Dirichlet rows and columns.
+    {
+        const int64_t nd = h.ndof;
+        std::vector<int32_t> kind(nd);
+        s->has_dirichlet = false;
+        for (int64_t i = 0; i < nd; ++i) {
+            kind[i] = cfg.periodic ? -1 : (int32_t)h.bc_kind[i];
+            if (kind[i] >= 0) s->has_dirichlet = true;
+        }
+        std::vector<double> gval(nd, 0.0);
+        if (!cfg.periodic) {
+            for (int64_t c = 0; c < h.nc; ++c)
+                for (int i = 0; i < 4; ++i) {
+                    const int64_t v = h.cell_vertices[4 * c + i], d = h.cell_dofs[4 * c + i];
+                    double val = 0.0;
+                    for (int j = 0; j < 3; ++j) val += h.coords[3 * v + j] * cfg.ext_E[j];
+                    gval[d] = val;
+                }
+        }
+        std::vector<int32_t> arow(nd + 1, 0), acol, mrow(nd + 1), mcol(h.col.size());
+        std::vector<double> aval, dinv(nd, 1.0), wext(nd, 0.0), wobj((size_t)std::max(1, s->n_obj) * nd, 0.0);
+        acol.reserve(h.col.size());
+        aval.reserve(h.col.size());
+        for (int64_t i = 0; i < nd; ++i) {
+            if (kind[i] >= 0) {
+                acol.push_back((int32_t)i);
+                aval.push_back(1.0);
+            } else {
+                for (int64_t k = h.rowptr[i]; k < h.rowptr[i + 1]; ++k) {
+                    const int64_t j = h.col[k];
+                    if (kind[j] < 0) {
+                        acol.push_back((int32_t)j);
+                        aval.push_back(h.K[k]);
+                        if (j == i) dinv[i] = 1.0 / h.K[k];
+                    } else if (kind[j] == 0) {
+                        wext[i] += h.K[k] * gval[j];
+                    } else {
+                        wobj[(size_t)(kind[j] - 1) * nd + i] += h.K[k];
+                    }
+                }
+            }
+            arow[i + 1] = (int32_t)acol.size();
+        }
+        for (int64_t i = 0; i <= nd; ++i) mrow[i] = (int32_t)h.rowptr[i];
+        for (size_t k = 0; k < h.col.size(); ++k) mcol[k] = (int32_t)h.col[k];
+        if ((rc = upload(s, &s->A_row, arow)) || (rc = upload(s, &s->A_col, acol)) || (rc = upload(s, &s->A_val, aval)) ||
+            (rc = upload(s, &s->A_dinv, dinv)) || (rc = upload(s, &s->M_row, mrow)) || (rc = upload(s, &s->M_col, mcol)) ||
+            (rc = upload(s, &s->M_val, h.M)) || (rc = upload(s, &s->bc_kind, kind)) || (rc = upload(s, &s->bc_value, gval)) ||
+            (rc = upload(s, &s->w_ext, wext)) || (rc = upload(s, &s->w_obj, wobj)))
+            return bail(rc);
+        const int nb = pcg_grid_blocks();
+        if ((rc = dalloc(s, &s->r, nd)) || (rc = dalloc(s, &s->z, nd)) || (rc = dalloc(s, &s->p0, nd)) ||
+            (rc = dalloc(s, &s->p1, nd)) || (rc = dalloc(s, &s->Ap, nd)) || (rc = dalloc(s, &s->pcg_part, 4 * nb)) ||
+            (rc = dalloc(s, &s->pcg_out_i, 2)) || (rc = dalloc(s, &s->pcg_out_d, 2)) ||
+            (rc = dalloc(s, &s->obj_pot, std::max(1, s->n_obj))) || (rc = dalloc(s, &s->image, std::max(1, s->n_obj))))
+            return bail(rc);
+    }
+
+    // boundary facets
+    s->ext_facets_h = h.ext_facets;
+    s->obj_facets_h = h.obj_facets;
+    s->n_ext = (int32_t)(h.ext_facets.size() / 14);
+    s->n_ofac = (int32_t)(h.obj_facets.size() / 7);
+    if ((rc = upload(s, &s->d_ext_facets, h.ext_facets)) || (rc = upload(s, &s->d_ofacets, h.obj_facets))) return bail(rc);
+
+    // state, reductions, sort scratch
+    if ((rc = dalloc(s, &s->state, 1))) return bail(rc);
+    cudaMemset(s->state, 0, sizeof(DevState));
+    if (cudaMallocHost(&s->state_h, sizeof(DevState)) != cudaSuccess) return bail(fail(PG_ERR_CUDA, "cudaMallocHost failed"));
+    std::memset(s->state_h, 0, sizeof(DevState));
+    s->n_part = sm_count() * 8;
+    if ((rc = dalloc(s, &s->partials, s->n_part)) || (rc = dalloc(s, &s->ke_dev, 1)) || (rc = dalloc(s, &s->d_q, kMaxSpecies)))
+        return bail(rc);
+    cudaMemset(s->d_q, 0, sizeof(double) * kMaxSpecies);
+    if ((rc = dalloc(s, &s->sort_hist, h.nc + 1)) || (rc = dalloc(s, &s->sort_cursor, h.nc + 1))) return bail(rc);
+    if ((rc = ensure_scan_tmp(s, h.nc + 1))) return bail(rc);
+    if (cfg.particle_capacity > 0) {
+        if ((rc = alloc_particles(s, s->P[0], cfg.particle_capacity)) || (rc = alloc_particles(s, s->P[1], cfg.particle_capacity)))
+            return bail(rc);
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess) return bail(fail(PG_ERR_CUDA, "pg_create: device error during upload"));
+    *out = s;
+    return PG_OK;
+}
+
+int pg_destroy(pg_sim *s) {
+    if (!s) return PG_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (void *p : s->allocs) cudaFree(p);
+    free_particles(s->P[0]);
+    free_particles(s->P[1]);
+    if (s->flux_num) cudaFree(s->flux_num);
+    if (s->pdf_max) cudaFree(s->pdf_max);
+    if (s->inj_counts) cudaFree(s->inj_counts);
+    if (s->inj_offsets) cudaFree(s->inj_offsets);
+    if (s->scan_tmp) cudaFree(s->scan_tmp);
+    if (s->state_h) cudaFreeHost(s->state_h);
+    for (auto &e : s->ev_pending) { cudaEventDestroy(e.second.first); cudaEventDestroy(e.second.second); }
+    for (auto &e : s->user_ev)
+        if (e) cudaEventDestroy(e);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return PG_OK;
+}
+
+int pg_status_detail(pg_sim *s, int32_t *code, int64_t *index) {
+    if (!s) return fail(PG_ERR_ARG, "NULL handle");
+    PG_CUDA(cudaMemcpyAsync(s->state_h, s->state, sizeof(DevState), cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    if (code) *code = s->state_h->err_code;
+    if (index) *index = s->state_h->err_index;
+    return PG_OK;
+}
+
+int pg_add_particles(pg_sim *s, const double *xs, const double *vs, int64_t n, double q, double m, int64_t *n_added) {
+    if (!s || (n > 0 && (!xs || !vs)) || n < 0) return fail(PG_ERR_ARG, "pg_add_particles: bad arguments");
+    if (n_added) *n_added = 0;
+    if (n == 0) return PG_OK;
+    if (s->cfg.precision == PG_MIXED) return fail(PG_ERR_STATE, "pg_add_particles: the mixed form is not built yet");
+    const int sp = species_id(s, q, m);
+    if (sp < 0) return fail(PG_ERR_ARG, "pg_add_particles: more than 8 species");
+    double *d_xyz = nullptr;
+    int32_t *d_cells = nullptr;
+    PG_CUDA(cudaMalloc(&d_xyz, sizeof(double) * 3 * n));
+    PG_CUDA(cudaMalloc(&d_cells, sizeof(int32_t) * n));
+    std::vector<int32_t> cells(n);
+    cudaMemcpyAsync(d_xyz, xs, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->stream);
+    launch_locate(s->dm, d_xyz, n, d_cells, s->stream);
+    cudaMemcpyAsync(cells.data(), d_cells, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s->stream);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    cudaFree(d_xyz);
+    cudaFree(d_cells);
+    if (e != cudaSuccess) return fail(PG_ERR_CUDA, std::string("pg_add_particles: ") + cudaGetErrorString(e));
+    std::vector<double> hx, hy, hz, hvx, hvy, hvz;
+    std::vector<int32_t> hc;
+    std::vector<uint8_t> hs;
+    std::vector<int64_t> hp;
+    for (int64_t i = 0; i < n; ++i) {
+        if (cells[i] < 0) continue;
+        hx.push_back(xs[3 * i]); hy.push_back(xs[3 * i + 1]); hz.push_back(xs[3 * i + 2]);
+        hvx.push_back(vs[3 * i]); hvy.push_back(vs[3 * i + 1]); hvz.push_back(vs[3 * i + 2]);
+        hc.push_back(cells[i]);
+        hs.push_back((uint8_t)sp);
+        hp.push_back(s->next_pid + i);
+    }
+    const int64_t k = (int64_t)hx.size();
+    int rc = ensure_capacity(s, s->n_slots + k);
+    if (rc) return rc;
+    const DevParticles &P = s->P[s->cur];
+    const int64_t o = s->n_slots;
+    PG_CUDA(cudaMemcpy(P.x + o, hx.data(), 8 * k, cudaMemcpyHostToDevice));
+    PG_CUDA(cudaMemcpy(P.y + o, hy.data(), 8 * k, cudaMemcpyHostToDevice));
+    PG_CUDA(cudaMemcpy(P.z + o, hz.data(), 8 * k, cudaMemcpyHostToDevice));
+    PG_CUDA(cudaMemcpy(P.vx + o, hvx.data(), 8 * k, cudaMemcpyHostToDevice));
+    PG_CUDA(cudaMemcpy(P.vy + o, hvy.data(), 8 * k, cudaMemcpyHostToDevice));
+    PG_CUDA(cudaMemcpy(P.vz + o, hvz.data(), 8 * k, cudaMemcpyHostToDevice));
+    PG_CUDA(cudaMemcpy(P.cell + o, hc.data(), 4 * k, cudaMemcpyHostToDevice));
+    PG_CUDA(cudaMemcpy(P.sp + o, hs.data(), k, cudaMemcpyHostToDevice));
+    PG_CUDA(cudaMemcpy(P.pid + o, hp.data(), 8 * k, cudaMemcpyHostToDevice));
+    s->n_slots += k;
+    s->next_pid += n;
+    // live count
+    PG_CUDA(cudaMemcpy(s->state_h, s->state, sizeof(DevState), cudaMemcpyDeviceToHost));
+    s->state_h->live[sp] += k;
+    PG_CUDA(cudaMemcpy(s->state, s->state_h, sizeof(DevState), cudaMemcpyHostToDevice));
+    s->rho_valid = false;
+    if (n_added) *n_added = k;
+    return PG_OK;
+}
+
+int pg_num_particles(pg_sim *s, int64_t *total, int64_t *neg, int64_t *pos) {
+    if (!s) return fail(PG_ERR_ARG, "NULL handle");
+    int rc = check_state(s);
+    if (rc) return rc;
+    int64_t t = 0, ng = 0, ps = 0;
+    for (int k = 0; k < s->n_species; ++k) {
+        t += s->state_h->live[k];
+        if (s->q[k] < 0) ng += s->state_h->live[k];
+        if (s->q[k] > 0) ps += s->state_h->live[k];
+    }
+    if (total) *total = t;
+    if (neg) *neg = ng;
+    if (pos) *pos = ps;
+    return PG_OK;
+}
+
+int pg_get_particles(pg_sim *s, int64_t capacity, double *x, double *v, double *q, double *m, int64_t *cell,
+                     int64_t *pid, int64_t *n_out) {
+    if (!s || !n_out) return fail(PG_ERR_ARG, "pg_get_particles: NULL argument");
+    const int64_t n = s->n_slots;
+    const DevParticles &P = s->P[s->cur];
+    std::vector<double> hx(n), hy(n), hz(n), hvx(n), hvy(n), hvz(n);
+    std::vector<int32_t> hc(n);
+    std::vector<uint8_t> hs(n);
+    std::vector<int64_t> hp(n);
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    if (n > 0) {
+        PG_CUDA(cudaMemcpy(hx.data(), P.x, 8 * n, cudaMemcpyDeviceToHost));
+        PG_CUDA(cudaMemcpy(hy.data(), P.y, 8 * n, cudaMemcpyDeviceToHost));
+        PG_CUDA(cudaMemcpy(hz.data(), P.z, 8 * n, cudaMemcpyDeviceToHost));
+        PG_CUDA(cudaMemcpy(hvx.data(), P.vx, 8 * n, cudaMemcpyDeviceToHost));
+        PG_CUDA(cudaMemcpy(hvy.data(), P.vy, 8 * n, cudaMemcpyDeviceToHost));
+        PG_CUDA(cudaMemcpy(hvz.data(), P.vz, 8 * n, cudaMemcpyDeviceToHost));
+        PG_CUDA(cudaMemcpy(hc.data(), P.cell, 4 * n, cudaMemcpyDeviceToHost));
+        PG_CUDA(cudaMemcpy(hs.data(), P.sp, n, cudaMemcpyDeviceToHost));
+        PG_CUDA(cudaMemcpy(hp.data(), P.pid, 8 * n, cudaMemcpyDeviceToHost));
+    }
+    std::vector<int64_t> idx;
+    idx.reserve(n);
+    for (int64_t i = 0; i < n; ++i)
+        if (hc[i] >= 0) idx.push_back(i);
+    std::sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) { return hc[a] != hc[b] ? hc[a] < hc[b] : hp[a] < hp[b]; });
+    const int64_t k = (int64_t)idx.size();
+    *n_out = k;
+    if (k > capacity && (x || v || q || m || cell || pid)) return fail(PG_ERR_ARG, "pg_get_particles: capacity too small");
+    for (int64_t t = 0; t < k; ++t) {
+        const int64_t i = idx[t];
+        if (x) { x[3 * t] = hx[i]; x[3 * t + 1] = hy[i]; x[3 * t + 2] = hz[i]; }
+        if (v) { v[3 * t] = hvx[i]; v[3 * t + 1] = hvy[i]; v[3 * t + 2] = hvz[i]; }
+        if (q) q[t] = s->q[hs[i]];
+        if (m) m[t] = s->m[hs[i]];
+        if (cell) cell[t] = hc[i];
+        if (pid) pid[t] = hp[i];
+    }
+    return PG_OK;
+}
+
+int pg_locate(pg_sim *s, const double *xs, int64_t n, int64_t *cells) {
+    if (!s || (n > 0 && (!xs || !cells)) || n < 0) return fail(PG_ERR_ARG, "pg_locate: bad arguments");
+    if (n == 0) return PG_OK;
+    double *d_xyz = nullptr;
+    int32_t *d_cells = nullptr;
+    PG_CUDA(cudaMalloc(&d_xyz, sizeof(double) * 3 * n));
+    PG_CUDA(cudaMalloc(&d_cells, sizeof(int32_t) * n));
+    std::vector<int32_t> c(n);
+    cudaMemcpyAsync(d_xyz, xs, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->stream);
+    launch_locate(s->dm, d_xyz, n, d_cells, s->stream);
+    cudaMemcpyAsync(c.data(), d_cells, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s->stream);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    cudaFree(d_xyz);
+    cudaFree(d_cells);
+    if (e != cudaSuccess) return fail(PG_ERR_CUDA, std::string("pg_locate: ") + cudaGetErrorString(e));
+    for (int64_t i = 0; i < n; ++i) cells[i] = c[i];
+    return PG_OK;
+}
+
+int pg_efield_dg0(pg_sim *s, const double *phi) {
+    if (!s) return fail(PG_ERR_ARG, "NULL handle");
+    if (phi) {
+        PG_CUDA(cudaMemcpyAsync(s->phi, phi, sizeof(double) * s->ndof, cudaMemcpyHostToDevice, s->stream));
+        s->phi_valid = true;
+    }
+    const double E0[3] = {0, 0, 0};
+    launch_efield(s->dm, s->phi, E0, s->stream);
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    return PG_OK;
+}
+
+int pg_set_efield(pg_sim *s, const double *E) {
+    if (!s || !E) return fail(PG_ERR_ARG, "pg_set_efield: NULL argument");
+    std::vector<double> e4(4 * (size_t)s->nc, 0.0);
+    for (int64_t c = 0; c < s->nc; ++c)
+        for (int j = 0; j < 3; ++j) e4[4 * c + j] = E[3 * c + j];
+    PG_CUDA(cudaMemcpy(s->dm.E, e4.data(), sizeof(double) * e4.size(), cudaMemcpyHostToDevice));
+    return PG_OK;
+}
+
+int pg_get_efield(pg_sim *s, double *E) {
+    if (!s || !E) return fail(PG_ERR_ARG, "pg_get_efield: NULL argument");
+    std::vector<double> e4(4 * (size_t)s->nc);
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    PG_CUDA(cudaMemcpy(e4.data(), s->dm.E, sizeof(double) * e4.size(), cudaMemcpyDeviceToHost));
+    for (int64_t c = 0; c < s->nc; ++c)
+        for (int j = 0; j < 3; ++j) E[3 * c + j] = e4[4 * c + j];
+    return PG_OK;
+}
+
+static int push_common(pg_sim *s, const double *B, double dt, bool accel, double *KE) {
+    if (!s) return fail(PG_ERR_ARG, "NULL handle");
+    PushParams pp;
+    fill_push(s, pp, dt, B, accel);
+    if (s->n_slots > 0) {
+        launch_push(s->dm, s->P[s->cur], s->n_slots, pp, s->partials, s->n_part, s->ke_dev, s->stream);
+        double ke = 0;
+        PG_CUDA(cudaMemcpyAsync(&ke, s->ke_dev, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        PG_CUDA(cudaStreamSynchronize(s->stream));
+        if (KE) *KE = ke;
+    } else if (KE) {
+        *KE = 0.0;
+    }
+    return PG_OK;
+}
+
+int pg_accel(pg_sim *s, double dt, double *KE) { return push_common(s, nullptr, dt, true, KE); }
+int pg_boris(pg_sim *s, const double B[3], double dt, double *KE) { return push_common(s, B, dt, false, KE); }
+
+int pg_move(pg_sim *s, double dt) {
+    if (!s) return fail(PG_ERR_ARG, "NULL handle");
+    MoveParams mp{};
+    mp.dt = dt;
+    if (s->n_slots > 0) launch_move(s->P[s->cur], s->n_slots, mp, s->stream);
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    s->rho_valid = false;
+    return PG_OK;
+}
+
+int pg_move_periodic(pg_sim *s, double dt, const double Ld[3]) {
+    if (!s || !Ld) return fail(PG_ERR_ARG, "pg_move_periodic: NULL argument");
+    MoveParams mp{};
+    mp.dt = dt;
+    mp.periodic = 1;
+    for (int j = 0; j < 3; ++j) mp.Ld[j] = Ld[j];
+    if (s->n_slots > 0) launch_move(s->P[s->cur], s->n_slots, mp, s->stream);
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    s->rho_valid = false;
+    return PG_OK;
+}
+
+int pg_update(pg_sim *s, pg_object *objects, int32_t n_objects, double dt) {
+    if (!s || (n_objects > 0 && !objects)) return fail(PG_ERR_ARG, "pg_update: bad arguments");
+    PG_CUDA(cudaMemsetAsync(s->state->absorbed, 0, sizeof(s->state->absorbed), s->stream));
+    if (s->n_slots > 0) launch_update(s->dm, s->P[s->cur], s->n_slots, s->cfg.max_walk_steps, s->state, s->stream);
+    int rc = check_state(s);
+    s->rho_valid = false;
+    if (rc) return rc;
+    absorbed_to_objects(s, objects, n_objects, dt, nullptr);
+    return PG_OK;
+}
+
+int pg_kinetic_energy(pg_sim *s, double *KE) {
+    if (!s || !KE) return fail(PG_ERR_ARG, "pg_kinetic_energy: NULL argument");
+    double hm[kMaxSpecies] = {0};
+    for (int k = 0; k < s->n_species; ++k) hm[k] = 0.5 * s->m[k];
+    *KE = 0.0;
+    if (s->n_slots == 0) return PG_OK;
+    launch_kinetic(s->P[s->cur], s->n_slots, hm, s->partials, s->n_part, s->ke_dev, s->stream);
+    PG_CUDA(cudaMemcpyAsync(KE, s->ke_dev, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    return PG_OK;
+}
+
+int pg_distribute_cg1(pg_sim *s, double *rho) {
+    if (!s) return fail(PG_ERR_ARG, "NULL handle");
+    int rc = deposit_all(s);
+    if (rc) return rc;
+    if (rho) PG_CUDA(cudaMemcpyAsync(rho, s->rho, sizeof(double) * s->ndof, cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    return PG_OK;
+}
+
+int pg_set_rho(pg_sim *s, const double *rho) {
+    if (!s || !rho) return fail(PG_ERR_ARG, "pg_set_rho: NULL argument");
+    PG_CUDA(cudaMemcpy(s->rho, rho, sizeof(double) * s->ndof, cudaMemcpyHostToDevice));
+    s->rho_valid = false;
+    return PG_OK;
+}
+
+int pg_get_rho(pg_sim *s, double *rho) {
+    if (!s || !rho) return fail(PG_ERR_ARG, "pg_get_rho: NULL argument");
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    PG_CUDA(cudaMemcpy(rho, s->rho, sizeof(double) * s->ndof, cudaMemcpyDeviceToHost));
+    return PG_OK;
+}
+
+int pg_get_phi(pg_sim *s, double *phi) {
+    if (!s || !phi) return fail(PG_ERR_ARG, "pg_get_phi: NULL argument");
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    PG_CUDA(cudaMemcpy(phi, s->phi, sizeof(double) * s->ndof, cudaMemcpyDeviceToHost));
+    return PG_OK;
+}
+
+int pg_poisson_solve(pg_sim *s, const pg_object *objects, int32_t n_objects, double *phi, pg_solve_info *info) {
+    if (!s || (n_objects > 0 && !objects)) return fail(PG_ERR_ARG, "pg_poisson_solve: bad arguments");
+    std::vector<double> pot(std::max(1, s->n_obj), 0.0);
+    for (int k = 0; k < n_objects; ++k) {
+        const int i = object_index(s, objects[k].bnd_id);
+        if (i < 0) return fail(PG_ERR_ARG, "object bnd_id is not an object tag");
+        pot[i] = objects[k].potential;
+    }
+    pg_solve_info acc{};
+    int rc = poisson_solve_internal(s, pot.data(), false, true, s->cfg.pcg_rtol, s->cfg.pcg_atol, &acc);
+    if (info) *info = acc;
+    if (rc) return rc;
+    if (phi) return pg_get_phi(s, phi);
+    return PG_OK;
+}
+
+int pg_circuit_cm_setup(pg_sim *s, const pg_source *vs, int32_t nvs, const pg_source *is, int32_t nis, double dt) {
+    if (!s || (nvs > 0 && !vs) || (nis > 0 && !is)) return fail(PG_ERR_ARG, "pg_circuit_cm_setup: bad arguments");
+    const int n = s->n_obj;
+    if (n == 0) return fail(PG_ERR_STATE, "pg_circuit_cm_setup: the mesh has no objects");
+    for (int k = 0; k < nvs; ++k)
+        if (vs[k].node_b < 0 || vs[k].node_b >= n || vs[k].node_a < -1 || vs[k].node_a >= n)
+            return fail(PG_ERR_ARG, "voltage source node out of range");
+    for (int k = 0; k < nis; ++k)
+        if (is[k].node_b < -1 || is[k].node_b >= n || is[k].node_a < -1 || is[k].node_a >= n)
+            return fail(PG_ERR_ARG, "current source node out of range");
+    s->vsrc.assign(vs, vs + nvs);
+    s->isrc.assign(is, is + nis);
+    s->circ_dt = dt;
+    // capacitance matrix: one Laplace solve per object (inv_capacitance,
+    // punc/src/object_CM.cpp:62-106 and laplace_solver 401-437).
+    std::vector<double> cap(n * n, 0.0);
+    for (int j = 0; j < n; ++j) {
+        std::vector<double> pot(n, 0.0);
+        pot[j] = 1.0;
+        int rc = poisson_solve_internal(s, pot.data(), true, false, 1e-12, 1e-14, nullptr);
+        if (rc) return rc;
+        std::vector<double> img;
+        rc = image_charges(s, img);
+        if (rc) return rc;
+        for (int i = 0; i < n; ++i) cap[i * n + j] = img[i];
+    }
+    s->phi_valid = false;
+    s->inv_cap = cap;
+    if (!invert(s->inv_cap, n)) return fail(PG_ERR_SINGULAR, "capacitance matrix is singular");
+    // circuit matrix (CircuitCM::CircuitCM and assemble_matrix, object_CM.cpp:135-273)
+    s->groups = charge_sharing_sets(s->vsrc, n);
+    s->fixed_voltage.clear();
+    for (size_t i = 0; i < s->vsrc.size(); ++i) {
+        if (s->vsrc[i].node_a == -1) {
+            std::vector<int> tmp{s->vsrc[i].node_b};
+            int node = s->vsrc[i].node_b;
+            for (size_t j = 0; j < s->vsrc.size(); ++j)
+                if (s->vsrc[j].node_a == node) { tmp.push_back(s->vsrc[j].node_b); node = s->vsrc[j].node_b; }
+            s->fixed_voltage.push_back(tmp);
+        }
+    }
+    s->circ_vec.assign(2 * n, 0.0);
+    for (auto &v : s->vsrc) s->circ_vec[v.node_b] = v.value;
+    std::vector<double> cm(4 * n * n, 0.0);
+    auto C = [&](int r, int c) -> double & { return cm[r * 2 * n + c]; };
+    auto IC = [&](int r, int c) { return s->inv_cap[r * n + c]; };
+    for (auto &v : s->vsrc) {
+        C(v.node_b, v.node_b) = 1.0;
+        if (v.node_a != -1) C(v.node_b, v.node_a) = -1.0;
+    }
+    for (auto &g : s->groups) {
+        for (int v : g) C(n + g[0], n + v) = 1.0;
+        C(g[0], g[0]) = 1.0;
+        for (int v : g) C(g[0], n + v) = -1.0 * IC(g[0], v);
+        for (size_t j = 1; j < g.size(); ++j) {
+            C(n + g[j], g[j]) = 1.0;
+            for (int v : g) C(n + g[j], n + v) = -1.0 * IC(g[j], v);
+        }
+    }
+    for (auto &fv : s->fixed_voltage)
+        for (int a : fv) {
+            C(n + a, a) = 1.0;
+            for (int b : fv) C(n + a, n + b) = -1.0 * IC(a, b);
+        }
+    s->inv_circ = cm;
+    if (!invert(s->inv_circ, 2 * n)) return fail(PG_ERR_SINGULAR, "circuit matrix is singular");
+    s->circuit_ready = true;
+    return PG_OK;
+}
+
+int pg_get_capacitance(pg_sim *s, double *inv_cap) {
+    if (!s || !inv_cap) return fail(PG_ERR_ARG, "pg_get_capacitance: NULL argument");
+    if (!s->circuit_ready) return fail(PG_ERR_STATE, "circuit not set up");
+    std::copy(s->inv_cap.begin(), s->inv_cap.end(), inv_cap);
+    return PG_OK;
+}
+
+int pg_solve_circuit(pg_sim *s, pg_object *objects, int32_t n_objects, double *phi, pg_solve_info *info) {
+    if (!s || (n_objects > 0 && !objects)) return fail(PG_ERR_ARG, "pg_solve_circuit: bad arguments");
+    if (!s->circuit_ready) return fail(PG_ERR_STATE, "pg_solve_circuit: call pg_circuit_cm_setup first");
+    pg_solve_info acc{};
+    int rc = solve_circuit_internal(s, objects, n_objects, &acc);
+    if (info) *info = acc;
+    if (rc) return rc;
+    if (phi) return pg_get_phi(s, phi);
+    return PG_OK;
+}
+
+int pg_create_flux(pg_sim *s, const pg_species *sp, int32_t n) {
+    if (!s || (n > 0 && !sp) || n < 0 || n > kMaxSpecies) return fail(PG_ERR_ARG, "pg_create_flux: bad arguments");
+    // Species slots follow the engine's species ids; injection table rows are
+    // indexed by engine species id so particles carry consistent ids.
+    pg_species tab[kMaxSpecies]{};
+    int nmax = 0;
+    for (int k = 0; k < n; ++k) {
+        const int id = species_id(s, sp[k].q, sp[k].m);
+        if (id < 0) return fail(PG_ERR_ARG, "pg_create_flux: more than 8 species");
+        tab[id] = sp[k];
+        nmax = std::max(nmax, id + 1);
+    }
+    const int nf = s->n_ext;
+    std::vector<double> num((size_t)nmax * nf, 0.0), pmax((size_t)nmax * nf, 0.0);
+    for (int k = 0; k < nmax; ++k) {
+        const pg_species &S = tab[k];
+        if (S.vth <= 0 && S.n == 0) continue;   // species without inflow
+        const double vth = S.vth, vth2 = vth * vth;
+        const double factor = 1.0 / std::pow(std::sqrt(2. * M_PI * vth2), 3);
+        for (int j = 0; j < nf; ++j) {
+            const double *F = &s->ext_facets_h[14 * (size_t)j];
+            const double area = F[0];
+            const double nrm[3] = {F[10], F[11], F[12]};
+            // Maxwellian::flux_num_particles (punc/src/distributions.cpp:52-60)
+            double vdn = 0.0;
+            for (int c = 0; c < 3; ++c) vdn += nrm[c] * S.vd[c];
+            num[(size_t)k * nf + j] = area * (vth / (std::sqrt(2 * M_PI)) * std::exp(-0.5 * (vdn / vth) * (vdn / vth)) +
+                                             0.5 * vdn * (1. + std::erf(vdn / (std::sqrt(2) * vth))));
+            // Maxwellian::flux_max (punc/src/distributions.cpp:62-72)
+            double tmp[3];
+            for (int c = 0; c < 3; ++c) tmp[c] = S.vd[c] - 0.5 * nrm[c] * vdn + 0.5 * nrm[c] * std::sqrt(4 * vth2 + vdn * vdn);
+            double vn = 0.0;
+            for (int c = 0; c < 3; ++c) vn += tmp[c] * nrm[c];
+            double vsq = 0.0;
+            for (int c = 0; c < 3; ++c) vsq += (tmp[c] - S.vd[c]) * (tmp[c] - S.vd[c]);
+            pmax[(size_t)k * nf + j] = (vn > 0.0) * vn * (factor * std::exp(-0.5 * vsq / vth2));
+        }
+    }
+    if (s->flux_num) cudaFree(s->flux_num);
+    if (s->pdf_max) cudaFree(s->pdf_max);
+    if (s->inj_counts) cudaFree(s->inj_counts);
+    if (s->inj_offsets) cudaFree(s->inj_offsets);
+    s->flux_num = s->pdf_max = nullptr;
+    s->inj_counts = s->inj_offsets = nullptr;
+    const size_t tot = std::max<size_t>(1, (size_t)nmax * nf);
+    PG_CUDA(cudaMalloc(&s->flux_num, sizeof(double) * tot));
+    PG_CUDA(cudaMalloc(&s->pdf_max, sizeof(double) * tot));
+    PG_CUDA(cudaMalloc(&s->inj_counts, sizeof(int64_t) * (tot + 1)));
+    PG_CUDA(cudaMalloc(&s->inj_offsets, sizeof(int64_t) * (tot + 1)));
+    if (!num.empty()) {
+        PG_CUDA(cudaMemcpy(s->flux_num, num.data(), sizeof(double) * num.size(), cudaMemcpyHostToDevice));
+        PG_CUDA(cudaMemcpy(s->pdf_max, pmax.data(), sizeof(double) * pmax.size(), cudaMemcpyHostToDevice));
+    }
+    s->flux_num_h = num;
+    s->n_inj_species = nmax;
+    for (int k = 0; k < nmax; ++k) s->inj[k] = tab[k];
+    s->flux_ready = true;
+    return PG_OK;
+}
+
+int pg_inject(pg_sim *s, double dt, uint64_t seed, uint64_t step, int64_t *n_injected) {
+    if (!s) return fail(PG_ERR_ARG, "NULL handle");
+    int rc = inject_internal(s, dt, seed, step, false, n_injected);
+    s->rho_valid = false;
+    return rc;
+}
+
+int pg_sort(pg_sim *s) {
+    if (!s) return fail(PG_ERR_ARG, "NULL handle");
+    return do_sort(s);
+}
+
+int pg_step(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_objects, pg_step_result *res) {
+    if (!s || !a || (n_objects > 0 && !objects)) return fail(PG_ERR_ARG, "pg_step: bad arguments");
+    pg_step_result out{};
+    int rc;
+    // distribute
+    {
+        StageScope t(s, "distributor");
+        if (!s->rho_valid) {
+            PG_CUDA(cudaMemsetAsync(s->rho_acc, 0, sizeof(double) * s->ndof, s->stream));
+            if (s->n_slots > 0) launch_deposit(s->dm, s->P[s->cur], s->n_slots, s->d_q, s->rho_acc, s->stream);
+        }
+        rho_from_acc(s);
+    }
+    // poisson (+ circuit)
+    {
+        StageScope t(s, "poisson");
+        pg_solve_info info{};
+        if (s->circuit_ready) {
+            rc = solve_circuit_internal(s, objects, n_objects, &info);
+        } else {
+            std::vector<double> pot(std::max(1, s->n_obj), 0.0);
+            for (int k = 0; k < n_objects; ++k) {
+                const int i = object_index(s, objects[k].bnd_id);
+                if (i >= 0) pot[i] = objects[k].potential;
+            }
+            rc = poisson_solve_internal(s, pot.data(), false, true, s->cfg.pcg_rtol, s->cfg.pcg_atol, &info);
+        }
+        out.pcg_iterations = info.iterations;
+        out.pcg_residual = info.residual;
+        if (rc) return rc;
+    }
+    {
+        StageScope t(s, "efield");
+        launch_efield(s->dm, s->phi, a->E0, s->stream);
+    }
+    // accelerator + move + update, depositing the next step's charge
+    {
+        StageScope t(s, "push_move_update_deposit");
+        const double dt_push = a->first_step ? 0.5 * a->dt : a->dt;
+        PushParams pp;
+        fill_push(s, pp, dt_push, a->B, a->use_accel != 0);
+        MoveParams mp{};
+        mp.dt = a->dt;
+        mp.periodic = a->periodic_move;
+        for (int j = 0; j < 3; ++j) mp.Ld[j] = a->Ld[j];
+        PG_CUDA(cudaMemsetAsync(s->rho_acc, 0, sizeof(double) * s->ndof, s->stream));
+        PG_CUDA(cudaMemsetAsync(s->state->absorbed, 0, sizeof(s->state->absorbed), s->stream));
+        if (s->n_slots > 0)
+            launch_fused_step(s->dm, s->P[s->cur], s->n_slots, pp, mp, s->cfg.max_walk_steps, s->d_q, s->rho_acc,
+                              s->state, s->partials, s->n_part, s->ke_dev, s->stream);
+        else
+            PG_CUDA(cudaMemsetAsync(s->ke_dev, 0, sizeof(double), s->stream));
+        double ke = 0;
+        PG_CUDA(cudaMemcpyAsync(&ke, s->ke_dev, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        rc = check_state(s);
+        if (rc) return rc;
+        out.KE = ke;
+        absorbed_to_objects(s, objects, n_objects, a->dt, &out.n_absorbed);
+    }
+    if (a->inject) {
+        StageScope t(s, "injector");
+        rc = inject_internal(s, a->dt, a->seed, a->step, true, &out.n_injected);
+        if (rc) return rc;
+    }
+    s->rho_valid = true;
+    ++s->step_count;
+    if (s->step_count % s->cfg.sort_interval == 0) {
+        StageScope t(s, "sort");
+        rc = do_sort(s);
+        if (rc) return rc;
+    }
+    collect_stages(s);
+    int64_t tot = 0;
+    for (int k = 0; k < s->n_species; ++k) tot += s->state_h->live[k];
+    out.n_particles = tot;
+    if (res) *res = out;
+    return PG_OK;
+}
+
+int pg_event_record(pg_sim *s, int32_t slot) {
+    if (!s || slot < 0 || slot >= 16) return fail(PG_ERR_ARG, "pg_event_record: bad slot");
+    if (!s->user_ev[slot]) PG_CUDA(cudaEventCreate(&s->user_ev[slot]));
+    PG_CUDA(cudaEventRecord(s->user_ev[slot], s->stream));
+    return PG_OK;
+}
+
+int pg_event_elapsed(pg_sim *s, int32_t a, int32_t b, double *ms) {
+    if (!s || !ms || a < 0 || b < 0 || a >= 16 || b >= 16 || !s->user_ev[a] || !s->user_ev[b])
+        return fail(PG_ERR_ARG, "pg_event_elapsed: slot not recorded");
+    PG_CUDA(cudaEventSynchronize(s->user_ev[b]));
+    float f = 0;
+    PG_CUDA(cudaEventElapsedTime(&f, s->user_ev[a], s->user_ev[b]));
+    *ms = f;
+    return PG_OK;
+}
+
+int pg_launch_count(int64_t *n) {
+    if (!n) return fail(PG_ERR_ARG, "pg_launch_count: NULL argument");
+    *n = launches_so_far();
+    return PG_OK;
+}
+
+int pg_synchronize(pg_sim *s) {
+    if (!s) return fail(PG_ERR_ARG, "NULL handle");
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    return PG_OK;
+}
+
+const char *pg_stage_name(pg_sim *s, int32_t index) {
+    if (!s || index < 0 || index >= (int32_t)s->stage_names.size()) return nullptr;
+    return s->stage_names[index].c_str();
+}
+
+int pg_set_profiling(pg_sim *s, int32_t on) {
+    if (!s) return fail(PG_ERR_ARG, "NULL handle");
+    s->profiling = on != 0;
+    return PG_OK;
+}
+
+int pg_stage_times(pg_sim *s, double *ms, int32_t capacity, int32_t *n_stages) {
+    if (!s || !n_stages) return fail(PG_ERR_ARG, "pg_stage_times: NULL argument");
+    collect_stages(s);
+    *n_stages = (int32_t)s->stage_names.size();
+    for (int32_t k = 0; k < *n_stages && k < capacity; ++k) {
+        if (ms) ms[k] = s->stage_ms[k];
+        s->stage_ms[k] = 0.0;
+    }
+    return PG_OK;
+}
+
+}  // extern "C"

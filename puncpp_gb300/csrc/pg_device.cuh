@@ -1,0 +1,172 @@
+// Device data layout and kernel launch wrappers of the engine.
+//
+// Layout in HBM:
+//   mesh, per cell: planes [Nc][16] f64 (facet i: c0, nx, ny, nz; one 128-B
+//   line per cell), neighbours [Nc] int4 (cell id or -tag), barycentric rows
+//   [Nc][12] f64, cell dofs [Nc] int4, DG0 field [Nc] f64x4;
+//   per dof: dv_inv, rho accumulator, rho, phi;
+//   particles: structure of arrays x, y, z, vx, vy, vz (f64, or f32 in the
+//   mixed form), cell (int32, -1 = free slot), species (uint8), id (int64).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "punc_gpu.h"
+
+namespace pg {
+
+constexpr int kMaxSpecies = 8;
+constexpr int kMaxTags = 64;
+constexpr int kDead = -1;                 // cell id of a free particle slot
+constexpr int kWalkFail = -2147483647;    // walk step limit reached
+
+struct DevMesh {
+    int32_t nc = 0, ndof = 0;
+    const double *planes = nullptr;   // [nc][16]
+    const int4 *nbr = nullptr;        // [nc]
+    const double *bary = nullptr;     // [nc][12]
+    const int4 *dofs = nullptr;       // [nc]
+    double *E = nullptr;              // [nc][4]
+    const double *dv_inv = nullptr;   // [ndof]
+    // FP32 copies for the mixed form
+    const float *planes_f = nullptr;  // [nc][16]
+    const float *bary_f = nullptr;    // [nc][12] padded to 16
+    float *E_f = nullptr;             // [nc][4]
+    // point-location bins
+    double lo[3] = {0, 0, 0}, bin_h[3] = {1, 1, 1};
+    int32_t nbin[3] = {1, 1, 1};
+    const int64_t *bin_ptr = nullptr;
+    const int32_t *bin_cells = nullptr;
+};
+
+struct DevParticles {
+    double *x = nullptr, *y = nullptr, *z = nullptr;
+    double *vx = nullptr, *vy = nullptr, *vz = nullptr;
+    float *xf = nullptr, *yf = nullptr, *zf = nullptr;
+    float *vxf = nullptr, *vyf = nullptr, *vzf = nullptr;
+    int32_t *cell = nullptr;
+    uint8_t *sp = nullptr;
+    int64_t *pid = nullptr;
+    int64_t capacity = 0;
+};
+
+// Device-side counters and error word, read back with one copy.
+struct DevState {
+    int32_t err_code;
+    int32_t err_pad;
+    int64_t err_index;
+    int64_t live[kMaxSpecies];                    // live particles per species
+    int64_t absorbed[kMaxTags][kMaxSpecies];      // absorbed this call, per tag and species
+    int64_t injected[kMaxSpecies];
+    int64_t inject_total;                         // slots appended by the last injection
+    double ke;                                    // last kinetic-energy reduction
+    double image_charge[kMaxTags];
+};
+
+// Per-species constants for one push.
+struct PushParams {
+    double coef[kMaxSpecies];     // (0.5*dt)*(q/m) for boris, dt*(q/m) for accel
+    double half_m[kMaxSpecies];   // 0.5*m
+    double t[kMaxSpecies][3];     // Boris rotation vectors (host tan)
+    double s[kMaxSpecies][3];
+    int32_t has_B;
+    int32_t accel;                // 1: accel() update rule
+};
+
+struct MoveParams {
+    double dt;
+    int32_t periodic;
+    double Ld[3];
+};
+
+struct InjectSpecies {
+    double ndt;                   // n*dt
+    double domain_lo[3], domain_w[3];
+    double vd[3];
+    double vth2, factor;
+    double q;
+};
+
+struct InjectParams {
+    int32_t n_species;
+    int32_t n_facets;
+    uint64_t seed;
+    uint32_t step;
+    double dt;
+    int64_t slot_base;            // first free slot
+    int64_t pid_base;
+    InjectSpecies sp[kMaxSpecies];
+};
+
+// PCG on the Dirichlet-reduced symmetric matrix, one cooperative launch.
+struct PcgArgs {
+    int32_t n;
+    const int32_t *rowptr;
+    const int32_t *col;
+    const double *val;
+    const double *dinv;
+    double *b;
+    double *x;
+    double *r;
+    double *z;
+    double *p0;
+    double *p1;
+    double *Ap;
+    double *partials;             // [4][grid]
+    double rtol, atol;
+    int32_t max_iter;
+    int32_t remove_mean;          // periodic: project b and x onto mean zero
+    int32_t *out_iter;
+    int32_t *out_status;          // 0 converged, 1 iteration cap, 2 breakdown
+    double *out_rr;               // ||r||^2
+    double *out_bb;               // ||b||^2
+};
+
+// ---- launch wrappers (all on `stream`) -----------------------------------
+int sm_count();
+// Kernels launched by this library in this process (pg_launch_count).
+void count_launches(int n);
+long long launches_so_far();
+
+void launch_efield(const DevMesh &m, const double *phi, const double E0[3], cudaStream_t st);
+void launch_push(const DevMesh &m, const DevParticles &p, int64_t n_slots, const PushParams &pp,
+                 double *partials, int nblocks, double *ke_out, cudaStream_t st);
+void launch_move(const DevParticles &p, int64_t n_slots, const MoveParams &mp, cudaStream_t st);
+void launch_update(const DevMesh &m, const DevParticles &p, int64_t n_slots, int max_steps,
+                   DevState *state, cudaStream_t st);
+void launch_deposit(const DevMesh &m, const DevParticles &p, int64_t n_slots, const double *q_species,
+                    double *rho_acc, cudaStream_t st);
+void launch_fused_step(const DevMesh &m, const DevParticles &p, int64_t n_slots, const PushParams &pp,
+                       const MoveParams &mp, int max_steps, const double *q_species, double *rho_acc,
+                       DevState *state, double *partials, int nblocks, double *ke_out, cudaStream_t st);
+void launch_kinetic(const DevParticles &p, int64_t n_slots, const double *half_m, double *partials,
+                    int nblocks, double *ke_out, cudaStream_t st);
+void launch_locate(const DevMesh &m, const double *xyz, int64_t n, int32_t *cells, cudaStream_t st);
+void launch_scale(const double *a, const double *b, double *out, int64_t n, cudaStream_t st);
+
+void launch_inject_count(const DevMesh &m, const InjectParams &ip, const double *flux_num,
+                         int64_t *counts, cudaStream_t st);
+void launch_inject_generate(const DevMesh &m, const DevParticles &p, const InjectParams &ip,
+                            const double *flux_num, const double *pdf_max, const double *facets,
+                            const int64_t *offsets, int max_steps, int deposit, const double *q_species,
+                            double *rho_acc, DevState *state, cudaStream_t st);
+
+void launch_scan_i64(const int64_t *in, int64_t *out, int64_t n, int64_t *tmp, cudaStream_t st);
+int64_t scan_tmp_size(int64_t n);
+void launch_sort_hist(const DevParticles &p, int64_t n_slots, int64_t *hist, cudaStream_t st);
+void launch_sort_scatter(const DevParticles &src, const DevParticles &dst, int64_t n_slots,
+                         int64_t *cursor, cudaStream_t st);
+
+void launch_rhs(const DevMesh &m, const int32_t *mrow, const int32_t *mcol, const double *mval,
+                const double *rho, const int32_t *bc_kind, const double *bc_value,
+                const double *w_ext, const double *w_obj, const double *obj_pot, int32_t n_obj,
+                int32_t use_ext, double *b, cudaStream_t st);
+void launch_set_bc(const int32_t *bc_kind, const double *bc_value, const double *obj_pot,
+                   int32_t n, double *x, cudaStream_t st);
+int launch_pcg(const PcgArgs &a, cudaStream_t st);
+int pcg_grid_blocks();
+void launch_image_charge(const DevMesh &m, const double *phi, const double *ofacets, int32_t n_ofacets,
+                         int32_t n_obj, double eps0, double *out, cudaStream_t st);
+
+}  // namespace pg

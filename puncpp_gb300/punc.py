@@ -1,0 +1,349 @@
+"""Python front end with the names and call order of the PUNC++ particle path.
+
+A time loop written against the reference (interaction/interaction.cpp:342-480):
+
+    distribute_cg1(pop, rho, dv_inv)
+    poisson.solve_circuit(phi, rho, mesh, objects, circuit)
+    esolver.solve(E, phi)                 # EFieldDG0
+    KE = boris(pop, E, B, dt)             # or accel(pop, E, dt)
+    move(pop, dt)
+    pop.update(objects, dt)
+    inject_particles(pop, species, mesh.exterior_facets, dt)
+
+runs unchanged on these classes; every call goes through the C ABI of
+libpunc_gpu.so into device-resident state.  Fields (E, rho, phi) live on the
+device inside the Population's engine handle; Function objects are views that
+download on .vector().
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+from .meshgen import MeshArrays
+
+
+class Mesh:
+    """Host mesh tables (pg_mesh_build): the reference Mesh plus the tables its
+    Population constructor derives (punc/src/mesh.cpp:41-60)."""
+
+    dim = 3
+    ext_bnd_id = 1
+
+    def __init__(self, arrays: MeshArrays, eps0: float = 1.0):
+        lib = L.load()
+        self.arrays = arrays
+        self.eps0 = eps0
+        self._keep = [np.ascontiguousarray(arrays.coords, np.float64), np.ascontiguousarray(arrays.cells, np.int64),
+                      np.ascontiguousarray(arrays.bfacets, np.int64), np.ascontiguousarray(arrays.btags, np.int32)]
+        v2d = None if arrays.vertex_to_dof is None else np.ascontiguousarray(arrays.vertex_to_dof, np.int64)
+        self._keep.append(v2d)
+        co, ce, bf, bt, _ = self._keep
+        d = L.MeshDesc(co.shape[0], L.dptr(co), ce.shape[0], L.i64ptr(ce), bf.shape[0], L.i64ptr(bf),
+                       L.i32ptr(bt), arrays.n_dofs, L.i64ptr(v2d))
+        h = C.c_void_p()
+        L.check(lib.pg_mesh_build(C.byref(d), eps0, C.byref(h)))
+        self.handle = h
+        self.num_objects = int(arrays.n_objects)
+        self.Ld = arrays.Ld
+
+    def table(self, which: int) -> np.ndarray:
+        ptr = C.c_void_p()
+        n = C.c_int64()
+        L.check(L.load().pg_mesh_array(self.handle, which, C.byref(ptr), C.byref(n)))
+        dt = L._TABLE_DTYPE[which]
+        if n.value == 0:
+            return np.zeros(0, dtype=dt)
+        buf = (C.c_char * (n.value * np.dtype(dt).itemsize)).from_address(ptr.value)
+        return np.frombuffer(buf, dtype=dt).copy()
+
+    @property
+    def exterior_facets(self) -> np.ndarray:
+        return self.table(L.T_EXT_FACETS).reshape(-1, 14)
+
+    @property
+    def n_dofs(self) -> int:
+        return int(self.arrays.n_dofs)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            L.load().pg_mesh_free(h)
+            self.handle = None
+
+
+@dataclass
+class Object:
+    """Reference Object (punc/include/punc/object.h:80-130)."""
+    bnd_id: int
+    charge: float = 0.0
+    current: float = 0.0
+    potential: float = 0.0
+
+    def set_potential(self, p: float):
+        self.potential = p
+
+    def get_potential(self) -> float:
+        return self.potential
+
+
+def _objects_in(objects):
+    arr = (L.Object * max(1, len(objects)))()
+    for k, o in enumerate(objects):
+        arr[k] = L.Object(o.bnd_id, o.charge, o.current, o.potential)
+    return arr
+
+
+def _objects_out(arr, objects):
+    for k, o in enumerate(objects):
+        o.charge, o.current, o.potential = arr[k].charge, arr[k].current, arr[k].potential
+
+
+@dataclass
+class Species:
+    """Maxwellian species of simulation particles (punc/src/population.cpp:41-70)."""
+    q: float
+    m: float
+    n: float = 0.0
+    vth: float = 0.0
+    vd: tuple = (0.0, 0.0, 0.0)
+    vdf_range: float = 5.0
+
+
+class Population:
+    """Population<3> on the device (punc/include/punc/population.h:236-308)."""
+
+    g_dim = 3
+
+    def __init__(self, mesh: Mesh, precision: int = L.PG_FP64, periodic: bool = False, capacity: int = 0,
+                 max_walk_steps: int = 0, sort_interval: int = 0, pcg_rtol: float = 0.0, pcg_atol: float = 0.0,
+                 pcg_max_iter: int = 0, warm_start: bool = True, ext_E=(0.0, 0.0, 0.0)):
+        lib = L.load()
+        self.mesh = mesh
+        cfg = L.Config(precision, 1 if periodic else 0, mesh.eps0, capacity, max_walk_steps, sort_interval,
+                       pcg_rtol, pcg_atol, pcg_max_iter, 1 if warm_start else 0, (C.c_double * 3)(*ext_E))
+        h = C.c_void_p()
+        L.check(lib.pg_create(mesh.handle, C.byref(cfg), C.byref(h)))
+        self.handle = h
+        self.num_cells = int(mesh.arrays.n_cells)
+        self.ndof = mesh.n_dofs
+        self.periodic = periodic
+
+    def close(self):
+        h = getattr(self, "handle", None)
+        if h:
+            L.load().pg_destroy(h)
+            self.handle = None
+
+    def __del__(self):
+        self.close()
+
+    def add_particles(self, xs, vs, q: float, m: float) -> int:
+        xs = np.ascontiguousarray(xs, np.float64).reshape(-1, 3)
+        vs = np.ascontiguousarray(vs, np.float64).reshape(-1, 3)
+        n = C.c_int64()
+        L.check(L.load().pg_add_particles(self.handle, L.dptr(xs), L.dptr(vs), xs.shape[0], q, m, C.byref(n)))
+        return n.value
+
+    def locate(self, xs) -> np.ndarray:
+        xs = np.ascontiguousarray(xs, np.float64).reshape(-1, 3)
+        out = np.zeros(xs.shape[0], np.int64)
+        L.check(L.load().pg_locate(self.handle, L.dptr(xs), xs.shape[0], L.i64ptr(out)))
+        return out
+
+    def _counts(self):
+        t, ng, ps = C.c_int64(), C.c_int64(), C.c_int64()
+        L.check(L.load().pg_num_particles(self.handle, C.byref(t), C.byref(ng), C.byref(ps)))
+        return t.value, ng.value, ps.value
+
+    def num_of_particles(self) -> int:
+        return self._counts()[0]
+
+    def num_of_negatives(self) -> int:
+        return self._counts()[1]
+
+    def num_of_positives(self) -> int:
+        return self._counts()[2]
+
+    def particles(self) -> dict:
+        """Live particles ordered by (cell, id): x, v, q, m, cell, id."""
+        lib = L.load()
+        n = C.c_int64()
+        L.check(lib.pg_get_particles(self.handle, 0, None, None, None, None, None, None, C.byref(n)))
+        k = n.value
+        x = np.zeros((k, 3)); v = np.zeros((k, 3)); q = np.zeros(k); m = np.zeros(k)
+        cell = np.zeros(k, np.int64); pid = np.zeros(k, np.int64)
+        L.check(lib.pg_get_particles(self.handle, k, L.dptr(x), L.dptr(v), L.dptr(q), L.dptr(m), L.i64ptr(cell),
+                                     L.i64ptr(pid), C.byref(n)))
+        return dict(x=x, v=v, q=q, m=m, cell=cell, id=pid)
+
+    def update(self, objects, dt: float):
+        arr = _objects_in(objects)
+        L.check(L.load().pg_update(self.handle, arr, len(objects), dt))
+        _objects_out(arr, objects)
+
+    def sort(self):
+        L.check(L.load().pg_sort(self.handle))
+
+    def status(self):
+        code, idx = C.c_int32(), C.c_int64()
+        L.check(L.load().pg_status_detail(self.handle, C.byref(code), C.byref(idx)))
+        return code.value, idx.value
+
+
+class Function:
+    """A field of the Population's engine: 'E' (DG0 vector), 'rho' or 'phi' (CG1)."""
+
+    def __init__(self, pop: Population, kind: str):
+        assert kind in ("E", "rho", "phi")
+        self.pop, self.kind = pop, kind
+
+    def vector(self) -> np.ndarray:
+        lib = L.load()
+        if self.kind == "E":
+            out = np.zeros((self.pop.num_cells, 3))
+            L.check(lib.pg_get_efield(self.pop.handle, L.dptr(out)))
+        else:
+            out = np.zeros(self.pop.ndof)
+            fn = lib.pg_get_rho if self.kind == "rho" else lib.pg_get_phi
+            L.check(fn(self.pop.handle, L.dptr(out)))
+        return out
+
+    def set_local(self, values):
+        v = np.ascontiguousarray(values, np.float64)
+        lib = L.load()
+        if self.kind == "E":
+            L.check(lib.pg_set_efield(self.pop.handle, L.dptr(v.reshape(-1, 3))))
+        elif self.kind == "rho":
+            L.check(lib.pg_set_rho(self.pop.handle, L.dptr(v)))
+        else:
+            L.check(lib.pg_efield_dg0(self.pop.handle, L.dptr(v)))  # uploads phi and refreshes E
+
+
+def accel(pop: Population, E: Function, dt: float) -> float:
+    """accel with a DG0 field (punc/include/punc/pusher.h:66-130)."""
+    ke = C.c_double()
+    L.check(L.load().pg_accel(pop.handle, dt, C.byref(ke)))
+    return ke.value
+
+
+def boris(pop: Population, E: Function, B, dt: float) -> float:
+    """boris with a DG0 field and uniform B (punc/include/punc/pusher.h:397-510)."""
+    b = np.ascontiguousarray(B, np.float64)
+    ke = C.c_double()
+    L.check(L.load().pg_boris(pop.handle, L.dptr(b), dt, C.byref(ke)))
+    return ke.value
+
+
+def move(pop: Population, dt: float):
+    L.check(L.load().pg_move(pop.handle, dt))
+
+
+def move_periodic(pop: Population, dt: float, Ld):
+    Ld = np.ascontiguousarray(Ld, np.float64)
+    L.check(L.load().pg_move_periodic(pop.handle, dt, L.dptr(Ld)))
+
+
+def distribute_cg1(pop: Population, rho: Function | None = None, dv_inv=None) -> np.ndarray:
+    """distribute_cg1 (punc/include/punc/distributor.h:168-210); dv_inv is the
+    engine's element_volume table, so the argument is accepted and unused."""
+    out = np.zeros(pop.ndof)
+    L.check(L.load().pg_distribute_cg1(pop.handle, L.dptr(out)))
+    return out
+
+
+def kinetic_energy(pop: Population) -> float:
+    ke = C.c_double()
+    L.check(L.load().pg_kinetic_energy(pop.handle, C.byref(ke)))
+    return ke.value
+
+
+class EFieldDG0:
+    """EFieldDG0 (punc/src/efield.cpp:77-99)."""
+
+    def solve(self, E: Function, phi: Function):
+        L.check(L.load().pg_efield_dg0(E.pop.handle, None))
+
+
+class CircuitCM:
+    """CircuitCM (punc/src/object_CM.cpp:135-197): capacitance matrix at set-up."""
+
+    def __init__(self, pop: Population, objects, vsources=(), isources=(), dt: float = 1.0):
+        vs = (L.Source * max(1, len(vsources)))(*[L.Source(int(a), int(b), float(v)) for a, b, v in vsources])
+        iss = (L.Source * max(1, len(isources)))(*[L.Source(int(a), int(b), float(v)) for a, b, v in isources])
+        L.check(L.load().pg_circuit_cm_setup(pop.handle, vs, len(vsources), iss, len(isources), dt))
+        self.pop = pop
+        self.correction_required = True
+
+    def inv_capacitance(self) -> np.ndarray:
+        n = self.pop.mesh.num_objects
+        out = np.zeros(n * n)
+        L.check(L.load().pg_get_capacitance(self.pop.handle, L.dptr(out)))
+        return out.reshape(n, n)
+
+
+class PoissonSolver:
+    """PoissonSolver (punc/src/poisson.cpp:260-385) on the device."""
+
+    def __init__(self, pop: Population, objects=(), circuit: CircuitCM | None = None):
+        self.pop = pop
+        self.last_info = None
+
+    def solve(self, phi: Function, rho: Function, objects=(), circuit=None) -> np.ndarray:
+        arr = _objects_in(objects)
+        info = L.SolveInfo()
+        L.check(L.load().pg_poisson_solve(self.pop.handle, arr, len(objects), None, C.byref(info)))
+        self.last_info = info
+        return phi.vector()
+
+    def solve_circuit(self, phi: Function, rho: Function, mesh, objects, circuit) -> np.ndarray:
+        arr = _objects_in(objects)
+        info = L.SolveInfo()
+        L.check(L.load().pg_solve_circuit(self.pop.handle, arr, len(objects), None, C.byref(info)))
+        _objects_out(arr, objects)
+        self.last_info = info
+        return phi.vector()
+
+
+def create_flux(pop: Population, species):
+    """create_flux (punc/src/injector.cpp:104-171), Maxwellian species."""
+    arr = (L.Species * max(1, len(species)))()
+    for k, s in enumerate(species):
+        arr[k] = L.Species(s.q, s.m, s.n, s.vth, (C.c_double * 3)(*s.vd), s.vdf_range)
+    L.check(L.load().pg_create_flux(pop.handle, arr, len(species)))
+
+
+def inject_particles(pop: Population, species, facets, dt: float, seed: int = 0, step: int = 0) -> int:
+    """inject_particles (punc/include/punc/injector.h:157-232); create_flux must
+    have been called for these species."""
+    n = C.c_int64()
+    L.check(L.load().pg_inject(pop.handle, dt, seed, step, C.byref(n)))
+    return n.value
+
+
+def step(pop: Population, objects, dt: float, B=(0.0, 0.0, 0.0), first_step=False, use_accel=False, Ld=None,
+         inject=False, seed=0, step_no=0, E0=(0.0, 0.0, 0.0)) -> L.StepResult:
+    """One fused timestep in the order of interaction.cpp:342-480."""
+    a = L.StepArgs(dt, (C.c_double * 3)(*B), 1 if first_step else 0, 1 if use_accel else 0,
+                   0 if Ld is None else 1, (C.c_double * 3)(*(Ld if Ld is not None else (0.0, 0.0, 0.0))),
+                   1 if inject else 0, seed, step_no, (C.c_double * 3)(*E0))
+    arr = _objects_in(objects)
+    res = L.StepResult()
+    L.check(L.load().pg_step(pop.handle, C.byref(a), arr, len(objects), C.byref(res)))
+    _objects_out(arr, objects)
+    return res
+
+
+def stage_times(pop: Population) -> dict:
+    lib = L.load()
+    n = C.c_int32()
+    ms = np.zeros(32)
+    L.check(lib.pg_stage_times(pop.handle, L.dptr(ms), 32, C.byref(n)))
+    return {lib.pg_stage_name(pop.handle, k).decode(): float(ms[k]) for k in range(n.value)}
+
+
+def set_profiling(pop: Population, on: bool):
+    L.check(L.load().pg_set_profiling(pop.handle, 1 if on else 0))

@@ -1,0 +1,64 @@
+"""The C-ABI library loads without a GPU and exports every entry point of
+include/punc_gpu.h; host-only entry points work on the CPU."""
+import ctypes as C
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "punc_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(pg_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_symbols()
+    assert len(names) >= 35
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, f"not exported: {missing}"
+
+
+def test_bindings_cover_the_header():
+    from puncpp_gb300 import _lib
+    assert set(declared_symbols()) == set(_lib.SIGNATURES)
+
+
+def test_abi_version(lib):
+    assert lib.pg_abi_version() == 1
+
+
+def test_philox_known_answers(lib, oracle_mod):
+    kat = json.load(open(os.path.join(ROOT, "tests", "golden", "philox4x32_10_kat.json")))
+    for v in kat["vectors"]:
+        ctr = (C.c_uint32 * 4)(*[int(x, 16) for x in v["ctr"]])
+        key = (C.c_uint32 * 2)(*[int(x, 16) for x in v["key"]])
+        out = (C.c_uint32 * 4)()
+        assert lib.pg_philox4x32_10(ctr, key, out) == 0
+        assert ["%08x" % x for x in out] == v["out"]
+        out2 = (C.c_uint32 * 4)()
+        oracle_mod.lib().or_philox_block(ctr, key, out2)
+        assert ["%08x" % x for x in out2] == v["out"]
+
+
+def test_oracle_exp_series_accuracy(oracle_mod):
+    L = oracle_mod.lib()
+    xs = np.concatenate([np.linspace(-740, 700, 20001), np.linspace(-40, 0, 10001), [0.0, -1e-300, 1e-300]])
+    got = np.array([L.or_exp_series(float(x)) for x in xs])
+    ref = np.exp(xs)
+    rel = np.abs(got - ref) / np.maximum(ref, 1e-300)
+    assert rel[ref > 1e-300].max() < 4e-16
+
+
+def test_errors_are_status_codes_not_aborts(lib):
+    from puncpp_gb300 import _lib
+    h = C.c_void_p()
+    assert lib.pg_mesh_build(None, 1.0, C.byref(h)) == 1
+    assert b"empty" in lib.pg_last_error()
+    assert lib.pg_mesh_array(None, 0, None, None) == 1
+    assert _lib.STATUS_NAMES[lib.pg_philox4x32_10(None, None, None)] == "PG_ERR_ARG"

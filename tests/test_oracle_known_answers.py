@@ -1,0 +1,146 @@
+"""Known answers of the reference's demos, checked on the oracle (CPU).
+
+PUNC++ stores no golden vectors; these are the analytic results its demos
+and integration test compare against (demo/capacitance, demo/boris,
+demo/langmuir, demo/injection, test/test.py), regenerated on the synthetic
+meshes.  They pin the oracle's physics; the GPU tests then pin the engine to
+the oracle."""
+import numpy as np
+import pytest
+
+from puncpp_gb300 import meshgen
+from helpers import langmuir_load
+
+
+def test_capacitance_concentric_spheres(oracle_mod):
+    # demo/capacitance/capacitance.cpp:40-42: C = 4 pi eps0 r R / (R - r)
+    r, R = 0.2, 1.0
+    exact = 4 * np.pi * r * R / (R - r)
+    facet_err, react_err = [], []
+    for n, k in ((8, 1), (16, 2), (24, 3)):
+        o = oracle_mod.Oracle(meshgen.mapped_sphere_shell(n, k, r, R))
+        phi = o.poisson_direct(np.zeros(o.ndof), potentials=[1.0])
+        K, _ = o.matrices()
+        kind, _ = o.dirichlet()
+        facet_err.append(abs(o.image_charges(phi)[0] - exact) / exact)
+        react_err.append(abs((K @ phi)[kind == 1].sum() - exact) / exact)
+    # the variationally consistent charge converges at second order
+    assert react_err[-1] < 0.02 and react_err[0] / react_err[1] > 3.0
+    # the reference's facet-flux form (Charge.ufl) converges from below
+    assert facet_err[0] > facet_err[1] > facet_err[2]
+
+
+def test_boris_gyration_angle_and_speed(oracle_mod):
+    # demo/boris: uniform B, no E: |v| is conserved, and with the reference's
+    # t = tan(q B dt / 2m) (pusher.h:469-474) the velocity turns by exactly
+    # -omega_c dt per step (2 atan(tan(x)) = 2x)
+    ma = meshgen.kuhn_box(4, -50.0, 50.0)
+    o = oracle_mod.Oracle(ma)
+    q, m, B, dt = -1.0, 1.0, 0.7, 0.3
+    o.add_particles(np.array([[0.1, 0.2, 0.3]]), np.array([[1.0, 0.0, 0.25]]), q, m)
+    E = np.zeros((o.nc, 3))
+    steps = 40
+    for _ in range(steps):
+        o.boris(E, (0.0, 0.0, B), dt)
+    v = o.particles()["v"][0]
+    theta = np.arctan2(v[1], v[0])
+    expect = -steps * (q / m) * B * dt
+    assert abs(np.angle(np.exp(1j * (theta - expect)))) < 1e-12
+    assert abs(np.hypot(v[0], v[1]) - 1.0) < 1e-14 and v[2] == 0.25
+
+
+def test_uniform_field_leapfrog_is_exact(oracle_mod):
+    ma = meshgen.kuhn_box(4, -100.0, 100.0)
+    o = oracle_mod.Oracle(ma)
+    q, m, dt = 2.0, 4.0, 0.125
+    E0 = np.array([0.5, -0.25, 1.0])
+    o.add_particles(np.array([[0.0, 0.0, 0.0]]), np.array([[1.0, 2.0, -1.0]]), q, m)
+    E = np.tile(E0, (o.nc, 1))
+    n = 16
+    for i in range(n):
+        o.boris(E, (0.0, 0.0, 0.0), dt)
+        o.move(dt)
+    p = o.particles()
+    a = q / m * E0
+    v_expect = np.array([1.0, 2.0, -1.0]) + n * a * dt
+    x_expect = np.array([1.0, 2.0, -1.0]) * n * dt + a * dt * dt * n * (n + 1) / 2
+    np.testing.assert_allclose(p["v"][0], v_expect, rtol=0, atol=1e-13)
+    np.testing.assert_allclose(p["x"][0], x_expect, rtol=0, atol=1e-12)
+
+
+def _langmuir_omega(oracle_mod, n_cells, ppc, dt=0.1, steps=130):
+    ma = meshgen.langmuir_cube(n_cells)
+    o = oracle_mod.Oracle(ma)
+    rng = np.random.default_rng(11)
+    x, v, q, m = langmuir_load(ma, ppc, rng, amplitude=0.02)
+    o.add_particles(x, v, q, m)
+    Ld = (1.0, 1.0, 1.0)
+    mode = []
+    for n in range(steps):
+        rho = o.distribute_cg1()
+        phi = o.poisson_direct(rho, periodic=True)
+        E = o.efield(phi)
+        o.boris(E, (0, 0, 0), dt * (0.5 if n == 0 else 1.0))
+        p = o.particles(sort=False)
+        mode.append(np.mean(p["v"][:, 0] * np.cos(2 * np.pi * p["x"][:, 0])))
+        o.move(dt, Ld)
+        o.update([], dt)
+    s = np.array(mode)
+    k = np.where(np.sign(s[1:]) != np.sign(s[:-1]))[0]
+    t0 = k + s[k] / (s[k] - s[k + 1])          # interpolated zero crossings (in steps)
+    assert len(t0) >= 3
+    return np.pi / (np.mean(np.diff(t0)) * dt)
+
+
+def test_langmuir_oscillates_at_the_plasma_frequency(oracle_mod):
+    # demo/langmuir: cold electrons over a neutralising background oscillate at
+    # omega_p = 1; the grid lowers it by O((k h)^2), so it must rise toward 1
+    w8 = _langmuir_omega(oracle_mod, 8, 16)
+    w12 = _langmuir_omega(oracle_mod, 12, 8)
+    assert w8 < w12 < 1.02
+    assert abs(w12 - 1.0) < 0.06, (w8, w12)
+
+
+def test_flux_injection_count_and_flux_weighted_speed(oracle_mod):
+    # demo/injection/injection.cpp:88-114: injected count follows the analytic
+    # Maxwellian flux n * vth / sqrt(2 pi) * area * dt
+    ma = meshgen.kuhn_box(6, -3.0, 3.0)
+    o = oracle_mod.Oracle(ma)
+    n_dens, vth, dt = 30.0, 1.0, 0.05
+    o.create_flux([dict(q=-1.0, m=1.0, n=n_dens, vth=vth)])
+    area = 6 * 36.0
+    expect_per_step = n_dens * vth / np.sqrt(2 * np.pi) * area * dt
+    total = 0
+    steps = 200
+    for s in range(steps):
+        k, _ = o.inject(dt, 1234, s)
+        total += k
+    mean = total / steps
+    sigma = np.sqrt(expect_per_step / steps)
+    assert abs(mean - expect_per_step) < 4 * sigma + 0.05 * expect_per_step * 0  # statistical, 4 sigma
+    p = o.particles(sort=False)
+    # flux-weighted normal speed of a Maxwellian: vth sqrt(pi/2).  A particle
+    # injected through wall w sits at distance r*dt*(v.n_w), r in [0,1], from it.
+    x = p["x"]
+    d = np.stack([x + 3.0, 3.0 - x], axis=2).reshape(len(x), 6)
+    normals = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]], float)
+    vn_all = p["v"] @ normals.T
+    ok = (vn_all > 0) & (d <= dt * vn_all * (1 + 1e-12) + 1e-12)
+    assert np.all(ok.any(axis=1))
+    vn = vn_all[np.arange(len(x)), np.argmax(ok, axis=1)]
+    assert abs(vn.mean() - vth * np.sqrt(np.pi / 2)) < 4 * vth / np.sqrt(len(vn))
+
+
+def test_update_absorbs_at_object_and_tallies_current(oracle_mod):
+    ma = meshgen.probe_box(8, 2.0, 0.6)
+    o = oracle_mod.Oracle(ma)
+    # one particle heading into the hole, one out through the wall, one staying
+    xs = np.array([[0.9, 0.05, 0.05], [1.9, 0.1, 0.1], [-1.2, -1.1, 1.0]])
+    vs = np.array([[-1.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 0.0]])
+    assert o.add_particles(xs, vs, -2.0, 1.0) == 3
+    o.move(0.5)
+    objs = [dict(bnd_id=2, charge=1.0, current=0.0, potential=0.0)]
+    absorbed = o.update(objs, 0.5)
+    assert absorbed[2] == 1 and absorbed[1] == 1
+    assert objs[0]["charge"] == 1.0 - 2.0 and objs[0]["current"] == -2.0 / 0.5
+    assert o.num_particles() == 1
