@@ -32,10 +32,15 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s on 1 GB300: mixed-precision vs FP64 form at ≤1e-5 rel ρ error"
 UNIT = "particle-steps/s"
-WORKLOAD = ("probe-80: [-10,10]^3, 80^3x6 Kuhn tets minus centroid r<1 (object), 2M e- + 2M ions (m_i=1836), "
-            "Maxwellian T_e=T_i, CM bias -2 kT/e, flux injection, dt=0.05, Poisson rtol 1e-10 atol 1e-12")
-N_SIDE, HALF, RADIUS = 80, 10.0, 1.0
-N_PER_SPECIES = 2_000_000
+HALF, RADIUS = 10.0, 1.0
+N_SIDE, N_PER_SPECIES = 80, 2_000_000   # the probe configuration; --workload probe-N scales particles with N^3
+
+
+def workload_name(n_side, n_per):
+    return (f"probe-{n_side}: [-10,10]^3, {n_side}^3x6 Kuhn tets minus centroid r<1 (object), "
+            f"{n_per / 1e6:g}M e- + {n_per / 1e6:g}M ions (m_i=1836), Maxwellian T_e=T_i, CM bias -2 kT/e, "
+            f"flux injection, dt=0.05, Poisson rtol 1e-10 atol 1e-12")
+
 DT = 0.05
 BIAS = -2.0
 RTOL, ATOL = 1e-10, 1e-12
@@ -97,18 +102,18 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-def make_workload():
+def make_workload(n_side=N_SIDE, n_per=N_PER_SPECIES):
     import numpy as np
 
     from puncpp_gb300 import meshgen
-    ma = meshgen.probe_box(N_SIDE, HALF, RADIUS)
+    ma = meshgen.probe_box(n_side, HALF, RADIUS)
     volume = (2 * HALF) ** 3 - 4.0 / 3.0 * math.pi * RADIUS ** 3
-    w = volume / N_PER_SPECIES               # physical density 1 per simulation particle weight
-    n_sim = N_PER_SPECIES / volume
+    w = volume / n_per                       # physical density 1 per simulation particle weight
+    n_sim = n_per / volume
     mi = 1836.0
     species = [dict(q=-w, m=w, n=n_sim, vth=1.0), dict(q=w, m=mi * w, n=n_sim, vth=1.0 / math.sqrt(mi))]
     rng = np.random.default_rng(0x5EED0002)
-    over = int(N_PER_SPECIES * (2 * HALF) ** 3 / volume) + 1
+    over = int(n_per * (2 * HALF) ** 3 / volume) + 1
     loads = []
     for s in species:
         x = -HALF + rng.random((over, 3)) * (2 * HALF)
@@ -123,9 +128,10 @@ def run_ours(args):
     from puncpp_gb300 import _lib as L
     from puncpp_gb300 import punc
 
-    ma, species, loads = make_workload()
+    ma, species, loads = make_workload(args.n_side, args.n_per)
     mesh = punc.Mesh(ma)
-    pop = punc.Population(mesh, capacity=int(2.6 * N_PER_SPECIES * 2), pcg_rtol=RTOL, pcg_atol=ATOL,
+    prec = L.PG_MIXED if args.precision == "mixed" else L.PG_FP64
+    pop = punc.Population(mesh, precision=prec, capacity=int(2.6 * args.n_per * 2), pcg_rtol=RTOL, pcg_atol=ATOL,
                           pcg_max_iter=4000)
     for s, (x, v) in zip(species, loads):
         pop.add_particles(x, v, s["q"], s["m"])
@@ -210,9 +216,10 @@ def run_ours(args):
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "precision_form": "fp64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64" if args.precision == "mixed" else "f64",
+        "precision_form": args.precision,
         "data": "synthetic: seeded uniform/Maxwellian particles on a generated Kuhn probe mesh (no dataset)",
-        "config": {"workload": WORKLOAD, "cells": nc, "dofs": nv, "nnz": nnz, "particles_initial": n0,
+        "config": {"workload": workload_name(args.n_side, args.n_per), "precision": args.precision, "cells": nc, "dofs": nv, "nnz": nnz, "particles_initial": n0,
                    "particles_mean_pushed": round(n_avg), "pcg_iterations_per_step": round(iters / args.steps, 1),
                    "l2": "inputs larger than L2 (particle SoA ~250 MB, mesh tables ~0.9 GB)"},
         "stage_ms": {k: round(v, 3) for k, v in stages.items()}, "stage_share": stages_share,
@@ -247,12 +254,12 @@ def launch_count():
 
 
 # ---------------------------------------------------------------------------
-def oracle_workload(nthreads):
+def oracle_workload(nthreads, n_side=N_SIDE, n_per=N_PER_SPECIES):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
     import oracle as O
 
-    ma, species, loads = make_workload()
+    ma, species, loads = make_workload(n_side, n_per)
     o = O.Oracle(ma)
     for s, (x, v) in zip(species, loads):
         o.add_particles(x, v, s["q"], s["m"])
@@ -284,9 +291,9 @@ def oracle_step(o, circ, objs, n, nthreads):
     return pushed
 
 
-def cpu_baseline(max_seconds=25.0):
+def cpu_baseline(args, max_seconds=25.0):
     nthreads = os.cpu_count() or 1
-    o, circ, objs = oracle_workload(nthreads)
+    o, circ, objs = oracle_workload(nthreads, args.n_side, args.n_per)
     oracle_step(o, circ, objs, 0, nthreads)         # first step (half push) untimed
     pushed, t0, n = 0, time.perf_counter(), 1
     while True:
@@ -296,13 +303,13 @@ def cpu_baseline(max_seconds=25.0):
         if el > max_seconds or n > 6:
             break
     return {"value": round(pushed / el, 1), "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{n - 1} full steps of the same probe-80 workload on the oracle (C++ restatement, "
+            "sample": f"{n - 1} full steps of the same probe-{args.n_side} workload on the oracle (C++ restatement, "
                       f"{nthreads} threads, Jacobi PCG for Poisson), after one untimed step"}
 
 
 def run_reference(args):
     nthreads = os.cpu_count() or 1
-    o, circ, objs = oracle_workload(nthreads)
+    o, circ, objs = oracle_workload(nthreads, args.n_side, args.n_per)
     n = 0
     for _ in range(max(1, args.warmup)):
         oracle_step(o, circ, objs, n, nthreads)
@@ -321,7 +328,7 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": round(el / done * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
             "data": "synthetic: seeded uniform/Maxwellian particles on a generated Kuhn probe mesh (no dataset)",
-            "config": {"workload": WORKLOAD},
+            "config": {"workload": workload_name(args.n_side, args.n_per), "precision": "fp64"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
                              "sample": f"{done} of {args.steps} timed steps (bounded to {budget:.0f} s) of the full "
                                        f"workload on the oracle, the reference's algorithm restated in C++ (the "
@@ -336,7 +343,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="probe-80", help="probe-N: N^3 sub-cubes, particles scaled by (N/80)^3")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     args = ap.parse_args()
+    if not args.workload.startswith("probe-"):
+        ap.error("--workload must be probe-N")
+    args.n_side = int(args.workload.split("-")[1])
+    args.n_per = int(round(N_PER_SPECIES * (args.n_side / N_SIDE) ** 3))
     if args.warmup < 3:
         args.warmup = 3
     rank = int(os.environ.get("RANK", "0"))
@@ -364,7 +377,7 @@ def main():
         res["config"]["parallelism"] = f"replicas x{world}"
     if rank == 0:
         if not args.no_cpu_baseline:
-            res["cpu_baseline"] = cpu_baseline()
+            res["cpu_baseline"] = cpu_baseline(args)
         print(json.dumps(res))
 
 

@@ -87,6 +87,13 @@ typedef struct pg_config {
     int32_t pcg_max_iter;       /* 0: 1000 */
     int32_t pcg_warm_start;     /* 1: start PCG from the previous potential */
     double ext_E[3];            /* exterior Dirichlet value phi = x . ext_E (PhiBoundary) */
+    int32_t circuit_resolve;    /* 1: CircuitCM correction by a second solve, as the reference
+                                   (punc/src/poisson.cpp:373-375); 0: by superposition of the
+                                   unit-potential Laplace solutions kept from set-up (same
+                                   potential up to the solver tolerance, one solve per step) */
+    int32_t pcg_precision;      /* 0: FP64 PCG for PG_FP64, mixed PCG for PG_MIXED; 1: FP64 PCG;
+                                   2: mixed PCG (FP32 recurrence, FP64 solution, inner products
+                                   and true-residual replacement; same FP64 stopping test) */
 } pg_config;
 
 /* Reference Object (punc/include/punc/object.h:80-130). */

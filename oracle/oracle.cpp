@@ -860,56 +860,66 @@ void or_create_flux(void *h, const double *sp, int32_t n_species) {
     }
 }
 
-// inject_particles (punc/include/punc/injector.h:157-232) with one Philox
-// stream per (species, facet).  Species slot s of the flux table is the
-// engine's species id s.  Returns the number kept; counts[s] per species.
+// Two uniforms of Philox block `block` of stream (c1, c2, c3).
+static void uniforms2(uint64_t seed, uint32_t block, uint32_t c1, uint32_t c2, uint32_t c3, double &a, double &b) {
+    uint32_t c[4] = {block, c1, c2, c3};
+    Philox::round10(c, uint32_t(seed), uint32_t(seed >> 32));
+    a = Stream::res53(c[0], c[1]);
+    b = Stream::res53(c[2], c[3]);
+}
+
+// inject_particles (punc/include/punc/injector.h:157-232) with counter-based
+// streams in place of the unseeded mt19937_64: per (species s, facet j) a
+// count stream (c1 = j, c2 = s, c3 = step) whose first uniform rounds N, and
+// per particle k a stream (c1 = j, c2 = s + 8(k+1), c3 = step): block 0 the
+// two uniforms of random_facet_points (punc/src/injector.cpp:78-102), block 1
+// the advance fraction r, blocks 2+2i and 3+2i candidate i of the flux
+// rejection sampler (punc/src/injector.cpp:51-76).  Species slot s of the flux
+// table is the engine's species id s.  Returns the number kept.
 int64_t or_inject(void *h, double dt, uint64_t seed, uint64_t step, int64_t *counts) {
     Oracle &o = *static_cast<Oracle *>(h);
     int64_t kept_total = 0;
     int64_t slot = 0;
+    const uint32_t c3 = (uint32_t)step;
     for (size_t s = 0; s < o.flux.size(); ++s) {
         SpeciesFlux &F = o.flux[s];
         int64_t kept = 0;
         for (size_t j = 0; j < o.ext.size(); ++j) {
             const ExtFacet &e = o.ext[j];
-            Stream rng(seed, (uint32_t)j, (uint32_t)s, (uint32_t)step);
             const double N_float = F.num_particles[j] * (F.n * dt);
             std::size_t N = static_cast<std::size_t>(N_float);
-            if (rng() < (N_float - N)) N += 1;
-            std::vector<double> xs(3 * N), vs(3 * N);
-            // random_facet_points (punc/src/injector.cpp:78-102)
+            double u0, unused;
+            uniforms2(seed, 0u, (uint32_t)j, (uint32_t)s, c3, u0, unused);
+            if (u0 < (N_float - N)) N += 1;
             for (std::size_t i = 0; i < N; ++i) {
-                double r = rng();
-                for (int c = 0; c < 3; ++c) xs[i * 3 + c] = (1.0 - r) * e.vertices[c] + r * e.vertices[c + 3];
-                r = std::sqrt(rng());
-                for (int c = 0; c < 3; ++c) xs[i * 3 + c] = r * xs[i * 3 + c] + (1.0 - r) * e.vertices[2 * 3 + c];
-            }
-            // rejection_sampler with the flux density (punc/src/injector.cpp:51-76)
-            for (std::size_t i = 0; i < N; ++i) {
+                const uint32_t c2 = (uint32_t)(s + 8 * (i + 1));
                 double tmp[3];
-                for (;;) {
-                    for (int c = 0; c < 3; ++c) tmp[c] = F.domain[c] + (F.domain[c + 3] - F.domain[c]) * rng();
-                    const double u = rng();
+                for (uint32_t cand = 0;; ++cand) {
+                    double a, b, c, u;
+                    uniforms2(seed, 2u + 2u * cand, (uint32_t)j, c2, c3, a, b);
+                    uniforms2(seed, 3u + 2u * cand, (uint32_t)j, c2, c3, c, u);
+                    const double r3[3] = {a, b, c};
+                    for (int d = 0; d < 3; ++d) tmp[d] = F.domain[d] + (F.domain[d + 3] - F.domain[d]) * r3[d];
                     double vn = 0.0;
-                    for (int c = 0; c < 3; ++c) vn += tmp[c] * e.normal[c];
+                    for (int d = 0; d < 3; ++d) vn += tmp[d] * e.normal[d];
                     double v_sqrt = 0.0;
-                    for (int c = 0; c < 3; ++c) v_sqrt += (tmp[c] - F.vd[c]) * (tmp[c] - F.vd[c]);
+                    for (int d = 0; d < 3; ++d) v_sqrt += (tmp[d] - F.vd[d]) * (tmp[d] - F.vd[d]);
                     const double pdf = (vn > 0.0) * vn * (F.factor * exp_series(-0.5 * v_sqrt / F.vth2));
                     if (u * F.pdf_max[j] < pdf) break;
                 }
-                for (int c = 0; c < 3; ++c) vs[i * 3 + c] = tmp[c];
-            }
-            // x += r dt v, keep if located: the walk from the facet's cell
-            for (std::size_t i = 0; i < N; ++i) {
-                const double r = rng();
+                double r1, r2, r;
+                uniforms2(seed, 0u, (uint32_t)j, c2, c3, r1, r2);
+                uniforms2(seed, 1u, (uint32_t)j, c2, c3, r, unused);
                 double x[3];
-                for (int c = 0; c < 3; ++c) x[c] = xs[i * 3 + c] + r * dt * vs[i * 3 + c];
+                for (int d = 0; d < 3; ++d) x[d] = (1.0 - r1) * e.vertices[d] + r1 * e.vertices[d + 3];
+                r2 = std::sqrt(r2);
+                for (int d = 0; d < 3; ++d) x[d] = r2 * x[d] + (1.0 - r2) * e.vertices[2 * 3 + d];
+                for (int d = 0; d < 3; ++d) x[d] = x[d] + r * dt * tmp[d];
                 const long cell = relocate_fast(o, x, (long)e.cell);
-                const int64_t id = o.next_id + slot + (int64_t)i;
                 if (cell >= 0) {
                     Particle p;
-                    for (int c = 0; c < 3; ++c) { p.x[c] = x[c]; p.v[c] = vs[i * 3 + c]; }
-                    p.q = F.q; p.m = F.m; p.id = id;
+                    for (int d = 0; d < 3; ++d) { p.x[d] = x[d]; p.v[d] = tmp[d]; }
+                    p.q = F.q; p.m = F.m; p.id = o.next_id + slot + (int64_t)i;
                     o.cells[cell].particles.push_back(p);
                     ++kept;
                 }

@@ -47,7 +47,8 @@ class Config(C.Structure):
     _fields_ = [("precision", C.c_int32), ("periodic", C.c_int32), ("eps0", C.c_double),
                 ("particle_capacity", C.c_int64), ("max_walk_steps", C.c_int32),
                 ("sort_interval", C.c_int32), ("pcg_rtol", C.c_double), ("pcg_atol", C.c_double),
-                ("pcg_max_iter", C.c_int32), ("pcg_warm_start", C.c_int32), ("ext_E", C.c_double * 3)]
+                ("pcg_max_iter", C.c_int32), ("pcg_warm_start", C.c_int32), ("ext_E", C.c_double * 3),
+                ("circuit_resolve", C.c_int32), ("pcg_precision", C.c_int32)]
 
 
 class Object(C.Structure):

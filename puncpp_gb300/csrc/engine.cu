@@ -36,15 +36,22 @@ struct pg_sim {
     // fields
     double *rho_acc = nullptr, *rho = nullptr, *phi = nullptr, *b = nullptr;
     bool rho_valid = false;
+    unsigned long long *rho_fixed = nullptr;   // mixed form: int64 fixed-point accumulator
 
     // solver
-    int32_t *A_row = nullptr, *A_col = nullptr, *M_row = nullptr, *M_col = nullptr;
+    int64_t *A_sptr = nullptr;                 // SELL-32 slices of the reduced matrix
+    int32_t *A_swidth = nullptr, *A_col = nullptr, *M_row = nullptr, *M_col = nullptr;
     double *A_val = nullptr, *A_dinv = nullptr, *M_val = nullptr;
+    double *phi0 = nullptr;                    // zero-potential solution (superposition mode)
+    bool phi0_valid = false;
+    double *lap = nullptr;                     // [n_obj][ndof] unit-potential Laplace solutions
     int32_t *bc_kind = nullptr;
     double *bc_value = nullptr, *w_ext = nullptr, *w_obj = nullptr;
     double *r = nullptr, *z = nullptr, *p0 = nullptr, *p1 = nullptr, *Ap = nullptr, *pcg_part = nullptr;
     int32_t *pcg_out_i = nullptr;
     double *pcg_out_d = nullptr;
+    float *A_val32 = nullptr, *A_dinv32 = nullptr;   // mixed PCG
+    float *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *Ap32 = nullptr;
     double *obj_pot = nullptr, *image = nullptr;
     bool has_dirichlet = false;
     bool phi_valid = false;
@@ -317,20 +324,23 @@ static int object_index(const pg_sim *s, int64_t bnd_id) {
     return (k >= 0 && k < s->n_obj) ? (int)k : -1;
 }
 
-// One Poisson solve with the given object potentials; rho from s->rho or zero.
+// One Poisson solve with the given object potentials into x (s->phi unless
+// given); rho from s->rho or zero; warm start from x's previous content when
+// `warm` and configured.
 static int poisson_solve_internal(pg_sim *s, const double *pot_h, bool zero_rho, bool use_ext, double rtol,
-                                  double atol, pg_solve_info *acc) {
+                                  double atol, pg_solve_info *acc, double *x_target = nullptr, bool *warm = nullptr) {
     if (s->n_obj > 0) PG_CUDA(cudaMemcpyAsync(s->obj_pot, pot_h, sizeof(double) * s->n_obj, cudaMemcpyHostToDevice, s->stream));
     if (zero_rho) PG_CUDA(cudaMemsetAsync(s->rho_acc, 0, sizeof(double) * s->ndof, s->stream));
     launch_rhs(s->dm, s->M_row, s->M_col, s->M_val, zero_rho ? s->rho_acc : s->rho, s->bc_kind, s->bc_value, s->w_ext,
                s->w_obj, s->obj_pot, s->n_obj, use_ext ? 1 : 0, s->b, s->stream);
     if (zero_rho) s->rho_valid = false;
-    double *x = s->phi;
-    if (!(s->cfg.pcg_warm_start && s->phi_valid) || zero_rho) PG_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * s->ndof, s->stream));
+    double *x = x_target ? x_target : s->phi;
+    bool *valid = warm ? warm : &s->phi_valid;
+    if (!(s->cfg.pcg_warm_start && *valid) || zero_rho) PG_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * s->ndof, s->stream));
     launch_set_bc(s->bc_kind, use_ext ? s->bc_value : nullptr, s->obj_pot, s->ndof, x, s->stream);
     PcgArgs a{};
     a.n = s->ndof;
-    a.rowptr = s->A_row; a.col = s->A_col; a.val = s->A_val; a.dinv = s->A_dinv;
+    a.slice_ptr = s->A_sptr; a.slice_width = s->A_swidth; a.col = s->A_col; a.val = s->A_val; a.dinv = s->A_dinv;
     a.b = s->b; a.x = x; a.r = s->r; a.z = s->z; a.p0 = s->p0; a.p1 = s->p1; a.Ap = s->Ap;
     a.partials = s->pcg_part;
     a.rtol = rtol; a.atol = atol;
@@ -338,6 +348,9 @@ static int poisson_solve_internal(pg_sim *s, const double *pot_h, bool zero_rho,
     a.remove_mean = s->cfg.periodic ? 1 : 0;
     a.out_iter = s->pcg_out_i; a.out_status = s->pcg_out_i + 1;
     a.out_rr = s->pcg_out_d; a.out_bb = s->pcg_out_d + 1;
+    a.val32 = s->A_val32; a.dinv32 = s->A_dinv32;
+    a.r32 = s->r32; a.z32 = s->z32; a.p32 = s->p32; a.Ap32 = s->Ap32;
+    a.out_updates = nullptr;
     int e;
     {
         StageScope t(s, "pcg");
@@ -349,7 +362,7 @@ static int poisson_solve_internal(pg_sim *s, const double *pot_h, bool zero_rho,
     PG_CUDA(cudaMemcpyAsync(oi, s->pcg_out_i, sizeof(oi), cudaMemcpyDeviceToHost, s->stream));
     PG_CUDA(cudaMemcpyAsync(od, s->pcg_out_d, sizeof(od), cudaMemcpyDeviceToHost, s->stream));
     PG_CUDA(cudaStreamSynchronize(s->stream));
-    s->phi_valid = true;
+    *valid = true;
     if (acc) {
         acc->iterations += oi[0];
         acc->solves += 1;
@@ -361,24 +374,74 @@ static int poisson_solve_internal(pg_sim *s, const double *pot_h, bool zero_rho,
     return PG_OK;
 }
 
-static int image_charges(pg_sim *s, std::vector<double> &out) {
+static int image_charges(pg_sim *s, std::vector<double> &out, const double *phi = nullptr) {
     out.assign(s->n_obj, 0.0);
     if (s->n_obj == 0) return PG_OK;
-    launch_image_charge(s->dm, s->phi, s->d_ofacets, s->n_ofac, s->n_obj, s->cfg.eps0, s->image, s->stream);
+    launch_image_charge(s->dm, phi ? phi : s->phi, s->d_ofacets, s->n_ofac, s->n_obj, s->cfg.eps0, s->image, s->stream);
     PG_CUDA(cudaMemcpyAsync(out.data(), s->image, sizeof(double) * s->n_obj, cudaMemcpyDeviceToHost, s->stream));
     PG_CUDA(cudaStreamSynchronize(s->stream));
     return PG_OK;
 }
 
+static bool is_mixed(const pg_sim *s) { return s->cfg.precision == PG_MIXED; }
+
+// Fixed-point unit of the mixed deposit: 2^-40 of the largest |q|.
+static double fixed_unit(const pg_sim *s) {
+    double qmax = 0.0;
+    for (int k = 0; k < s->n_species; ++k) qmax = std::max(qmax, std::fabs(s->q[k]));
+    if (qmax == 0.0) qmax = 1.0;
+    return std::ldexp(qmax, -40);
+}
+
+static void fill_mixed(const pg_sim *s, MixedParams &mp, double dt_push, const double *B, bool accel, double dt_move,
+                       bool periodic, const double *Ld) {
+    mp = MixedParams{};
+    mp.accel = accel ? 1 : 0;
+    mp.has_B = (!accel && B && (B[0] != 0.0 || B[1] != 0.0 || B[2] != 0.0)) ? 1 : 0;
+    const double unit = fixed_unit(s);
+    for (int k = 0; k < s->n_species; ++k) {
+        const double q = s->q[k], m = s->m[k];
+        mp.coef[k] = (float)(accel ? dt_push * (q / m) : 0.5 * dt_push * (q / m));
+        mp.half_m[k] = (float)(0.5 * m);
+        mp.q_scaled[k] = (float)(q / unit);
+        if (mp.has_B) {
+            double t[3], t2 = 0.0;
+            for (int i = 0; i < 3; ++i) { t[i] = std::tan((dt_push * q / (2.0 * m)) * B[i]); t2 += t[i] * t[i]; }
+            for (int i = 0; i < 3; ++i) { mp.t[k][i] = (float)t[i]; mp.s[k][i] = (float)(2 * t[i] / (1 + t2)); }
+        }
+    }
+    mp.dt = (float)dt_move;
+    mp.periodic = periodic ? 1 : 0;
+    for (int j = 0; j < 3; ++j) mp.Ld[j] = Ld ? (float)Ld[j] : 1.0f;
+}
+
 static int rho_from_acc(pg_sim *s) {
-    launch_scale(s->rho_acc, s->dm.dv_inv, s->rho, s->ndof, s->stream);
+    if (is_mixed(s))
+        launch_fixed_to_rho(s->rho_fixed, s->dm.dv_inv, fixed_unit(s), s->ndof, s->rho_acc, s->rho, s->stream);
+    else
+        launch_scale(s->rho_acc, s->dm.dv_inv, s->rho, s->ndof, s->stream);
     return PG_OK;
 }
 
-// Deposit the current particles into rho_acc (zeroed first), then rho.
+// Deposit the current particles into the accumulator (zeroed first).
+static int deposit_into_acc(pg_sim *s) {
+    if (is_mixed(s)) {
+        PG_CUDA(cudaMemsetAsync(s->rho_fixed, 0, sizeof(unsigned long long) * s->ndof, s->stream));
+        MixedParams mp;
+        fill_mixed(s, mp, 0.0, nullptr, false, 0.0, false, nullptr);
+        launch_mixed_pass(s->dm, s->P[s->cur], s->n_slots, mp, false, false, false, true, s->cfg.max_walk_steps,
+                          s->rho_fixed, s->state, s->partials, s->n_part, s->ke_dev, s->stream);
+    } else {
+        PG_CUDA(cudaMemsetAsync(s->rho_acc, 0, sizeof(double) * s->ndof, s->stream));
+        if (s->n_slots > 0) launch_deposit(s->dm, s->P[s->cur], s->n_slots, s->d_q, s->rho_acc, s->stream);
+    }
+    return PG_OK;
+}
+
+// Deposit the current particles, then rho = accumulator * dv_inv.
 static int deposit_all(pg_sim *s) {
-    PG_CUDA(cudaMemsetAsync(s->rho_acc, 0, sizeof(double) * s->ndof, s->stream));
-    if (s->n_slots > 0) launch_deposit(s->dm, s->P[s->cur], s->n_slots, s->d_q, s->rho_acc, s->stream);
+    int rc = deposit_into_acc(s);
+    if (rc) return rc;
     s->rho_valid = true;
     return rho_from_acc(s);
 }
@@ -403,11 +466,14 @@ static int solve_circuit_internal(pg_sim *s, pg_object *objects, int32_t n_objec
     }
     std::vector<double> pot(n, 0.0);
     for (int i = 0; i < n; ++i) obj[i]->potential = 0.0;
-    int rc = poisson_solve_internal(s, pot.data(), false, true, s->cfg.pcg_rtol, s->cfg.pcg_atol, info);
+    const bool superpose = !s->cfg.circuit_resolve && s->lap;
+    int rc = superpose ? poisson_solve_internal(s, pot.data(), false, true, s->cfg.pcg_rtol, s->cfg.pcg_atol, info,
+                                                s->phi0, &s->phi0_valid)
+                       : poisson_solve_internal(s, pot.data(), false, true, s->cfg.pcg_rtol, s->cfg.pcg_atol, info);
     if (rc) return rc;
     // post_solve
     std::vector<double> img;
-    rc = image_charges(s, img);
+    rc = image_charges(s, img, superpose ? s->phi0 : s->phi);
     if (rc) return rc;
     std::vector<double> &cv = s->circ_vec;
     for (auto &g : s->groups) {
@@ -438,6 +504,15 @@ static int solve_circuit_internal(pg_sim *s, pg_object *objects, int32_t n_objec
         obj[i]->potential = p;
         obj[i]->charge = c;
         pot[i] = p;
+    }
+    if (superpose) {
+        // the potential is affine in the object potentials: phi = phi0 + sum V_k L_k
+        Pots pv{};
+        pv.n = n;
+        for (int i = 0; i < n; ++i) pv.v[i] = pot[i];
+        launch_superpose(s->phi0, s->lap, pv, s->ndof, s->phi, s->stream);
+        s->phi_valid = true;
+        return PG_OK;
     }
     // correction solve with the new potentials
     return poisson_solve_internal(s, pot.data(), false, true, s->cfg.pcg_rtol, s->cfg.pcg_atol, info);
@@ -523,12 +598,17 @@ static int inject_internal(pg_sim *s, double dt, uint64_t seed, uint64_t step, b
     for (int k = 0; k < ip.n_species; ++k) ipd.sp[k] = ip.sp[k];
     ipd.slot_base = s->n_slots;
     ipd.pid_base = s->next_pid;
+    ipd.rho_fixed = s->rho_fixed;
+    {
+        const double unit = fixed_unit(s);
+        for (int k = 0; k < s->n_species; ++k) ipd.q_scaled[k] = (float)(s->q[k] / unit);
+    }
     PG_CUDA(cudaMemsetAsync(s->inj_counts, 0, sizeof(int64_t) * (total + 1), s->stream));
     PG_CUDA(cudaMemsetAsync(s->state->injected, 0, sizeof(s->state->injected), s->stream));
     launch_inject_count(s->dm, ipd, s->flux_num, s->inj_counts, s->stream);
     launch_scan_i64(s->inj_counts, s->inj_offsets, total + 1, s->scan_tmp, s->stream);
     launch_inject_generate(s->dm, s->P[s->cur], ipd, s->flux_num, s->pdf_max, s->d_ext_facets, s->inj_offsets,
-                           s->cfg.max_walk_steps, deposit ? 1 : 0, s->d_q, s->rho_acc, s->state, s->stream);
+                           s->cfg.max_walk_steps, deposit ? 1 : 0, s->d_q, s->rho_acc, s->state, bound, s->stream);
     rc = check_state(s);
     if (rc) return rc;
     const int64_t appended = s->state_h->inject_total;
@@ -595,6 +675,20 @@ int pg_create(const pg_mesh *mesh, const pg_config *cfg_in, pg_sim **out) {
         (rc = upload(s, &d_dofs, dof32)) || (rc = upload(s, &d_dvinv, h.dv_inv)) || (rc = dalloc(s, &d_E, 4 * h.nc)))
         return bail(rc);
     cudaMemset(d_E, 0, sizeof(double) * 4 * h.nc);
+    if (cfg.precision == PG_MIXED) {
+        float *pf, *bf, *ef;
+        if ((rc = dalloc(s, &pf, 16 * h.nc)) || (rc = dalloc(s, &bf, 12 * h.nc)) || (rc = dalloc(s, &ef, 4 * h.nc)) ||
+            (rc = dalloc(s, &s->rho_fixed, h.ndof)))
+            return bail(rc);
+        cudaMemset(ef, 0, sizeof(float) * 4 * h.nc);
+        cudaMemset(s->rho_fixed, 0, sizeof(unsigned long long) * h.ndof);
+        launch_float_tables(d_planes, d_bary, (int32_t)h.nc, pf, bf, s->stream);
+        s->dm.planes_f = pf;
+        s->dm.bary_f = bf;
+        s->dm.E_f = ef;
+    } else if (cfg.precision != PG_FP64) {
+        return bail(fail(PG_ERR_ARG, "pg_create: unknown precision"));
+    }
     s->dm.nc = s->nc;
     s->dm.ndof = s->ndof;
     s->dm.planes = d_planes;
@@ -663,7 +757,30 @@ int pg_create(const pg_mesh *mesh, const pg_config *cfg_in, pg_sim **out) {
         }
         for (int64_t i = 0; i <= nd; ++i) mrow[i] = (int32_t)h.rowptr[i];
         for (size_t k = 0; k < h.col.size(); ++k) mcol[k] = (int32_t)h.col[k];
-        if ((rc = upload(s, &s->A_row, arow)) || (rc = upload(s, &s->A_col, acol)) || (rc = upload(s, &s->A_val, aval)) ||
+        // SELL-32: slice s holds rows 32s..32s+31 column-major, padded with (row, 0.0)
+        const int64_t nsl = (nd + 31) / 32;
+        std::vector<int64_t> sptr(nsl + 1, 0);
+        std::vector<int32_t> swidth(nsl, 0);
+        for (int64_t sl = 0; sl < nsl; ++sl) {
+            int32_t w = 0;
+            for (int64_t r = 32 * sl; r < std::min(nd, 32 * sl + 32); ++r) w = std::max(w, arow[r + 1] - arow[r]);
+            swidth[sl] = w;
+            sptr[sl + 1] = sptr[sl] + 32 * (int64_t)w;
+        }
+        std::vector<int32_t> scol(sptr[nsl]);
+        std::vector<double> sval(sptr[nsl], 0.0);
+        for (int64_t sl = 0; sl < nsl; ++sl)
+            for (int lane = 0; lane < 32; ++lane) {
+                const int64_t r = 32 * sl + lane;
+                const int32_t len = r < nd ? arow[r + 1] - arow[r] : 0;
+                for (int32_t k = 0; k < swidth[sl]; ++k) {
+                    const int64_t o = sptr[sl] + 32 * (int64_t)k + lane;
+                    if (k < len) { scol[o] = acol[arow[r] + k]; sval[o] = aval[arow[r] + k]; }
+                    else { scol[o] = (int32_t)std::min<int64_t>(r, nd - 1); sval[o] = 0.0; }
+                }
+            }
+        if ((rc = upload(s, &s->A_sptr, sptr)) || (rc = upload(s, &s->A_swidth, swidth)) ||
+            (rc = upload(s, &s->A_col, scol)) || (rc = upload(s, &s->A_val, sval)) || (rc = dalloc(s, &s->phi0, nd)) ||
             (rc = upload(s, &s->A_dinv, dinv)) || (rc = upload(s, &s->M_row, mrow)) || (rc = upload(s, &s->M_col, mcol)) ||
             (rc = upload(s, &s->M_val, h.M)) || (rc = upload(s, &s->bc_kind, kind)) || (rc = upload(s, &s->bc_value, gval)) ||
             (rc = upload(s, &s->w_ext, wext)) || (rc = upload(s, &s->w_obj, wobj)))
@@ -674,6 +791,16 @@ int pg_create(const pg_mesh *mesh, const pg_config *cfg_in, pg_sim **out) {
             (rc = dalloc(s, &s->pcg_out_i, 2)) || (rc = dalloc(s, &s->pcg_out_d, 2)) ||
             (rc = dalloc(s, &s->obj_pot, std::max(1, s->n_obj))) || (rc = dalloc(s, &s->image, std::max(1, s->n_obj))))
             return bail(rc);
+        const int mode = cfg.pcg_precision == 0 ? (cfg.precision == PG_MIXED ? 2 : 1) : cfg.pcg_precision;
+        if (mode == 2) {
+            std::vector<float> v32(sval.begin(), sval.end()), d32(dinv.begin(), dinv.end());
+            if ((rc = upload(s, &s->A_val32, v32)) || (rc = upload(s, &s->A_dinv32, d32)) ||
+                (rc = dalloc(s, &s->r32, nd)) || (rc = dalloc(s, &s->z32, nd)) || (rc = dalloc(s, &s->p32, nd)) ||
+                (rc = dalloc(s, &s->Ap32, nd)))
+                return bail(rc);
+        } else if (mode != 1) {
+            return bail(fail(PG_ERR_ARG, "pg_create: unknown pcg_precision"));
+        }
     }
 
     // boundary facets
@@ -736,15 +863,22 @@ int pg_add_particles(pg_sim *s, const double *xs, const double *vs, int64_t n, d
     if (!s || (n > 0 && (!xs || !vs)) || n < 0) return fail(PG_ERR_ARG, "pg_add_particles: bad arguments");
     if (n_added) *n_added = 0;
     if (n == 0) return PG_OK;
-    if (s->cfg.precision == PG_MIXED) return fail(PG_ERR_STATE, "pg_add_particles: the mixed form is not built yet");
     const int sp = species_id(s, q, m);
     if (sp < 0) return fail(PG_ERR_ARG, "pg_add_particles: more than 8 species");
+    // the mixed form stores FP32 positions: locate the rounded points
+    std::vector<double> rounded;
+    const double *pos = xs;
+    if (is_mixed(s)) {
+        rounded.resize(3 * n);
+        for (int64_t k = 0; k < 3 * n; ++k) rounded[k] = (double)(float)xs[k];
+        pos = rounded.data();
+    }
     double *d_xyz = nullptr;
     int32_t *d_cells = nullptr;
     PG_CUDA(cudaMalloc(&d_xyz, sizeof(double) * 3 * n));
     PG_CUDA(cudaMalloc(&d_cells, sizeof(int32_t) * n));
     std::vector<int32_t> cells(n);
-    cudaMemcpyAsync(d_xyz, xs, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->stream);
+    cudaMemcpyAsync(d_xyz, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->stream);
     launch_locate(s->dm, d_xyz, n, d_cells, s->stream);
     cudaMemcpyAsync(cells.data(), d_cells, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s->stream);
     cudaError_t e = cudaStreamSynchronize(s->stream);
@@ -768,12 +902,21 @@ int pg_add_particles(pg_sim *s, const double *xs, const double *vs, int64_t n, d
     if (rc) return rc;
     const DevParticles &P = s->P[s->cur];
     const int64_t o = s->n_slots;
-    PG_CUDA(cudaMemcpy(P.x + o, hx.data(), 8 * k, cudaMemcpyHostToDevice));
-    PG_CUDA(cudaMemcpy(P.y + o, hy.data(), 8 * k, cudaMemcpyHostToDevice));
-    PG_CUDA(cudaMemcpy(P.z + o, hz.data(), 8 * k, cudaMemcpyHostToDevice));
-    PG_CUDA(cudaMemcpy(P.vx + o, hvx.data(), 8 * k, cudaMemcpyHostToDevice));
-    PG_CUDA(cudaMemcpy(P.vy + o, hvy.data(), 8 * k, cudaMemcpyHostToDevice));
-    PG_CUDA(cudaMemcpy(P.vz + o, hvz.data(), 8 * k, cudaMemcpyHostToDevice));
+    if (is_mixed(s)) {
+        auto up = [&](float *dst, const std::vector<double> &src) {
+            std::vector<float> f(src.begin(), src.end());
+            return cudaMemcpy(dst + o, f.data(), 4 * k, cudaMemcpyHostToDevice);
+        };
+        PG_CUDA(up(P.xf, hx)); PG_CUDA(up(P.yf, hy)); PG_CUDA(up(P.zf, hz));
+        PG_CUDA(up(P.vxf, hvx)); PG_CUDA(up(P.vyf, hvy)); PG_CUDA(up(P.vzf, hvz));
+    } else {
+        PG_CUDA(cudaMemcpy(P.x + o, hx.data(), 8 * k, cudaMemcpyHostToDevice));
+        PG_CUDA(cudaMemcpy(P.y + o, hy.data(), 8 * k, cudaMemcpyHostToDevice));
+        PG_CUDA(cudaMemcpy(P.z + o, hz.data(), 8 * k, cudaMemcpyHostToDevice));
+        PG_CUDA(cudaMemcpy(P.vx + o, hvx.data(), 8 * k, cudaMemcpyHostToDevice));
+        PG_CUDA(cudaMemcpy(P.vy + o, hvy.data(), 8 * k, cudaMemcpyHostToDevice));
+        PG_CUDA(cudaMemcpy(P.vz + o, hvz.data(), 8 * k, cudaMemcpyHostToDevice));
+    }
     PG_CUDA(cudaMemcpy(P.cell + o, hc.data(), 4 * k, cudaMemcpyHostToDevice));
     PG_CUDA(cudaMemcpy(P.sp + o, hs.data(), k, cudaMemcpyHostToDevice));
     PG_CUDA(cudaMemcpy(P.pid + o, hp.data(), 8 * k, cudaMemcpyHostToDevice));
@@ -814,13 +957,24 @@ int pg_get_particles(pg_sim *s, int64_t capacity, double *x, double *v, double *
     std::vector<uint8_t> hs(n);
     std::vector<int64_t> hp(n);
     PG_CUDA(cudaStreamSynchronize(s->stream));
-    if (n > 0) {
+    if (n > 0 && is_mixed(s)) {
+        std::vector<float> f(n);
+        auto dn = [&](std::vector<double> &dst, const float *src) {
+            cudaError_t e = cudaMemcpy(f.data(), src, 4 * n, cudaMemcpyDeviceToHost);
+            for (int64_t i = 0; i < n; ++i) dst[i] = f[i];
+            return e;
+        };
+        PG_CUDA(dn(hx, P.xf)); PG_CUDA(dn(hy, P.yf)); PG_CUDA(dn(hz, P.zf));
+        PG_CUDA(dn(hvx, P.vxf)); PG_CUDA(dn(hvy, P.vyf)); PG_CUDA(dn(hvz, P.vzf));
+    } else if (n > 0) {
         PG_CUDA(cudaMemcpy(hx.data(), P.x, 8 * n, cudaMemcpyDeviceToHost));
         PG_CUDA(cudaMemcpy(hy.data(), P.y, 8 * n, cudaMemcpyDeviceToHost));
         PG_CUDA(cudaMemcpy(hz.data(), P.z, 8 * n, cudaMemcpyDeviceToHost));
         PG_CUDA(cudaMemcpy(hvx.data(), P.vx, 8 * n, cudaMemcpyDeviceToHost));
         PG_CUDA(cudaMemcpy(hvy.data(), P.vy, 8 * n, cudaMemcpyDeviceToHost));
         PG_CUDA(cudaMemcpy(hvz.data(), P.vz, 8 * n, cudaMemcpyDeviceToHost));
+    }
+    if (n > 0) {
         PG_CUDA(cudaMemcpy(hc.data(), P.cell, 4 * n, cudaMemcpyDeviceToHost));
         PG_CUDA(cudaMemcpy(hs.data(), P.sp, n, cudaMemcpyDeviceToHost));
         PG_CUDA(cudaMemcpy(hp.data(), P.pid, 8 * n, cudaMemcpyDeviceToHost));
@@ -900,7 +1054,14 @@ static int push_common(pg_sim *s, const double *B, double dt, bool accel, double
     PushParams pp;
     fill_push(s, pp, dt, B, accel);
     if (s->n_slots > 0) {
-        launch_push(s->dm, s->P[s->cur], s->n_slots, pp, s->partials, s->n_part, s->ke_dev, s->stream);
+        if (is_mixed(s)) {
+            MixedParams mp;
+            fill_mixed(s, mp, dt, B, accel, 0.0, false, nullptr);
+            launch_mixed_pass(s->dm, s->P[s->cur], s->n_slots, mp, true, false, false, false, s->cfg.max_walk_steps,
+                              s->rho_fixed, s->state, s->partials, s->n_part, s->ke_dev, s->stream);
+        } else {
+            launch_push(s->dm, s->P[s->cur], s->n_slots, pp, s->partials, s->n_part, s->ke_dev, s->stream);
+        }
         double ke = 0;
         PG_CUDA(cudaMemcpyAsync(&ke, s->ke_dev, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
         PG_CUDA(cudaStreamSynchronize(s->stream));
@@ -914,11 +1075,19 @@ static int push_common(pg_sim *s, const double *B, double dt, bool accel, double
 int pg_accel(pg_sim *s, double dt, double *KE) { return push_common(s, nullptr, dt, true, KE); }
 int pg_boris(pg_sim *s, const double B[3], double dt, double *KE) { return push_common(s, B, dt, false, KE); }
 
+static void move_mixed(pg_sim *s, double dt, bool periodic, const double *Ld) {
+    MixedParams mp;
+    fill_mixed(s, mp, 0.0, nullptr, false, dt, periodic, Ld);
+    launch_mixed_pass(s->dm, s->P[s->cur], s->n_slots, mp, false, true, false, false, s->cfg.max_walk_steps,
+                      s->rho_fixed, s->state, s->partials, s->n_part, s->ke_dev, s->stream);
+}
+
 int pg_move(pg_sim *s, double dt) {
     if (!s) return fail(PG_ERR_ARG, "NULL handle");
     MoveParams mp{};
     mp.dt = dt;
-    if (s->n_slots > 0) launch_move(s->P[s->cur], s->n_slots, mp, s->stream);
+    if (s->n_slots > 0 && is_mixed(s)) move_mixed(s, dt, false, nullptr);
+    else if (s->n_slots > 0) launch_move(s->P[s->cur], s->n_slots, mp, s->stream);
     PG_CUDA(cudaStreamSynchronize(s->stream));
     s->rho_valid = false;
     return PG_OK;
@@ -930,7 +1099,8 @@ int pg_move_periodic(pg_sim *s, double dt, const double Ld[3]) {
     mp.dt = dt;
     mp.periodic = 1;
     for (int j = 0; j < 3; ++j) mp.Ld[j] = Ld[j];
-    if (s->n_slots > 0) launch_move(s->P[s->cur], s->n_slots, mp, s->stream);
+    if (s->n_slots > 0 && is_mixed(s)) move_mixed(s, dt, true, Ld);
+    else if (s->n_slots > 0) launch_move(s->P[s->cur], s->n_slots, mp, s->stream);
     PG_CUDA(cudaStreamSynchronize(s->stream));
     s->rho_valid = false;
     return PG_OK;
@@ -939,7 +1109,14 @@ int pg_move_periodic(pg_sim *s, double dt, const double Ld[3]) {
 int pg_update(pg_sim *s, pg_object *objects, int32_t n_objects, double dt) {
     if (!s || (n_objects > 0 && !objects)) return fail(PG_ERR_ARG, "pg_update: bad arguments");
     PG_CUDA(cudaMemsetAsync(s->state->absorbed, 0, sizeof(s->state->absorbed), s->stream));
-    if (s->n_slots > 0) launch_update(s->dm, s->P[s->cur], s->n_slots, s->cfg.max_walk_steps, s->state, s->stream);
+    if (s->n_slots > 0 && is_mixed(s)) {
+        MixedParams mp;
+        fill_mixed(s, mp, 0.0, nullptr, false, 0.0, false, nullptr);
+        launch_mixed_pass(s->dm, s->P[s->cur], s->n_slots, mp, false, false, true, false, s->cfg.max_walk_steps,
+                          s->rho_fixed, s->state, s->partials, s->n_part, s->ke_dev, s->stream);
+    } else if (s->n_slots > 0) {
+        launch_update(s->dm, s->P[s->cur], s->n_slots, s->cfg.max_walk_steps, s->state, s->stream);
+    }
     int rc = check_state(s);
     s->rho_valid = false;
     if (rc) return rc;
@@ -953,7 +1130,13 @@ int pg_kinetic_energy(pg_sim *s, double *KE) {
     for (int k = 0; k < s->n_species; ++k) hm[k] = 0.5 * s->m[k];
     *KE = 0.0;
     if (s->n_slots == 0) return PG_OK;
-    launch_kinetic(s->P[s->cur], s->n_slots, hm, s->partials, s->n_part, s->ke_dev, s->stream);
+    if (is_mixed(s)) {
+        MixedParams mp;
+        fill_mixed(s, mp, 0.0, nullptr, false, 0.0, false, nullptr);
+        launch_kinetic_mixed(s->P[s->cur], s->n_slots, mp, s->partials, s->n_part, s->ke_dev, s->stream);
+    } else {
+        launch_kinetic(s->P[s->cur], s->n_slots, hm, s->partials, s->n_part, s->ke_dev, s->stream);
+    }
     PG_CUDA(cudaMemcpyAsync(KE, s->ke_dev, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     PG_CUDA(cudaStreamSynchronize(s->stream));
     return PG_OK;
@@ -1021,16 +1204,25 @@ int pg_circuit_cm_setup(pg_sim *s, const pg_source *vs, int32_t nvs, const pg_so
     // capacitance matrix: one Laplace solve per object (inv_capacitance,
     // punc/src/object_CM.cpp:62-106 and laplace_solver 401-437).
     std::vector<double> cap(n * n, 0.0);
+    if (!s->lap) {
+        int rc = dalloc(s, &s->lap, (size_t)n * s->ndof);
+        if (rc) return rc;
+    }
     for (int j = 0; j < n; ++j) {
         std::vector<double> pot(n, 0.0);
         pot[j] = 1.0;
-        int rc = poisson_solve_internal(s, pot.data(), true, false, 1e-12, 1e-14, nullptr);
+        // the reference's laplace_solver uses the PoissonSolver defaults (rel 1e-12, abs 1e-14)
+        int rc = poisson_solve_internal(s, pot.data(), true, false, std::min(1e-12, s->cfg.pcg_rtol),
+                                        std::min(1e-14, s->cfg.pcg_atol), nullptr);
         if (rc) return rc;
         std::vector<double> img;
         rc = image_charges(s, img);
         if (rc) return rc;
         for (int i = 0; i < n; ++i) cap[i * n + j] = img[i];
+        PG_CUDA(cudaMemcpyAsync(s->lap + (size_t)j * s->ndof, s->phi, sizeof(double) * s->ndof,
+                                cudaMemcpyDeviceToDevice, s->stream));
     }
+    s->phi0_valid = false;
     s->phi_valid = false;
     s->inv_cap = cap;
     if (!invert(s->inv_cap, n)) return fail(PG_ERR_SINGULAR, "capacitance matrix is singular");
@@ -1173,8 +1365,8 @@ int pg_step(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_obje
     {
         StageScope t(s, "distributor");
         if (!s->rho_valid) {
-            PG_CUDA(cudaMemsetAsync(s->rho_acc, 0, sizeof(double) * s->ndof, s->stream));
-            if (s->n_slots > 0) launch_deposit(s->dm, s->P[s->cur], s->n_slots, s->d_q, s->rho_acc, s->stream);
+            rc = deposit_into_acc(s);
+            if (rc) return rc;
         }
         rho_from_acc(s);
     }
@@ -1210,12 +1402,21 @@ int pg_step(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_obje
         mp.dt = a->dt;
         mp.periodic = a->periodic_move;
         for (int j = 0; j < 3; ++j) mp.Ld[j] = a->Ld[j];
-        PG_CUDA(cudaMemsetAsync(s->rho_acc, 0, sizeof(double) * s->ndof, s->stream));
         PG_CUDA(cudaMemsetAsync(s->state->absorbed, 0, sizeof(s->state->absorbed), s->stream));
-        if (s->n_slots > 0)
+        if (is_mixed(s)) {
+            PG_CUDA(cudaMemsetAsync(s->rho_fixed, 0, sizeof(unsigned long long) * s->ndof, s->stream));
+            MixedParams xp;
+            fill_mixed(s, xp, dt_push, a->B, a->use_accel != 0, a->dt, a->periodic_move != 0, a->Ld);
+            if (s->n_slots > 0)
+                launch_mixed_pass(s->dm, s->P[s->cur], s->n_slots, xp, true, true, true, true, s->cfg.max_walk_steps,
+                                  s->rho_fixed, s->state, s->partials, s->n_part, s->ke_dev, s->stream);
+        } else {
+            PG_CUDA(cudaMemsetAsync(s->rho_acc, 0, sizeof(double) * s->ndof, s->stream));
+        }
+        if (s->n_slots > 0 && !is_mixed(s))
             launch_fused_step(s->dm, s->P[s->cur], s->n_slots, pp, mp, s->cfg.max_walk_steps, s->d_q, s->rho_acc,
                               s->state, s->partials, s->n_part, s->ke_dev, s->stream);
-        else
+        else if (s->n_slots == 0)
             PG_CUDA(cudaMemsetAsync(s->ke_dev, 0, sizeof(double), s->stream));
         double ke = 0;
         PG_CUDA(cudaMemcpyAsync(&ke, s->ke_dev, sizeof(double), cudaMemcpyDeviceToHost, s->stream));

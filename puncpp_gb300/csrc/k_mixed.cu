@@ -1,0 +1,208 @@
+// Mixed-precision particle kernels: FP32 positions and velocities, FP32
+// push and move with fused multiply-adds, the FP32 facet walk with an FP64
+// re-test of facets the particle lies within the FP32 error bound of, and the
+// int64 fixed-point CG1 deposit (bitwise identical from run to run).
+//
+// Per particle a pass reads 24 B of FP32 position and velocity, 4 B of cell
+// id and 1 B of species, and writes back 28 B; per occupied cell it reads
+// 64 B of FP32 planes, 16 B of neighbours, 48 B of FP32 barycentric rows,
+// 16 B of dofs and 16 B of FP32 field.
+#include <cuda_runtime.h>
+
+#include "pg_device.cuh"
+#include "pg_walk.cuh"
+
+namespace pg {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ double block_sum_d(double v) {
+    __shared__ double warp_part[32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) warp_part[wid] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (wid == 0) {
+        s = lane < (int)(blockDim.x >> 5) ? warp_part[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    }
+    __syncthreads();
+    return s;
+}
+
+template <bool PUSH, bool HAS_B, bool ACCEL, bool MOVE, bool PERIODIC, bool WALK, bool DEPOSIT>
+__global__ void __launch_bounds__(kThreads) k_mixed(DevMesh m, DevParticles p, int64_t n_slots, MixedParams mp,
+                                                   int max_steps, unsigned long long *__restrict__ rho_fixed,
+                                                   DevState *__restrict__ st, double *__restrict__ partials) {
+    double ke = 0.0;
+    int retests = 0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_slots; i += stride) {
+        int c = p.cell[i];
+        if (c < 0) continue;
+        const int s = p.sp[i];
+        float x = p.xf[i], y = p.yf[i], z = p.zf[i];
+        if (PUSH || MOVE) {
+            float vx = p.vxf[i], vy = p.vyf[i], vz = p.vzf[i];
+            if (PUSH) {
+                const float4 E = __ldg(reinterpret_cast<const float4 *>(m.E_f) + c);
+                const float coef = mp.coef[s], hm = mp.half_m[s];
+                if (ACCEL) {
+                    const float ax = E.x * coef, ay = E.y * coef, az = E.z * coef;
+                    ke += (double)(hm * fmaf(vx, vx + ax, fmaf(vy, vy + ay, vz * (vz + az))));
+                    vx += ax; vy += ay; vz += az;
+                } else {
+                    const float hx = coef * E.x, hy = coef * E.y, hz = coef * E.z;
+                    const float mx = vx + hx, my = vy + hy, mz = vz + hz;
+                    ke += (double)(hm * fmaf(mx, mx, fmaf(my, my, mz * mz)));
+                    float px = mx, py = my, pz = mz;
+                    if (HAS_B) {
+                        const float t0 = mp.t[s][0], t1 = mp.t[s][1], t2 = mp.t[s][2];
+                        const float s0 = mp.s[s][0], s1 = mp.s[s][1], s2 = mp.s[s][2];
+                        const float rx = mx + (my * t2 - mz * t1);
+                        const float ry = my + (mz * t0 - mx * t2);
+                        const float rz = mz + (mx * t1 - my * t0);
+                        px = mx + (ry * s2 - rz * s1);
+                        py = my + (rz * s0 - rx * s2);
+                        pz = mz + (rx * s1 - ry * s0);
+                    }
+                    vx = px + hx; vy = py + hy; vz = pz + hz;
+                }
+                p.vxf[i] = vx; p.vyf[i] = vy; p.vzf[i] = vz;
+            }
+            if (MOVE) {
+                x = fmaf(mp.dt, vx, x); y = fmaf(mp.dt, vy, y); z = fmaf(mp.dt, vz, z);
+                if (PERIODIC) {
+                    x -= mp.Ld[0] * floorf(x / mp.Ld[0]);
+                    y -= mp.Ld[1] * floorf(y / mp.Ld[1]);
+                    z -= mp.Ld[2] * floorf(z / mp.Ld[2]);
+                }
+                p.xf[i] = x; p.yf[i] = y; p.zf[i] = z;
+            }
+        }
+        if (WALK) {
+            const int nc = walk_mixed(m, x, y, z, c, max_steps, retests);
+            if (nc == kWalkFail) {
+                raise_device_error(st, PG_ERR_WALK_LIMIT, i);
+                continue;
+            }
+            if (nc < 0) {
+                const int tag = -nc;
+                atomicAdd(reinterpret_cast<unsigned long long *>(&st->absorbed[tag < kMaxTags ? tag : 0][s]), 1ull);
+                atomicAdd(reinterpret_cast<unsigned long long *>(&st->live[s]), ~0ull);
+                p.cell[i] = kDead;
+                continue;
+            }
+            if (nc != c) { p.cell[i] = nc; c = nc; }
+        }
+        if (DEPOSIT) deposit_fixed(m, c, x, y, z, mp.q_scaled[s], rho_fixed);
+    }
+    if (PUSH) {
+        const double t = block_sum_d(ke);
+        if (threadIdx.x == 0) partials[blockIdx.x] = t;
+    }
+    if (WALK && retests) atomicAdd(reinterpret_cast<unsigned long long *>(&st->retests), (unsigned long long)retests);
+}
+
+__global__ void k_sum_partials_m(const double *__restrict__ part, int n, double *__restrict__ out) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) v += part[i];
+    const double s = block_sum_d(v);
+    if (threadIdx.x == 0) *out = s;
+}
+
+__global__ void __launch_bounds__(kThreads) k_kinetic_mixed(DevParticles p, int64_t n_slots, MixedParams mp,
+                                                           double *__restrict__ partials) {
+    double ke = 0.0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_slots; i += stride) {
+        if (p.cell[i] < 0) continue;
+        const float hm = mp.half_m[p.sp[i]];
+        const float vx = p.vxf[i], vy = p.vyf[i], vz = p.vzf[i];
+        ke += (double)(hm * fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
+    }
+    const double s = block_sum_d(ke);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// rho = (sum in units of 2^-40 q_max) * q_max 2^-40 * dv_inv
+__global__ void k_fixed_to_rho(const unsigned long long *__restrict__ fixed, const double *__restrict__ dv_inv,
+                               double unit, int32_t n, double *__restrict__ rho_acc, double *__restrict__ rho) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double a = (double)(long long)fixed[i] * unit;
+    if (rho_acc) rho_acc[i] = a;
+    rho[i] = a * dv_inv[i];
+}
+
+__global__ void k_float_tables(const double *__restrict__ planes, const double *__restrict__ bary, int32_t nc,
+                               float *__restrict__ planes_f, float *__restrict__ bary_f) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    for (int k = 0; k < 16; ++k) planes_f[16 * (size_t)c + k] = (float)planes[16 * (size_t)c + k];
+    for (int k = 0; k < 12; ++k) bary_f[12 * (size_t)c + k] = (float)bary[12 * (size_t)c + k];
+}
+
+inline int grid_for(int64_t n, int max_blocks) {
+    int64_t g = (n + kThreads - 1) / kThreads;
+    if (g < 1) g = 1;
+    if (g > max_blocks) g = max_blocks;
+    return (int)g;
+}
+
+}  // namespace
+
+void launch_mixed_pass(const DevMesh &m, const DevParticles &p, int64_t n_slots, const MixedParams &mp, bool push,
+                       bool move, bool walk, bool deposit, int max_steps, unsigned long long *rho_fixed,
+                       DevState *state, double *partials, int nblocks, double *ke_out, cudaStream_t st) {
+    if (n_slots <= 0) return;
+    const int g = grid_for(n_slots, push ? nblocks : (1 << 20));
+    count_launches(push ? 2 : 1);
+#define PG_MIX(PU, HB, AC, MO, PE, WA, DE) \
+    k_mixed<PU, HB, AC, MO, PE, WA, DE><<<g, kThreads, 0, st>>>(m, p, n_slots, mp, max_steps, rho_fixed, state, partials)
+    if (push && move && walk && deposit) {
+        if (mp.accel) { if (mp.periodic) PG_MIX(true, false, true, true, true, true, true); else PG_MIX(true, false, true, true, false, true, true); }
+        else if (mp.has_B) { if (mp.periodic) PG_MIX(true, true, false, true, true, true, true); else PG_MIX(true, true, false, true, false, true, true); }
+        else { if (mp.periodic) PG_MIX(true, false, false, true, true, true, true); else PG_MIX(true, false, false, true, false, true, true); }
+    } else if (push) {
+        if (mp.accel) PG_MIX(true, false, true, false, false, false, false);
+        else if (mp.has_B) PG_MIX(true, true, false, false, false, false, false);
+        else PG_MIX(true, false, false, false, false, false, false);
+    } else if (move) {
+        if (mp.periodic) PG_MIX(false, false, false, true, true, false, false);
+        else PG_MIX(false, false, false, true, false, false, false);
+    } else if (walk) {
+        PG_MIX(false, false, false, false, false, true, false);
+    } else if (deposit) {
+        PG_MIX(false, false, false, false, false, false, true);
+    }
+#undef PG_MIX
+    if (push) k_sum_partials_m<<<1, 1024, 0, st>>>(partials, g, ke_out);
+}
+
+void launch_kinetic_mixed(const DevParticles &p, int64_t n_slots, const MixedParams &mp, double *partials, int nblocks,
+                          double *ke_out, cudaStream_t st) {
+    const int g = grid_for(n_slots, nblocks);
+    count_launches(2);
+    k_kinetic_mixed<<<g, kThreads, 0, st>>>(p, n_slots, mp, partials);
+    k_sum_partials_m<<<1, 1024, 0, st>>>(partials, g, ke_out);
+}
+
+void launch_fixed_to_rho(const unsigned long long *fixed, const double *dv_inv, double unit, int32_t n,
+                         double *rho_acc, double *rho, cudaStream_t st) {
+    if (n <= 0) return;
+    count_launches(1);
+    k_fixed_to_rho<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(fixed, dv_inv, unit, n, rho_acc, rho);
+}
+
+void launch_float_tables(const double *planes, const double *bary, int32_t nc, float *planes_f, float *bary_f,
+                         cudaStream_t st) {
+    if (nc <= 0) return;
+    count_launches(1);
+    k_float_tables<<<(nc + kThreads - 1) / kThreads, kThreads, 0, st>>>(planes, bary, nc, planes_f, bary_f);
+}
+
+}  // namespace pg

@@ -9,16 +9,13 @@
 #include <atomic>
 
 #include "pg_device.cuh"
+#include "pg_walk.cuh"
 
 namespace pg {
 
 namespace {
 
 constexpr int kThreads = 256;
-
-__device__ __forceinline__ void raise_error(DevState *st, int code, int64_t idx) {
-    if (atomicCAS(&st->err_code, 0, code) == 0) st->err_index = idx;
-}
 
 __device__ __forceinline__ double block_sum(double v) {
     __shared__ double warp_part[32];
@@ -36,32 +33,6 @@ __device__ __forceinline__ double block_sum(double v) {
     return s;  // valid in thread 0
 }
 
-// relocate_fast (punc/include/punc/population.h:539-569) as a loop: the first
-// facet i (in order 0..3) whose plane value c0 + c1 x + c2 y + c3 z, summed
-// left to right, is > 0 moves the walk to neighbour i or ends it with -tag;
-// no positive facet ends it in the current cell.
-__device__ __forceinline__ int walk_fp64(const DevMesh &m, double x, double y, double z, int c, int max_steps) {
-    for (int it = 0; it < max_steps; ++it) {
-        const double2 *P = reinterpret_cast<const double2 *>(m.planes) + 8 * (size_t)c;
-        const double2 q0 = __ldg(P + 0), q1 = __ldg(P + 1), q2 = __ldg(P + 2), q3 = __ldg(P + 3);
-        const double2 q4 = __ldg(P + 4), q5 = __ldg(P + 5), q6 = __ldg(P + 6), q7 = __ldg(P + 7);
-        const int4 nb = __ldg(m.nbr + c);
-        double d0 = q0.x + q0.y * x; d0 = d0 + q1.x * y; d0 = d0 + q1.y * z;
-        double d1 = q2.x + q2.y * x; d1 = d1 + q3.x * y; d1 = d1 + q3.y * z;
-        double d2 = q4.x + q4.y * x; d2 = d2 + q5.x * y; d2 = d2 + q5.y * z;
-        double d3 = q6.x + q6.y * x; d3 = d3 + q7.x * y; d3 = d3 + q7.y * z;
-        int next;
-        if (d0 > 0) next = nb.x;
-        else if (d1 > 0) next = nb.y;
-        else if (d2 > 0) next = nb.z;
-        else if (d3 > 0) next = nb.w;
-        else return c;
-        if (next < 0) return next;
-        c = next;
-    }
-    return kWalkFail;
-}
-
 // All four plane values <= 0: the point is in the cell (the walk would stay).
 __device__ __forceinline__ bool inside_fp64(const DevMesh &m, double x, double y, double z, int c) {
     const double2 *P = reinterpret_cast<const double2 *>(m.planes) + 8 * (size_t)c;
@@ -71,18 +42,6 @@ __device__ __forceinline__ bool inside_fp64(const DevMesh &m, double x, double y
         if (d > 0) return false;
     }
     return true;
-}
-
-// Cell<3>::barycentric (punc/include/punc/population.h:885-893).
-__device__ __forceinline__ void barycentric_fp64(const DevMesh &m, int c, double x, double y, double z,
-                                                 double &l0, double &l1, double &l2, double &l3) {
-    const double2 *A = reinterpret_cast<const double2 *>(m.bary) + 6 * (size_t)c;
-    const double2 a0 = __ldg(A + 0), a1 = __ldg(A + 1), a2 = __ldg(A + 2);
-    const double2 a3 = __ldg(A + 3), a4 = __ldg(A + 4), a5 = __ldg(A + 5);
-    l0 = a0.x + a0.y * x; l0 = l0 + a1.x * y; l0 = l0 + a1.y * z;
-    l1 = a2.x + a2.y * x; l1 = l1 + a3.x * y; l1 = l1 + a3.y * z;
-    l2 = a4.x + a4.y * x; l2 = l2 + a5.x * y; l2 = l2 + a5.y * z;
-    l3 = 1.0 - l0 - l1 - l2;
 }
 
 // One pass over the particle slots doing any of push, move, walk and deposit.
@@ -153,7 +112,7 @@ __global__ void __launch_bounds__(kThreads) k_particles(DevMesh m, DevParticles 
             // Population::update (punc/include/punc/population.h:641-699).
             const int nc = walk_fp64(m, x, y, z, c, max_steps);
             if (nc == kWalkFail) {
-                raise_error(st, PG_ERR_WALK_LIMIT, i);
+                raise_device_error(st, PG_ERR_WALK_LIMIT, i);
                 continue;
             }
             if (nc < 0) {

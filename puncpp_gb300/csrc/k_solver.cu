@@ -29,8 +29,10 @@ __global__ void k_efield(DevMesh m, const double *__restrict__ phi, double e0x, 
     const double gy = a * A[2] + b * A[6] + e * A[10];
     const double gz = a * A[3] + b * A[7] + e * A[11];
     double2 *E = reinterpret_cast<double2 *>(m.E) + 2 * (size_t)c;
-    E[0] = make_double2(-gx + e0x, -gy + e0y);
-    E[1] = make_double2(-gz + e0z, 0.0);
+    const double ex = -gx + e0x, ey = -gy + e0y, ez = -gz + e0z;
+    E[0] = make_double2(ex, ey);
+    E[1] = make_double2(ez, 0.0);
+    if (m.E_f) reinterpret_cast<float4 *>(m.E_f)[c] = make_float4((float)ex, (float)ey, (float)ez, 0.0f);
 }
 
 // b = M rho on free rows, minus the Dirichlet columns moved to the right-hand
@@ -82,21 +84,69 @@ __device__ double block_reduce(double v, double *sh) {
     return s;
 }
 
-__device__ double grid_total(const double *part, int nb, double *sh) {
-    double v = 0.0;
-    for (int i = threadIdx.x; i < nb; i += blockDim.x) v += __ldcg(part + i);
-    return block_reduce(v, sh);
+// ---- PCG reductions ---------------------------------------------------------
+// GB300 executes a warp-wide FP64 add in ~64 cycles of one SM sub-partition,
+// so the reductions keep FP64 work off most warps: the 512 per-thread partials
+// go to shared memory, warps 0-3 (one per sub-partition) each sum a quarter,
+// and thread 0 alone forms the scalars of the iteration.
+
+// Sum of two per-thread values over the block; valid in thread 0.
+__device__ __forceinline__ void block_sum2(double a, double b, double *sh, double &ra, double &rb) {
+    const int t = threadIdx.x, w = t >> 5, lane = t & 31;
+    sh[t] = a;
+    sh[kPcgThreads + t] = b;
+    __syncthreads();
+    if (w < 4) {
+        const int q = kPcgThreads / 4;
+        double sa = 0.0, sb = 0.0;
+        for (int k = lane; k < q; k += 32) { sa += sh[w * q + k]; sb += sh[kPcgThreads + w * q + k]; }
+        for (int o = 16; o > 0; o >>= 1) {
+            sa += __shfl_down_sync(0xffffffffu, sa, o);
+            sb += __shfl_down_sync(0xffffffffu, sb, o);
+        }
+        if (lane == 0) { sh[2 * kPcgThreads + w] = sa; sh[2 * kPcgThreads + 4 + w] = sb; }
+    }
+    __syncthreads();
+    if (t == 0) {
+        const double *r = sh + 2 * kPcgThreads;
+        ra = (r[0] + r[1]) + (r[2] + r[3]);
+        rb = (r[4] + r[5]) + (r[6] + r[7]);
+    }
+}
+
+// Sum of the per-block partials of two quantities (all blocks read the same
+// partials in the same order, so every block gets the same totals); valid in thread 0.
+__device__ __forceinline__ void grid_sum2(const double *pa, const double *pb, int nb, double *sh, double &ra, double &rb) {
+    const int t = threadIdx.x, w = t >> 5, lane = t & 31;
+    if (w < 4) {
+        double sa = 0.0, sb = 0.0;
+        for (int k = w * 32 + lane; k < nb; k += 128) { sa += __ldcg(pa + k); if (pb) sb += __ldcg(pb + k); }
+        for (int o = 16; o > 0; o >>= 1) {
+            sa += __shfl_down_sync(0xffffffffu, sa, o);
+            sb += __shfl_down_sync(0xffffffffu, sb, o);
+        }
+        if (lane == 0) { sh[2 * kPcgThreads + 8 + w] = sa; sh[2 * kPcgThreads + 12 + w] = sb; }
+    }
+    __syncthreads();
+    if (t == 0) {
+        const double *r = sh + 2 * kPcgThreads + 8;
+        ra = (r[0] + r[1]) + (r[2] + r[3]);
+        rb = (r[4] + r[5]) + (r[6] + r[7]);
+    }
 }
 
 // Preconditioned CG with the Jacobi preconditioner, all iterations in one
-// cooperative launch.  Per iteration:
-//   phase A: p_new = z + beta p_old (on the fly in the gather), Ap = A p_new,
-//            partial p_new.Ap
-//   phase B: x += alpha p_new, r -= alpha Ap, z = D^-1 r, partials r.z, r.r
-// Stops when ||r|| <= max(rtol ||b||, atol) (unpreconditioned residual).
-__global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgArgs a) {
+// cooperative launch.  Per iteration (three grid-wide barriers):
+//   A: Ap = A p (SELL-32 rows, one FMA and one gather per entry), partial p.Ap
+//   B: x += alpha p, r -= alpha Ap, z = D^-1 r, partials r.z and r.r
+//   C: p = z + beta p
+// Stops when ||r||^2 <= max(rtol ||b||, atol)^2 (unpreconditioned residual).
+// The solver is checked against a direct solve to a tolerance, so it uses
+// FMAs (GB300's FP64 rate makes FP64 instruction count the bound here).
+__global__ void __launch_bounds__(kPcgThreads, 2) k_pcg(PcgArgs a) {
     cg::grid_group grid = cg::this_grid();
-    __shared__ double sh[32];
+    __shared__ double sh[2 * kPcgThreads + 16];
+    __shared__ double scal[4];      // alpha or beta, status, ...
     const int nb = gridDim.x;
     const int n = a.n;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -105,102 +155,297 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgArgs a) {
     double *partB = a.partials + nb;
     double *partC = a.partials + 2 * nb;
     double *partD = a.partials + 3 * nb;
+    double *p = a.p0;
+    double ra, rb;
 
     if (a.remove_mean) {
         double s = 0.0;
         for (int i = gtid; i < n; i += gstride) s += a.b[i];
-        s = block_reduce(s, sh);
-        if (threadIdx.x == 0) partD[blockIdx.x] = s;
+        block_sum2(s, 0.0, sh, ra, rb);
+        if (threadIdx.x == 0) partD[blockIdx.x] = ra;
         grid.sync();
-        const double mean = grid_total(partD, nb, sh) / (double)n;
+        grid_sum2(partD, nullptr, nb, sh, ra, rb);
+        if (threadIdx.x == 0) scal[0] = ra / (double)n;
+        __syncthreads();
+        const double mean = scal[0];
         for (int i = gtid; i < n; i += gstride) a.b[i] = a.b[i] - mean;
         grid.sync();
     }
-    // r = b - A x, z = D^-1 r, p_old = 0.
+    // r = b - A x, z = D^-1 r, p = z
     double rz = 0.0, rr = 0.0, bb = 0.0;
     for (int i = gtid; i < n; i += gstride) {
         double s = 0.0;
-        for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) s += a.val[k] * a.x[a.col[k]];
+        const int64_t base = a.slice_ptr[i >> 5] + (i & 31);
+        const int w = a.slice_width[i >> 5];
+        for (int k = 0; k < w; ++k) s = fma(__ldg(a.val + base + 32 * k), a.x[__ldg(a.col + base + 32 * k)], s);
         const double bi = a.b[i];
         const double ri = bi - s;
         const double zi = a.dinv[i] * ri;
-        a.r[i] = ri; a.z[i] = zi; a.p0[i] = 0.0;
-        rz += ri * zi; rr += ri * ri; bb += bi * bi;
+        a.r[i] = ri; a.z[i] = zi; p[i] = zi;
+        rz = fma(ri, zi, rz); rr = fma(ri, ri, rr); bb = fma(bi, bi, bb);
     }
-    rz = block_reduce(rz, sh);
-    rr = block_reduce(rr, sh);
-    bb = block_reduce(bb, sh);
-    if (threadIdx.x == 0) { partA[blockIdx.x] = rz; partB[blockIdx.x] = rr; partC[blockIdx.x] = bb; }
+    block_sum2(rz, rr, sh, ra, rb);
+    if (threadIdx.x == 0) { partA[blockIdx.x] = ra; partB[blockIdx.x] = rb; }
+    block_sum2(bb, 0.0, sh, ra, rb);
+    if (threadIdx.x == 0) partC[blockIdx.x] = ra;
     grid.sync();
-    rz = grid_total(partA, nb, sh);
-    rr = grid_total(partB, nb, sh);
-    bb = grid_total(partC, nb, sh);
-    const double tol = fmax(a.rtol * sqrt(bb), a.atol);
-    int status = 1, it = 0;
-    double beta = 0.0;
-    double *pold = a.p0, *pnew = a.p1;
-    if (sqrt(rr) <= tol) status = 0;
+    // thread 0 keeps the scalars: rz, tol^2, iteration, status
+    double t_rz = 0.0, t_tol2 = 0.0, t_rr = 0.0, t_bb = 0.0;
+    int t_it = 0, t_status = 1;
+    grid_sum2(partA, partB, nb, sh, ra, rb);
+    if (threadIdx.x == 0) { t_rz = ra; t_rr = rb; }
+    grid_sum2(partC, nullptr, nb, sh, ra, rb);
+    if (threadIdx.x == 0) {
+        t_bb = ra;
+        const double tol = fmax(a.rtol * sqrt(t_bb), a.atol);
+        t_tol2 = tol * tol;
+        if (t_rr <= t_tol2) t_status = 0;
+        if (a.max_iter <= 0 && t_status == 1) t_status = 1;
+        scal[1] = (t_status == 1 && a.max_iter > 0) ? 1.0 : 0.0;
+    }
+    __syncthreads();
     grid.sync();
-    while (status == 1 && it < a.max_iter) {
-        ++it;
-        // phase A
+    while (scal[1] != 0.0) {
+        // A
         double pap = 0.0;
         for (int i = gtid; i < n; i += gstride) {
             double s = 0.0;
-            for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) {
-                const int j = a.col[k];
-                const double pj = __ldcg(a.z + j) + beta * __ldcg(pold + j);
-                s += a.val[k] * pj;
-            }
-            const double pi = __ldcg(a.z + i) + beta * __ldcg(pold + i);
-            pnew[i] = pi;
+            const int64_t base = a.slice_ptr[i >> 5] + (i & 31);
+            const int w = a.slice_width[i >> 5];
+#pragma unroll 4
+            for (int k = 0; k < w; ++k)
+                s = fma(__ldg(a.val + base + 32 * k), __ldcg(p + __ldg(a.col + base + 32 * k)), s);
             a.Ap[i] = s;
-            pap += pi * s;
+            pap = fma(__ldcg(p + i), s, pap);
         }
-        pap = block_reduce(pap, sh);
-        if (threadIdx.x == 0) partA[blockIdx.x] = pap;
+        block_sum2(pap, 0.0, sh, ra, rb);
+        if (threadIdx.x == 0) partA[blockIdx.x] = ra;
         grid.sync();
-        pap = grid_total(partA, nb, sh);
-        if (!(pap > 0.0)) { status = 2; break; }
-        const double alpha = rz / pap;
-        // phase B
+        grid_sum2(partA, nullptr, nb, sh, ra, rb);
+        if (threadIdx.x == 0) {
+            ++t_it;
+            if (!(ra > 0.0)) { t_status = 2; scal[1] = 0.0; scal[0] = 0.0; }
+            else scal[0] = t_rz / ra;
+        }
+        __syncthreads();
+        if (scal[1] == 0.0) break;
+        const double alpha = scal[0];
+        // B
         double rzn = 0.0, rrn = 0.0;
         for (int i = gtid; i < n; i += gstride) {
-            const double pi = pnew[i];
-            const double api = a.Ap[i];
-            a.x[i] = a.x[i] + alpha * pi;
-            const double ri = a.r[i] - alpha * api;
+            const double pi = __ldcg(p + i);
+            a.x[i] = fma(alpha, pi, a.x[i]);
+            const double ri = fma(-alpha, a.Ap[i], a.r[i]);
             const double zi = a.dinv[i] * ri;
             a.r[i] = ri; a.z[i] = zi;
-            rzn += ri * zi; rrn += ri * ri;
+            rzn = fma(ri, zi, rzn); rrn = fma(ri, ri, rrn);
         }
-        rzn = block_reduce(rzn, sh);
-        rrn = block_reduce(rrn, sh);
-        if (threadIdx.x == 0) { partB[blockIdx.x] = rzn; partC[blockIdx.x] = rrn; }
+        block_sum2(rzn, rrn, sh, ra, rb);
+        if (threadIdx.x == 0) { partB[blockIdx.x] = ra; partC[blockIdx.x] = rb; }
         grid.sync();
-        rzn = grid_total(partB, nb, sh);
-        rr = grid_total(partC, nb, sh);
-        if (sqrt(rr) <= tol) { status = 0; break; }
-        beta = rzn / rz;
-        rz = rzn;
-        double *t = pold; pold = pnew; pnew = t;
+        grid_sum2(partB, partC, nb, sh, ra, rb);
+        if (threadIdx.x == 0) {
+            t_rr = rb;
+            if (t_rr <= t_tol2) { t_status = 0; scal[1] = 0.0; }
+            else if (t_it >= a.max_iter) { t_status = 1; scal[1] = 0.0; }
+            scal[0] = ra / t_rz;
+            t_rz = ra;
+        }
+        __syncthreads();
+        if (scal[1] == 0.0) break;
+        const double beta = scal[0];
+        // C
+        for (int i = gtid; i < n; i += gstride) p[i] = fma(beta, __ldcg(p + i), a.z[i]);
         grid.sync();
     }
     if (a.remove_mean) {
         grid.sync();
         double s = 0.0;
         for (int i = gtid; i < n; i += gstride) s += a.x[i];
-        s = block_reduce(s, sh);
-        if (threadIdx.x == 0) partD[blockIdx.x] = s;
+        block_sum2(s, 0.0, sh, ra, rb);
+        if (threadIdx.x == 0) partD[blockIdx.x] = ra;
         grid.sync();
-        const double mean = grid_total(partD, nb, sh) / (double)n;
+        grid_sum2(partD, nullptr, nb, sh, ra, rb);
+        if (threadIdx.x == 0) scal[2] = ra / (double)n;
+        __syncthreads();
+        const double mean = scal[2];
         for (int i = gtid; i < n; i += gstride) a.x[i] = a.x[i] - mean;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        *a.out_iter = it;
-        *a.out_status = status;
-        *a.out_rr = rr;
-        *a.out_bb = bb;
+        *a.out_iter = t_it;
+        *a.out_status = t_status;
+        *a.out_rr = t_rr;
+        *a.out_bb = t_bb;
+    }
+}
+
+// Mixed-precision PCG with reliable updates: the Krylov recurrence (SpMV,
+// residual, preconditioned residual, search direction) in FP32, the solution
+// accumulated in FP64, every inner product reduced in FP64, and the residual
+// replaced by the FP64 true residual b - A x whenever the recursive one has
+// dropped tenfold since the last replacement.  It stops only when the FP64
+// true residual meets ||r|| <= max(rtol ||b||, atol).
+__global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_rel(PcgArgs a) {
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double sh[2 * kPcgThreads + 16];
+    __shared__ double scal[4];
+    const int nb = gridDim.x;
+    const int n = a.n;
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gstride = nb * blockDim.x;
+    double *partA = a.partials;
+    double *partB = a.partials + nb;
+    double *partC = a.partials + 2 * nb;
+    double *partD = a.partials + 3 * nb;
+    double ra, rb;
+
+    if (a.remove_mean) {
+        double s = 0.0;
+        for (int i = gtid; i < n; i += gstride) s += a.b[i];
+        block_sum2(s, 0.0, sh, ra, rb);
+        if (threadIdx.x == 0) partD[blockIdx.x] = ra;
+        grid.sync();
+        grid_sum2(partD, nullptr, nb, sh, ra, rb);
+        if (threadIdx.x == 0) scal[0] = ra / (double)n;
+        __syncthreads();
+        const double mean = scal[0];
+        for (int i = gtid; i < n; i += gstride) a.b[i] = a.b[i] - mean;
+        grid.sync();
+    }
+    double t_rz = 0.0, t_tol2 = 0.0, t_rr = 0.0, t_bb = 0.0, t_rmax = 0.0;
+    int t_it = 0, t_status = 1, t_updates = 0;
+    // true residual in FP64, copied to the FP32 recurrence; p = z on the first pass
+    for (int pass = 0;; ++pass) {
+        double rz = 0.0, rr = 0.0, bb = 0.0;
+        for (int i = gtid; i < n; i += gstride) {
+            double s = 0.0;
+            const int64_t base = a.slice_ptr[i >> 5] + (i & 31);
+            const int w = a.slice_width[i >> 5];
+            for (int k = 0; k < w; ++k) s = fma(__ldg(a.val + base + 32 * k), a.x[__ldg(a.col + base + 32 * k)], s);
+            const double bi = a.b[i];
+            const double ri = bi - s;
+            const float r32 = (float)ri;
+            const float z32 = a.dinv32[i] * r32;
+            a.r32[i] = r32; a.z32[i] = z32;
+            if (pass == 0) a.p32[i] = z32;
+            rz = fma((double)r32, (double)z32, rz); rr = fma(ri, ri, rr);
+            if (pass == 0) bb = fma(bi, bi, bb);
+        }
+        block_sum2(rz, rr, sh, ra, rb);
+        if (threadIdx.x == 0) { partA[blockIdx.x] = ra; partB[blockIdx.x] = rb; }
+        if (pass == 0) {
+            block_sum2(bb, 0.0, sh, ra, rb);
+            if (threadIdx.x == 0) partC[blockIdx.x] = ra;
+        }
+        grid.sync();
+        grid_sum2(partA, partB, nb, sh, ra, rb);
+        if (threadIdx.x == 0) {
+            const double rz_new = ra;
+            t_rr = rb;
+            if (pass > 0) ++t_updates;
+            // keep the search direction; its coefficient uses the replaced r.z
+            scal[0] = pass > 0 ? rz_new / t_rz : 0.0;
+            t_rz = rz_new;
+            t_rmax = t_rr;
+        }
+        if (pass == 0) {
+            grid_sum2(partC, nullptr, nb, sh, ra, rb);
+            if (threadIdx.x == 0) {
+                t_bb = ra;
+                const double tol = fmax(a.rtol * sqrt(t_bb), a.atol);
+                t_tol2 = tol * tol;
+            }
+        }
+        if (threadIdx.x == 0) {
+            if (t_rr <= t_tol2) { t_status = 0; scal[1] = 0.0; }
+            else if (t_it >= a.max_iter) { t_status = 1; scal[1] = 0.0; }
+            else scal[1] = 1.0;
+        }
+        __syncthreads();
+        if (scal[1] == 0.0) break;
+        if (pass > 0) {
+            // p = z + beta p with the replaced residual
+            const float beta = (float)scal[0];
+            for (int i = gtid; i < n; i += gstride) a.p32[i] = fmaf(beta, __ldcg(a.p32 + i), a.z32[i]);
+        }
+        grid.sync();
+        // FP32 recurrence until the residual has dropped tenfold (or converged)
+        bool replace = false;
+        while (!replace) {
+            float pap32 = 0.0f;
+            for (int i = gtid; i < n; i += gstride) {
+                float s = 0.0f;
+                const int64_t base = a.slice_ptr[i >> 5] + (i & 31);
+                const int w = a.slice_width[i >> 5];
+#pragma unroll 4
+                for (int k = 0; k < w; ++k)
+                    s = fmaf(__ldg(a.val32 + base + 32 * k), __ldcg(a.p32 + __ldg(a.col + base + 32 * k)), s);
+                a.Ap32[i] = s;
+                pap32 = fmaf(__ldcg(a.p32 + i), s, pap32);
+            }
+            block_sum2((double)pap32, 0.0, sh, ra, rb);
+            if (threadIdx.x == 0) partA[blockIdx.x] = ra;
+            grid.sync();
+            grid_sum2(partA, nullptr, nb, sh, ra, rb);
+            if (threadIdx.x == 0) {
+                ++t_it;
+                if (!(ra > 0.0)) { t_status = 2; scal[1] = 0.0; scal[0] = 0.0; }
+                else { scal[0] = t_rz / ra; scal[1] = 1.0; }
+            }
+            __syncthreads();
+            if (scal[1] == 0.0) break;
+            const double alpha = scal[0];
+            const float alpha32 = (float)alpha;
+            float rz32 = 0.0f, rr32 = 0.0f;
+            for (int i = gtid; i < n; i += gstride) {
+                const float pi = __ldcg(a.p32 + i);
+                a.x[i] = fma(alpha, (double)pi, a.x[i]);
+                const float ri = fmaf(-alpha32, a.Ap32[i], a.r32[i]);
+                const float zi = a.dinv32[i] * ri;
+                a.r32[i] = ri; a.z32[i] = zi;
+                rz32 = fmaf(ri, zi, rz32); rr32 = fmaf(ri, ri, rr32);
+            }
+            block_sum2((double)rz32, (double)rr32, sh, ra, rb);
+            if (threadIdx.x == 0) { partB[blockIdx.x] = ra; partC[blockIdx.x] = rb; }
+            grid.sync();
+            grid_sum2(partB, partC, nb, sh, ra, rb);
+            if (threadIdx.x == 0) {
+                const double rr_rec = rb;
+                // replace the residual after a tenfold drop, at the tolerance, or at the cap;
+                // on a replacement r.z of the previous step stays for the next beta
+                const bool rep = rr_rec <= 0.01 * t_rmax || rr_rec <= t_tol2 || t_it >= a.max_iter;
+                scal[2] = rep ? 1.0 : 0.0;
+                if (!rep) { scal[0] = ra / t_rz; t_rz = ra; }
+            }
+            __syncthreads();
+            replace = scal[2] != 0.0;
+            if (replace) break;
+            const float beta = (float)scal[0];
+            for (int i = gtid; i < n; i += gstride) a.p32[i] = fmaf(beta, __ldcg(a.p32 + i), a.z32[i]);
+            grid.sync();
+        }
+        if (scal[1] == 0.0) break;      // breakdown
+        grid.sync();
+    }
+    if (a.remove_mean) {
+        grid.sync();
+        double s = 0.0;
+        for (int i = gtid; i < n; i += gstride) s += a.x[i];
+        block_sum2(s, 0.0, sh, ra, rb);
+        if (threadIdx.x == 0) partD[blockIdx.x] = ra;
+        grid.sync();
+        grid_sum2(partD, nullptr, nb, sh, ra, rb);
+        if (threadIdx.x == 0) scal[2] = ra / (double)n;
+        __syncthreads();
+        const double mean = scal[2];
+        for (int i = gtid; i < n; i += gstride) a.x[i] = a.x[i] - mean;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *a.out_iter = t_it;
+        *a.out_status = t_status;
+        *a.out_rr = t_rr;
+        *a.out_bb = t_bb;
+        if (a.out_updates) *a.out_updates = t_updates;
     }
 }
 
@@ -232,7 +477,24 @@ __global__ void k_image_charge(DevMesh m, const double *__restrict__ phi, const 
     }
 }
 
+// phi = phi0 + sum_k V_k L_k: the solution with object potentials V from the
+// one with zero potentials and the unit-potential Laplace solutions L_k.
+__global__ void k_superpose(const double *__restrict__ phi0, const double *__restrict__ lap, Pots pots,
+                            int32_t n, double *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = phi0[i];
+    for (int k = 0; k < pots.n; ++k) v = v + pots.v[k] * lap[(size_t)k * n + i];
+    out[i] = v;
+}
+
 }  // namespace
+
+void launch_superpose(const double *phi0, const double *lap, const Pots &pots, int32_t n, double *out,
+                      cudaStream_t st) {
+    count_launches(1);
+    k_superpose<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(phi0, lap, pots, n, out);
+}
 
 void launch_efield(const DevMesh &m, const double *phi, const double E0[3], cudaStream_t st) {
     if (m.nc <= 0) return;
@@ -257,10 +519,12 @@ void launch_set_bc(const int32_t *bc_kind, const double *bc_value, const double 
 int pcg_grid_blocks() {
     static int g = 0;
     if (g == 0) {
-        int per_sm = 0;
+        int per_sm = 0, per_sm_rel = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg, kPcgThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_rel, k_pcg_rel, kPcgThreads, 0);
+        if (per_sm_rel < per_sm) per_sm = per_sm_rel;
         if (per_sm < 1) per_sm = 1;
-        if (per_sm > 2) per_sm = 2;
+        if (per_sm > 4) per_sm = 4;
         g = per_sm * sm_count();
     }
     return g;
@@ -273,7 +537,8 @@ int launch_pcg(const PcgArgs &a, cudaStream_t st) {
     PcgArgs arg = a;
     void *params[] = {&arg};
     count_launches(1);
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_pcg, dim3(nb), dim3(kPcgThreads), params, 0, st);
+    const void *fn = a.val32 ? (const void *)k_pcg_rel : (const void *)k_pcg;
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(nb), dim3(kPcgThreads), params, 0, st);
     return e == cudaSuccess ? 0 : (int)e;
 }
 

@@ -60,6 +60,7 @@ struct DevState {
     int64_t absorbed[kMaxTags][kMaxSpecies];      // absorbed this call, per tag and species
     int64_t injected[kMaxSpecies];
     int64_t inject_total;                         // slots appended by the last injection
+    int64_t retests;                              // mixed form: facets re-tested in FP64
     double ke;                                    // last kinetic-energy reduction
     double image_charge[kMaxTags];
 };
@@ -97,12 +98,33 @@ struct InjectParams {
     int64_t slot_base;            // first free slot
     int64_t pid_base;
     InjectSpecies sp[kMaxSpecies];
+    // mixed form: fixed-point deposit target and q * 2^40 / q_max per species
+    unsigned long long *rho_fixed;
+    float q_scaled[kMaxSpecies];
+};
+
+// Mixed-form per-species constants of one particle pass.
+struct MixedParams {
+    float coef[kMaxSpecies];      // (0.5*dt)*(q/m) or dt*(q/m)
+    float half_m[kMaxSpecies];
+    float t[kMaxSpecies][3];
+    float s[kMaxSpecies][3];
+    float q_scaled[kMaxSpecies];  // q * 2^40 / q_max
+    int32_t has_B;
+    int32_t accel;
+    float dt;
+    int32_t periodic;
+    float Ld[3];
 };
 
 // PCG on the Dirichlet-reduced symmetric matrix, one cooperative launch.
+// The matrix is in SELL-32 form: rows in slices of 32, each slice stored
+// column-major (entry k of row 32*s + lane at slice_ptr[s] + 32*k + lane),
+// padded to the slice's longest row with (own column, 0.0).
 struct PcgArgs {
     int32_t n;
-    const int32_t *rowptr;
+    const int64_t *slice_ptr;     // [n_slices + 1]
+    const int32_t *slice_width;   // [n_slices]
     const int32_t *col;
     const double *val;
     const double *dinv;
@@ -121,6 +143,11 @@ struct PcgArgs {
     int32_t *out_status;          // 0 converged, 1 iteration cap, 2 breakdown
     double *out_rr;               // ||r||^2
     double *out_bb;               // ||b||^2
+    // mixed solver: FP32 copies of the matrix and the Krylov vectors
+    const float *val32;
+    const float *dinv32;
+    float *r32, *z32, *p32, *Ap32;
+    int32_t *out_updates;         // reliable updates done
 };
 
 // ---- launch wrappers (all on `stream`) -----------------------------------
@@ -150,7 +177,7 @@ void launch_inject_count(const DevMesh &m, const InjectParams &ip, const double 
 void launch_inject_generate(const DevMesh &m, const DevParticles &p, const InjectParams &ip,
                             const double *flux_num, const double *pdf_max, const double *facets,
                             const int64_t *offsets, int max_steps, int deposit, const double *q_species,
-                            double *rho_acc, DevState *state, cudaStream_t st);
+                            double *rho_acc, DevState *state, int64_t max_particles, cudaStream_t st);
 
 void launch_scan_i64(const int64_t *in, int64_t *out, int64_t n, int64_t *tmp, cudaStream_t st);
 int64_t scan_tmp_size(int64_t n);
@@ -166,6 +193,23 @@ void launch_set_bc(const int32_t *bc_kind, const double *bc_value, const double 
                    int32_t n, double *x, cudaStream_t st);
 int launch_pcg(const PcgArgs &a, cudaStream_t st);
 int pcg_grid_blocks();
+struct Pots {
+    int32_t n;
+    double v[kMaxTags];
+};
+void launch_superpose(const double *phi0, const double *lap, const Pots &pots, int32_t n, double *out,
+                      cudaStream_t st);
+
+// mixed-precision form
+void launch_mixed_pass(const DevMesh &m, const DevParticles &p, int64_t n_slots, const MixedParams &mp, bool push,
+                       bool move, bool walk, bool deposit, int max_steps, unsigned long long *rho_fixed,
+                       DevState *state, double *partials, int nblocks, double *ke_out, cudaStream_t st);
+void launch_kinetic_mixed(const DevParticles &p, int64_t n_slots, const MixedParams &mp, double *partials,
+                          int nblocks, double *ke_out, cudaStream_t st);
+void launch_fixed_to_rho(const unsigned long long *fixed, const double *dv_inv, double unit, int32_t n,
+                         double *rho_acc, double *rho, cudaStream_t st);
+void launch_float_tables(const double *planes, const double *bary, int32_t nc, float *planes_f, float *bary_f,
+                         cudaStream_t st);
 void launch_image_charge(const DevMesh &m, const double *phi, const double *ofacets, int32_t n_ofacets,
                          int32_t n_obj, double eps0, double *out, cudaStream_t st);
 

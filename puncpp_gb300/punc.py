@@ -120,11 +120,13 @@ class Population:
 
     def __init__(self, mesh: Mesh, precision: int = L.PG_FP64, periodic: bool = False, capacity: int = 0,
                  max_walk_steps: int = 0, sort_interval: int = 0, pcg_rtol: float = 0.0, pcg_atol: float = 0.0,
-                 pcg_max_iter: int = 0, warm_start: bool = True, ext_E=(0.0, 0.0, 0.0)):
+                 pcg_max_iter: int = 0, warm_start: bool = True, ext_E=(0.0, 0.0, 0.0),
+                 circuit_resolve: bool = False, pcg_precision: int = 0):
         lib = L.load()
         self.mesh = mesh
         cfg = L.Config(precision, 1 if periodic else 0, mesh.eps0, capacity, max_walk_steps, sort_interval,
-                       pcg_rtol, pcg_atol, pcg_max_iter, 1 if warm_start else 0, (C.c_double * 3)(*ext_E))
+                       pcg_rtol, pcg_atol, pcg_max_iter, 1 if warm_start else 0, (C.c_double * 3)(*ext_E),
+                       1 if circuit_resolve else 0, pcg_precision)
         h = C.c_void_p()
         L.check(lib.pg_create(mesh.handle, C.byref(cfg), C.byref(h)))
         self.handle = h

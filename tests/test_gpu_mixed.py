@@ -1,0 +1,124 @@
+"""The mixed-precision form: FP32 particles, FP32 push and walk with an FP64
+re-test near facets, int64 fixed-point deposit.
+
+Bars: every cell decision equals the oracle's FP64 walk evaluated at the
+FP32 position (bit-exact cell indices and absorbed counts); the deposit is
+bitwise identical from run to run and within 1e-5 (relative to max |rho|) of
+the FP64 deposit of the same FP32 positions; velocities within 1e-6 relative
+of the FP64 push."""
+import numpy as np
+import pytest
+
+from helpers import maxwellian_velocities, uniform_points
+from puncpp_gb300 import _lib as L
+from puncpp_gb300 import meshgen, punc
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def f32(a):
+    return np.asarray(a, np.float64).astype(np.float32).astype(np.float64)
+
+
+def mixed_setup(oracle_mod, n=8, half=2.0, radius=0.6, n_particles=20000, seed=3, periodic=False, **cfg):
+    ma = meshgen.langmuir_cube(n) if periodic else meshgen.probe_box(n, half, radius)
+    mesh = punc.Mesh(ma)
+    pop = punc.Population(mesh, precision=L.PG_MIXED, periodic=periodic, **cfg)
+    o = oracle_mod.Oracle(ma)
+    rng = np.random.default_rng(seed)
+    for q, m, vth in ((-1.0, 1.0, 1.0), (1.0, 100.0, 0.1)):
+        xs = uniform_points(ma, n_particles, rng)
+        vs = maxwellian_velocities(n_particles, vth, rng)
+        k1 = pop.add_particles(xs, vs, q, m)
+        k2 = o.add_particles(f32(xs), f32(vs), q, m)
+        assert k1 == k2
+    return ma, mesh, pop, o, rng
+
+
+def test_mixed_particles_are_the_rounded_inputs(lib, oracle_mod):
+    ma, mesh, pop, o, rng = mixed_setup(oracle_mod)
+    a, b = pop.particles(), o.particles()
+    assert np.array_equal(a["id"], b["id"]) and np.array_equal(a["cell"], b["cell"])
+    assert np.array_equal(a["x"], b["x"]) and np.array_equal(a["v"], b["v"])
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_mixed_walk_equals_fp64_walk_at_fp32_positions(periodic, lib, oracle_mod):
+    ma, mesh, pop, o, rng = mixed_setup(oracle_mod, periodic=periodic)
+    before = pop.particles()
+    dt = 0.9
+    if periodic:
+        punc.move_periodic(pop, dt, ma.Ld)
+    else:
+        punc.move(pop, dt)
+    moved = pop.particles()                       # FP32 positions after the move, old cells
+    assert np.array_equal(moved["cell"], before["cell"])
+    o.set_particles(moved)
+    objs = [] if periodic else [punc.Object(2)]
+    oobjs = [] if periodic else [dict(bnd_id=2, charge=0.0, current=0.0, potential=0.0)]
+    pop.update(objs, dt)
+    absorbed = o.update(oobjs, dt)
+    a, b = pop.particles(), o.particles()
+    assert np.array_equal(a["id"], b["id"]), "absorbed sets differ"
+    assert np.array_equal(a["cell"], b["cell"]), "cell indices differ"
+    if not periodic:
+        assert absorbed[1] > 0 and absorbed[2] > 0
+        assert abs(objs[0].current - oobjs[0]["current"]) <= 1e-12 * abs(oobjs[0]["current"])
+
+
+def test_mixed_deposit_is_deterministic_and_close_to_fp64(lib, oracle_mod):
+    ma, mesh, pop, o, rng = mixed_setup(oracle_mod)
+    r1 = punc.distribute_cg1(pop)
+    r2 = punc.distribute_cg1(pop)
+    assert np.array_equal(r1.view(np.uint64), r2.view(np.uint64))
+    pop.sort()
+    r3 = punc.distribute_cg1(pop)                 # another particle order
+    assert np.array_equal(r1.view(np.uint64), r3.view(np.uint64))
+    assert rel(r1, o.distribute_cg1()) < 1e-5
+
+
+def test_mixed_push_close_to_fp64(lib, oracle_mod):
+    ma, mesh, pop, o, rng = mixed_setup(oracle_mod)
+    phi = rng.normal(size=mesh.n_dofs)
+    punc.Function(pop, "phi").set_local(phi)
+    E = o.efield(phi)
+    dt = 0.07
+    ke_g = punc.boris(pop, punc.Function(pop, "E"), (0, 0, 0), dt)
+    ke_o = o.boris(E, (0, 0, 0), dt)
+    assert abs(ke_g - ke_o) < 1e-6 * abs(ke_o)
+    a, b = pop.particles(), o.particles()
+    assert np.array_equal(a["id"], b["id"])
+    assert rel(a["v"], b["v"]) < 1e-6
+
+
+def test_mixed_fused_steps_track_the_fp64_form(lib, oracle_mod):
+    """Same seeded start in both forms; after each fused step the charge
+    density of the mixed form stays within 1e-5 of the FP64 form's."""
+    ma = meshgen.probe_box(10, 3.0, 0.8)
+    mesh = punc.Mesh(ma)
+    rng = np.random.default_rng(5)
+    xs_e = uniform_points(ma, 30000, rng); vs_e = maxwellian_velocities(30000, 1.0, rng)
+    xs_i = uniform_points(ma, 30000, rng); vs_i = maxwellian_velocities(30000, 0.1, rng)
+    pops = {}
+    for prec in (L.PG_FP64, L.PG_MIXED):
+        pop = punc.Population(mesh, precision=prec, pcg_rtol=1e-12)
+        pop.add_particles(f32(xs_e), f32(vs_e), -1.0, 1.0)
+        pop.add_particles(f32(xs_i), f32(vs_i), 1.0, 100.0)
+        punc.create_flux(pop, [punc.Species(-1.0, 1.0, n=20.0, vth=1.0), punc.Species(1.0, 100.0, n=20.0, vth=0.1)])
+        pops[prec] = pop
+    objs = {p: [punc.Object(2, potential=-1.0)] for p in pops}
+    for n in range(3):
+        res = {p: punc.step(pops[p], objs[p], 0.1, first_step=(n == 0), inject=True, seed=9, step_no=n) for p in pops}
+        rho64 = punc.Function(pops[L.PG_FP64], "rho").vector()
+        rho32 = punc.Function(pops[L.PG_MIXED], "rho").vector()
+        assert rel(rho32, rho64) < 1e-5, n
+        assert abs(res[L.PG_MIXED].n_particles - res[L.PG_FP64].n_particles) <= 2
+        assert abs(res[L.PG_MIXED].KE - res[L.PG_FP64].KE) < 1e-5 * abs(res[L.PG_FP64].KE)
+    phi64 = punc.Function(pops[L.PG_FP64], "phi").vector()
+    phi32 = punc.Function(pops[L.PG_MIXED], "phi").vector()
+    assert rel(phi32, phi64) < 1e-5
