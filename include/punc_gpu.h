@@ -259,6 +259,22 @@ int pg_synchronize(pg_sim *sim);
 /* Number of kernels this library has launched in this process. */
 int pg_launch_count(int64_t *n);
 
+/* Jacobi-preconditioned CG on a caller's CSR matrix (SPD, int32 indices, all
+ * arrays in device memory), for callers that cannot allocate device memory:
+ * the work vectors live in a static device array of the library instead of
+ * buffers from cudaMalloc, and the call allocates nothing.  No counterpart in
+ * the reference (it solves through PETSc).  x holds the initial guess and
+ * receives the solution; stops when ||b - A x|| <= max(rtol ||b||, atol).
+ * At most 524,288 rows (larger n: PG_ERR_ARG); the array (about 20 MB) stays
+ * on every GPU that loads the library.  All calls share it, so calls that
+ * overlap on the GPU race.  The first call on a device sets the device up
+ * (looks up the array's address): make it before any stream capture.
+ * stream: a cudaStream_t, or NULL for the default stream; the call waits for
+ * the solve to finish. */
+int pg_pcg_solve_noalloc(int32_t n, const int32_t *rowptr, const int32_t *col, const double *val,
+                         const double *b, double *x, double rtol, double atol, int32_t max_iter,
+                         void *stream, int32_t *iterations, double *residual);
+
 #ifdef __cplusplus
 }
 #endif

@@ -128,6 +128,8 @@ SIGNATURES = {
     "pg_event_elapsed": ([_P, C.c_int32, C.c_int32, _D], C.c_int),
     "pg_synchronize": ([_P], C.c_int),
     "pg_launch_count": ([_I64], C.c_int),
+    "pg_pcg_solve_noalloc": ([C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                              C.c_double, C.c_int32, C.c_void_p, _I32, _D], C.c_int),
 }
 
 _lib = None

@@ -32,6 +32,7 @@ CU_UNITS = {
     "k_solver.cu": [],
     "k_inject.cu": [],
     "k_mixed.cu": ["--fmad=true"],
+    "k_noalloc.cu": [],
 }
 CPP_UNITS = ["mesh_tables.cpp"]
 
