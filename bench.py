@@ -200,17 +200,28 @@ def run_ours(args):
     occ = nc * (1.0 - math.exp(-n_avg / nc))
     part_ms = stages.get("push_move_update_deposit", 0.0)
     pcg_ms = stages.get("pcg", 0.0)
-    if pcg_ms >= part_ms:
-        bytes_ = iters * (nnz * 12 + 7 * nv * 8)
-        kname, t_k = "k_pcg (Jacobi PCG, all iterations of a solve in one cooperative launch)", pcg_ms
+    mixed = args.precision == "mixed"
+    # algorithmic bytes: particle pass per particle / occupied cell / dof,
+    # PCG per iteration per nonzero / dof
+    if mixed:
+        pb, cb, pmodel = n_avg * 57 + occ * 160 + nv * 8, None, "Np*57 + occupied cells*160 + Ndof*8"
+        kb, kmodel = nnz * 8 + nv * 52, "per iteration nnz*8 + Ndof*52"
     else:
-        bytes_ = args.steps * (n_avg * 104 + occ * (256 + 32) + nv * 8)
-        kname, t_k = "k_particles (fused push+move+walk+deposit)", part_ms
-    achieved = bytes_ / (t_k / 1e3) / 1e9 if t_k > 0 else 0.0
-    roof = {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": hbm,
-            "unit": "GB/s", "frac": round(achieved / hbm, 4), "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)"
-            if src == "measured" else "fallback 6.8 TB/s", "traffic": None,
-            "algorithmic_bytes": "PCG: per iteration nnz*12 + 7*Ndof*8; particles: Np*104 + occupied cells*288 + Ndof*8"}
+        pb, cb, pmodel = n_avg * 104 + occ * 288 + nv * 8, None, "Np*104 + occupied cells*288 + Ndof*8"
+        kb, kmodel = nnz * 12 + 7 * nv * 8, "per iteration nnz*12 + 7*Ndof*8"
+    peak_src = (src + " (MEASURED_PEAKS.json hbm_gbs)") if src == "measured" else "fallback 6.8 TB/s"
+
+    def roof_of(name, bytes_total, t_ms, model):
+        ach = bytes_total / (t_ms / 1e3) / 1e9 if t_ms > 0 else 0.0
+        return {"bound": "hbm", "kernel": name, "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(ach / hbm, 4), "peak_source": peak_src, "traffic": None,
+                "algorithmic_bytes": model}
+
+    r_part = roof_of("k_mixed (fused FP32 push+move+walk, fixed-point deposit)" if mixed
+                     else "k_particles (fused FP64 push+move+walk+deposit)", args.steps * pb, part_ms, pmodel)
+    r_pcg = roof_of("k_pcg_rel (mixed PCG, one cooperative launch per solve)" if mixed
+                    else "k_pcg (FP64 Jacobi PCG, one cooperative launch per solve)", iters * kb, pcg_ms, kmodel)
+    roof = r_pcg if pcg_ms >= part_ms else r_part
     stages_share = {k: round(v / ms, 4) for k, v in stages.items()}
 
     out = {
@@ -223,7 +234,7 @@ def run_ours(args):
                    "particles_mean_pushed": round(n_avg), "pcg_iterations_per_step": round(iters / args.steps, 1),
                    "l2": "inputs larger than L2 (particle SoA ~250 MB, mesh tables ~0.9 GB)"},
         "stage_ms": {k: round(v, 3) for k, v in stages.items()}, "stage_share": stages_share,
-        "roofline": roof,
+        "roofline": roof, "roofline_particles": r_part, "roofline_pcg": r_pcg,
         "e2e": {"value": round(e2e_pushed / e2e_s, 1), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "path": "pg_step + pg_get_phi per step through the C ABI, host wall clock"},

@@ -1,0 +1,242 @@
+// punc_gpu.hpp - C++ front end over the C ABI of punc_gpu.h with the names and
+// argument order of the PUNC++ particle path, so a time loop written against
+// the reference (interaction/interaction.cpp:342-480) keeps its shape:
+//
+//     punc::gpu::distribute_cg1(pop, rho, dv_inv);
+//     poisson.solve_circuit(phi, rho, mesh, objects, circuit);
+//     esolver.solve(E, phi);
+//     KE = punc::gpu::boris(pop, E, B, dt);
+//     punc::gpu::move(pop, dt);
+//     pop.update(objects, dt);
+//     punc::gpu::inject_particles(pop, species, dt, seed, n);
+//
+// DOLFIN types are replaced by plain arrays: a Mesh is built from vertex
+// coordinates, cell vertex ids and tagged boundary facets; Functions are views
+// of the fields the engine keeps on the device.  Errors throw punc::gpu::Error
+// carrying the pg_status code.
+#ifndef PUNC_GPU_HPP
+#define PUNC_GPU_HPP
+
+#include <cstddef>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "punc_gpu.h"
+
+namespace punc {
+namespace gpu {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const char *msg) : std::runtime_error(std::string("punc_gpu: ") + (msg ? msg : "")), code(c) {}
+};
+
+inline void check(int rc) {
+    if (rc != PG_OK) throw Error(rc, pg_last_error());
+}
+
+// Mesh (punc/include/punc/mesh.h:49-97) as arrays: tag 1 = exterior, 2.. = objects.
+class Mesh {
+public:
+    Mesh(const std::vector<double> &coords, const std::vector<int64_t> &cells,
+         const std::vector<int64_t> &bfacet_vertices, const std::vector<int32_t> &bfacet_tags,
+         double eps0 = 1.0, const std::vector<int64_t> *vertex_to_dof = nullptr, int64_t n_dofs = 0)
+        : eps0(eps0) {
+        pg_mesh_desc d{};
+        d.n_vertices = (int64_t)(coords.size() / 3);
+        d.coords = coords.data();
+        d.n_cells = (int64_t)(cells.size() / 4);
+        d.cells = cells.data();
+        d.n_boundary_facets = (int64_t)(bfacet_tags.size());
+        d.bfacet_vertices = bfacet_vertices.data();
+        d.bfacet_tags = bfacet_tags.data();
+        d.n_dofs = vertex_to_dof ? n_dofs : d.n_vertices;
+        d.vertex_to_dof = vertex_to_dof ? vertex_to_dof->data() : nullptr;
+        check(pg_mesh_build(&d, eps0, &handle));
+    }
+    ~Mesh() { pg_mesh_free(handle); }
+    Mesh(const Mesh &) = delete;
+    Mesh &operator=(const Mesh &) = delete;
+    pg_mesh *handle = nullptr;
+    double eps0;
+};
+
+// Object (punc/include/punc/object.h:80-130).
+struct Object {
+    explicit Object(std::size_t bnd_id) : bnd_id(bnd_id) {}
+    void set_potential(double p) { potential = p; }
+    double get_potential() const { return potential; }
+    double charge = 0, current = 0;
+    std::size_t bnd_id;
+    double potential = 0;
+};
+using ObjectVector = std::vector<std::shared_ptr<Object>>;
+
+struct VSource { int node_a, node_b; double value; };
+struct ISource { int node_a, node_b; double value; };
+using VSourceVector = std::vector<VSource>;
+using ISourceVector = std::vector<ISource>;
+
+// Maxwellian species of simulation particles (punc/src/population.cpp:41-70).
+struct Species {
+    double q, m, n, vth;
+    double vd[3] = {0, 0, 0};
+    double vdf_range = 5.0;
+};
+
+namespace detail {
+inline std::vector<pg_object> to_c(const ObjectVector &objs) {
+    std::vector<pg_object> v;
+    for (auto &o : objs) v.push_back(pg_object{(int64_t)o->bnd_id, o->charge, o->current, o->potential});
+    return v;
+}
+inline void from_c(const std::vector<pg_object> &v, ObjectVector &objs) {
+    for (std::size_t k = 0; k < objs.size(); ++k) {
+        objs[k]->charge = v[k].charge;
+        objs[k]->current = v[k].current;
+        objs[k]->potential = v[k].potential;
+    }
+}
+}  // namespace detail
+
+template <std::size_t len> class Population;
+
+// Population<3> (punc/include/punc/population.h:236-308) on the device.
+template <> class Population<3> {
+public:
+    explicit Population(const Mesh &mesh, pg_config cfg = pg_config{}) {
+        if (cfg.eps0 == 0) cfg.eps0 = mesh.eps0;
+        check(pg_create(mesh.handle, &cfg, &handle));
+    }
+    ~Population() { pg_destroy(handle); }
+    Population(const Population &) = delete;
+    Population &operator=(const Population &) = delete;
+
+    void add_particles(const std::vector<double> &xs, const std::vector<double> &vs, double q, double m) {
+        int64_t added = 0;
+        check(pg_add_particles(handle, xs.data(), vs.data(), (int64_t)(xs.size() / 3), q, m, &added));
+    }
+    signed long int locate(const double *p) {
+        int64_t c = -1;
+        check(pg_locate(handle, p, 1, &c));
+        return (signed long int)c;
+    }
+    void update(ObjectVector objects, double dt) {
+        auto v = detail::to_c(objects);
+        check(pg_update(handle, v.data(), (int32_t)v.size(), dt));
+        detail::from_c(v, objects);
+    }
+    std::size_t num_of_particles() { return counts(0); }
+    std::size_t num_of_negatives() { return counts(1); }
+    std::size_t num_of_positives() { return counts(2); }
+
+    pg_sim *handle = nullptr;
+    static constexpr std::size_t g_dim = 3;
+
+private:
+    std::size_t counts(int which) {
+        int64_t c[3] = {0, 0, 0};
+        check(pg_num_particles(handle, &c[0], &c[1], &c[2]));
+        return (std::size_t)c[which];
+    }
+};
+
+// A field of the engine: E (DG0 vector), rho or phi (CG1).
+class Function {
+public:
+    enum Kind { E, Rho, Phi };
+    Function(Population<3> &pop, Kind k) : pop_(pop), kind_(k) {}
+    std::vector<double> vector(std::size_t n) const {
+        std::vector<double> out(n);
+        if (kind_ == E) check(pg_get_efield(pop_.handle, out.data()));
+        else if (kind_ == Rho) check(pg_get_rho(pop_.handle, out.data()));
+        else check(pg_get_phi(pop_.handle, out.data()));
+        return out;
+    }
+    Population<3> &pop() const { return pop_; }
+
+private:
+    Population<3> &pop_;
+    Kind kind_;
+};
+
+// pusher.h:66-130, 397-510, 648-681
+inline double accel(Population<3> &pop, const Function &, double dt) {
+    double ke = 0;
+    check(pg_accel(pop.handle, dt, &ke));
+    return ke;
+}
+inline double boris(Population<3> &pop, const Function &, const std::vector<double> &B, double dt) {
+    double ke = 0;
+    check(pg_boris(pop.handle, B.data(), dt, &ke));
+    return ke;
+}
+inline void move(Population<3> &pop, double dt) { check(pg_move(pop.handle, dt)); }
+inline void move_periodic(Population<3> &pop, double dt, const std::vector<double> &Ld) {
+    check(pg_move_periodic(pop.handle, dt, Ld.data()));
+}
+// distributor.h:168-210; dv_inv is the engine's own element_volume table.
+inline void distribute_cg1(Population<3> &pop, Function &, const std::vector<double> &) {
+    check(pg_distribute_cg1(pop.handle, nullptr));
+}
+inline double kinetic_energy(Population<3> &pop) {
+    double ke = 0;
+    check(pg_kinetic_energy(pop.handle, &ke));
+    return ke;
+}
+
+// EFieldDG0 (punc/src/efield.cpp:77-99)
+struct EFieldDG0 {
+    void solve(Function &E, const Function &) { check(pg_efield_dg0(E.pop().handle, nullptr)); }
+};
+
+// CircuitCM (punc/src/object_CM.cpp:135-197)
+class CircuitCM {
+public:
+    CircuitCM(Population<3> &pop, ObjectVector &, const VSourceVector &vs, const ISourceVector &is, double dt) {
+        std::vector<pg_source> v, i;
+        for (auto &s : vs) v.push_back(pg_source{s.node_a, s.node_b, s.value});
+        for (auto &s : is) i.push_back(pg_source{s.node_a, s.node_b, s.value});
+        check(pg_circuit_cm_setup(pop.handle, v.data(), (int32_t)v.size(), i.data(), (int32_t)i.size(), dt));
+    }
+    bool correction_required = true;
+};
+
+// PoissonSolver (punc/src/poisson.cpp:260-385)
+class PoissonSolver {
+public:
+    explicit PoissonSolver(Population<3> &pop) : pop_(pop) {}
+    void solve(Function &, const Function &, ObjectVector &objects) {
+        auto v = detail::to_c(objects);
+        check(pg_poisson_solve(pop_.handle, v.data(), (int32_t)v.size(), nullptr, &info));
+    }
+    void solve_circuit(Function &, const Function &, const Mesh &, ObjectVector &objects, CircuitCM &) {
+        auto v = detail::to_c(objects);
+        check(pg_solve_circuit(pop_.handle, v.data(), (int32_t)v.size(), nullptr, &info));
+        detail::from_c(v, objects);
+    }
+    pg_solve_info info{};
+
+private:
+    Population<3> &pop_;
+};
+
+// create_flux / inject_particles (punc/src/injector.cpp:104-171, injector.h:157-232)
+inline void create_flux(Population<3> &pop, const std::vector<Species> &species) {
+    std::vector<pg_species> s;
+    for (auto &x : species) s.push_back(pg_species{x.q, x.m, x.n, x.vth, {x.vd[0], x.vd[1], x.vd[2]}, x.vdf_range});
+    check(pg_create_flux(pop.handle, s.data(), (int32_t)s.size()));
+}
+inline std::size_t inject_particles(Population<3> &pop, const std::vector<Species> &, double dt, uint64_t seed,
+                                    uint64_t step) {
+    int64_t n = 0;
+    check(pg_inject(pop.handle, dt, seed, step, &n));
+    return (std::size_t)n;
+}
+
+}  // namespace gpu
+}  // namespace punc
+
+#endif  // PUNC_GPU_HPP

@@ -928,6 +928,8 @@ int pg_add_particles(pg_sim *s, const double *xs, const double *vs, int64_t n, d
     PG_CUDA(cudaMemcpy(s->state, s->state_h, sizeof(DevState), cudaMemcpyHostToDevice));
     s->rho_valid = false;
     if (n_added) *n_added = k;
+    // loaded points come in any order: sort by cell so cell tables are read once per warp
+    if (k > 0) return do_sort(s);
     return PG_OK;
 }
 

@@ -55,6 +55,25 @@ def test_oracle_exp_series_accuracy(oracle_mod):
     assert rel[ref > 1e-300].max() < 4e-16
 
 
+def build_cpp_time_loop(tmp_path):
+    """Compile tests/cpp/time_loop.cpp (a PUNC++-shaped loop on include/punc_gpu.hpp)."""
+    import shutil
+    import subprocess
+    if not shutil.which("g++"):
+        pytest.skip("g++ not available")
+    exe = tmp_path / "time_loop"
+    libdir = os.path.join(ROOT, "puncpp_gb300")
+    r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", "time_loop.cpp"), "-L" + libdir, "-lpunc_gpu",
+                        "-Wl,-rpath," + libdir, "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_cpp_front_end_compiles_and_links(lib, tmp_path):
+    assert build_cpp_time_loop(tmp_path).exists()
+
+
 def test_errors_are_status_codes_not_aborts(lib):
     from puncpp_gb300 import _lib
     h = C.c_void_p()

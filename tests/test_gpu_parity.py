@@ -270,6 +270,18 @@ def test_fused_deposit_equals_distribute(lib, oracle_mod):
     assert rel(punc.Function(pop, "rho").vector(), rho_o) < RTOL
 
 
+def test_cpp_time_loop_runs(lib, tmp_path):
+    """The C++ front end (include/punc_gpu.hpp) drives three reference-shaped steps."""
+    import subprocess
+
+    from test_abi import build_cpp_time_loop
+    exe = build_cpp_time_loop(tmp_path)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    lines = [l for l in r.stdout.splitlines() if l.startswith("step")]
+    assert len(lines) == 3 and all(l.endswith("particles 1") for l in lines)
+
+
 def test_sort_keeps_the_particle_set(lib, oracle_mod):
     ma, mesh, pop, o, rng = probe_setup(lib, oracle_mod)
     punc.move(pop, 0.5)
