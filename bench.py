@@ -44,6 +44,7 @@ def workload_name(n_side, n_per):
 DT = 0.05
 BIAS = -2.0
 RTOL, ATOL = 1e-10, 1e-12
+PRECONDS = {"amg": 0, "jacobi": 1}
 
 
 def peaks():
@@ -132,7 +133,7 @@ def run_ours(args):
     mesh = punc.Mesh(ma)
     prec = L.PG_MIXED if args.precision == "mixed" else L.PG_FP64
     pop = punc.Population(mesh, precision=prec, capacity=int(2.6 * args.n_per * 2), pcg_rtol=RTOL, pcg_atol=ATOL,
-                          pcg_max_iter=4000)
+                          pcg_max_iter=4000, pcg_precond=PRECONDS[args.pcg_precond])
     for s, (x, v) in zip(species, loads):
         pop.add_particles(x, v, s["q"], s["m"])
     sp = [punc.Species(s["q"], s["m"], n=s["n"], vth=s["vth"]) for s in species]
@@ -195,7 +196,8 @@ def run_ours(args):
     # roofline of the dominant stage
     hbm, src = peaks()
     nc, nv = ma.n_cells, mesh.n_dofs
-    nnz = int(mesh.table(L.T_CSR_COL).shape[0])
+    lay = punc.poisson_layout(pop)
+    nnz = lay["nnz"]
     n_avg = pushed_total / args.steps
     occ = nc * (1.0 - math.exp(-n_avg / nc))
     part_ms = stages.get("push_move_update_deposit", 0.0)
@@ -205,9 +207,13 @@ def run_ours(args):
     # PCG per iteration per nonzero / dof
     if mixed:
         pb, cb, pmodel = n_avg * 57 + occ * 160 + nv * 8, None, "Np*57 + occupied cells*160 + Ndof*8"
-        kb, kmodel = nnz * 8 + nv * 52, "per iteration nnz*8 + Ndof*52"
     else:
         pb, cb, pmodel = n_avg * 104 + occ * 288 + nv * 8, None, "Np*104 + occupied cells*288 + Ndof*8"
+    if lay["levels"]:
+        kb, kmodel = amg_iteration_bytes(lay)
+    elif mixed:
+        kb, kmodel = nnz * 8 + nv * 52, "per iteration nnz*8 + Ndof*52"
+    else:
         kb, kmodel = nnz * 12 + 7 * nv * 8, "per iteration nnz*12 + 7*Ndof*8"
     peak_src = (src + " (MEASURED_PEAKS.json hbm_gbs)") if src == "measured" else "fallback 6.8 TB/s"
 
@@ -219,8 +225,10 @@ def run_ours(args):
 
     r_part = roof_of("k_mixed (fused FP32 push+move+walk, fixed-point deposit)" if mixed
                      else "k_particles (fused FP64 push+move+walk+deposit)", args.steps * pb, part_ms, pmodel)
-    r_pcg = roof_of("k_pcg_rel (mixed PCG, one cooperative launch per solve)" if mixed
-                    else "k_pcg (FP64 Jacobi PCG, one cooperative launch per solve)", iters * kb, pcg_ms, kmodel)
+    pcg_kernel = ("k_pcg_amg (AMG-preconditioned mixed PCG, one cooperative launch per solve)" if lay["levels"]
+                  else "k_pcg_rel (mixed Jacobi PCG, one cooperative launch per solve)" if mixed
+                  else "k_pcg (FP64 Jacobi PCG, one cooperative launch per solve)")
+    r_pcg = roof_of(pcg_kernel, iters * kb, pcg_ms, kmodel)
     roof = r_pcg if pcg_ms >= part_ms else r_part
     stages_share = {k: round(v / ms, 4) for k, v in stages.items()}
 
@@ -230,7 +238,9 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64" if args.precision == "mixed" else "f64",
         "precision_form": args.precision,
         "data": "synthetic: seeded uniform/Maxwellian particles on a generated Kuhn probe mesh (no dataset)",
-        "config": {"workload": workload_name(args.n_side, args.n_per), "precision": args.precision, "cells": nc, "dofs": nv, "nnz": nnz, "particles_initial": n0,
+        "config": {"workload": workload_name(args.n_side, args.n_per), "precision": args.precision,
+                   "pcg_precond": args.pcg_precond, "cells": nc, "dofs": nv, "nnz": nnz,
+                   "amg_levels": [[v["rows"], v["nnz"]] for v in lay["levels"]], "particles_initial": n0,
                    "particles_mean_pushed": round(n_avg), "pcg_iterations_per_step": round(iters / args.steps, 1),
                    "l2": "inputs larger than L2 (particle SoA ~250 MB, mesh tables ~0.9 GB)"},
         "stage_ms": {k: round(v, 3) for k, v in stages.items()}, "stage_share": stages_share,
@@ -244,6 +254,26 @@ def run_ours(args):
     }
     pop.close()
     return out
+
+
+def amg_iteration_bytes(lay):
+    """Algorithmic bytes of one AMG-preconditioned PCG iteration, every operator
+    read once per use (FP32 value + int32 column = 8 B an entry):
+    level 0: the PCG product plus two smoother products of A, restriction and
+    prolongation, and 104 B of FP32/FP64 vector traffic per row; coarser
+    levels: two products of A, R and P, 52 B per row; the dense coarsest
+    inverse once."""
+    lv = lay["levels"]
+    b = 0
+    for l, v in enumerate(lv):
+        if l == len(lv) - 1:
+            b += v["rows"] * v["rows"] * 8 + v["rows"] * 8
+        elif l == 0:
+            b += 3 * v["nnz"] * 8 + 2 * v["nnz_p"] * 8 + 104 * v["rows"]
+        else:
+            b += 2 * v["nnz"] * 8 + 2 * v["nnz_p"] * 8 + 52 * v["rows"]
+    return b, ("per iteration: level 0 3*nnz*8 + 2*nnzP*8 + 104*rows; levels 1.. 2*nnz*8 + 2*nnzP*8 + 52*rows; "
+               "coarsest rows^2*8 (operators re-read from L2 count each time)")
 
 
 def ctypes_ms(lib, pop, a, b):
@@ -356,6 +386,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="probe-80", help="probe-N: N^3 sub-cubes, particles scaled by (N/80)^3")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--pcg-precond", default="amg", choices=sorted(PRECONDS),
+                    help="Poisson preconditioner: one AMG V-cycle or Jacobi per iteration")
     args = ap.parse_args()
     if not args.workload.startswith("probe-"):
         ap.error("--workload must be probe-N")

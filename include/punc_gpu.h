@@ -91,9 +91,13 @@ typedef struct pg_config {
                                    (punc/src/poisson.cpp:373-375); 0: by superposition of the
                                    unit-potential Laplace solutions kept from set-up (same
                                    potential up to the solver tolerance, one solve per step) */
-    int32_t pcg_precision;      /* 0: FP64 PCG for PG_FP64, mixed PCG for PG_MIXED; 1: FP64 PCG;
-                                   2: mixed PCG (FP32 recurrence, FP64 solution, inner products
-                                   and true-residual replacement; same FP64 stopping test) */
+    int32_t pcg_precision;      /* Jacobi preconditioner only: 0: FP64 PCG for PG_FP64, mixed PCG
+                                   for PG_MIXED; 1: FP64 PCG; 2: mixed PCG (FP32 recurrence, FP64
+                                   solution, inner products and true-residual replacement; same
+                                   FP64 stopping test) */
+    int32_t pcg_precond;        /* 0: smoothed-aggregation AMG V-cycle (mixed PCG; the reference
+                                   preconditions with hypre AMG, punc/src/object_CM.cpp:208-219);
+                                   1: Jacobi */
 } pg_config;
 
 /* Reference Object (punc/include/punc/object.h:80-130). */
@@ -258,6 +262,23 @@ int pg_event_elapsed(pg_sim *sim, int32_t from_slot, int32_t to_slot, double *ms
 int pg_synchronize(pg_sim *sim);
 /* Number of kernels this library has launched in this process. */
 int pg_launch_count(int64_t *n);
+
+/* Storage of the Poisson operator and its AMG hierarchy, for diagnostics and
+ * traffic models.  The reference's counterpart is PETSc's matrix and hypre's
+ * hierarchy statistics (-ksp_view). */
+#define PG_MAX_AMG_LEVELS 12
+typedef struct pg_poisson_layout {
+    int64_t n_rows;                          /* rows of the reduced operator (= dofs) */
+    int64_t nnz;                             /* stored nonzeros (exact zeros of K dropped) */
+    int64_t sell_entries;                    /* SELL-32 entries including padding */
+    int32_t precond;                         /* pg_config.pcg_precond */
+    int32_t levels;                          /* AMG levels (0 for Jacobi) */
+    int64_t level_rows[PG_MAX_AMG_LEVELS];
+    int64_t level_nnz[PG_MAX_AMG_LEVELS];    /* operator nonzeros per level */
+    int64_t level_nnz_p[PG_MAX_AMG_LEVELS];  /* nonzeros of the transfer operator S = (I - w D^-1 A) P
+                                                to the next level (0 on the coarsest level) */
+} pg_poisson_layout;
+int pg_poisson_layout_get(pg_sim *sim, pg_poisson_layout *out);
 
 /* Jacobi-preconditioned CG on a caller's CSR matrix (SPD, int32 indices, all
  * arrays in device memory), for callers that cannot allocate device memory:

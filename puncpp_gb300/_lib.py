@@ -48,7 +48,7 @@ class Config(C.Structure):
                 ("particle_capacity", C.c_int64), ("max_walk_steps", C.c_int32),
                 ("sort_interval", C.c_int32), ("pcg_rtol", C.c_double), ("pcg_atol", C.c_double),
                 ("pcg_max_iter", C.c_int32), ("pcg_warm_start", C.c_int32), ("ext_E", C.c_double * 3),
-                ("circuit_resolve", C.c_int32), ("pcg_precision", C.c_int32)]
+                ("circuit_resolve", C.c_int32), ("pcg_precision", C.c_int32), ("pcg_precond", C.c_int32)]
 
 
 class Object(C.Structure):
@@ -79,6 +79,16 @@ class StepArgs(C.Structure):
 class StepResult(C.Structure):
     _fields_ = [("KE", C.c_double), ("n_particles", C.c_int64), ("n_absorbed", C.c_int64),
                 ("n_injected", C.c_int64), ("pcg_iterations", C.c_int32), ("pcg_residual", C.c_double)]
+
+
+MAX_AMG_LEVELS = 12
+
+
+class PoissonLayout(C.Structure):
+    _fields_ = [("n_rows", C.c_int64), ("nnz", C.c_int64), ("sell_entries", C.c_int64),
+                ("precond", C.c_int32), ("levels", C.c_int32),
+                ("level_rows", C.c_int64 * MAX_AMG_LEVELS), ("level_nnz", C.c_int64 * MAX_AMG_LEVELS),
+                ("level_nnz_p", C.c_int64 * MAX_AMG_LEVELS)]
 
 
 # Every entry point of include/punc_gpu.h with its argument types.
@@ -128,6 +138,7 @@ SIGNATURES = {
     "pg_event_elapsed": ([_P, C.c_int32, C.c_int32, _D], C.c_int),
     "pg_synchronize": ([_P], C.c_int),
     "pg_launch_count": ([_I64], C.c_int),
+    "pg_poisson_layout_get": ([_P, C.POINTER(PoissonLayout)], C.c_int),
     "pg_pcg_solve_noalloc": ([C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                               C.c_double, C.c_int32, C.c_void_p, _I32, _D], C.c_int),
 }

@@ -33,8 +33,9 @@ CU_UNITS = {
     "k_inject.cu": [],
     "k_mixed.cu": ["--fmad=true"],
     "k_noalloc.cu": [],
+    "k_amg.cu": [],
 }
-CPP_UNITS = ["mesh_tables.cpp"]
+CPP_UNITS = ["mesh_tables.cpp", "amg.cpp"]
 
 
 def _nvcc() -> str:

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "pg_device.cuh"
+#include "pg_amg.h"
 #include "pg_internal.h"
 
 using namespace pg;
@@ -54,6 +55,10 @@ struct pg_sim {
     float *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *Ap32 = nullptr;
     double *obj_pot = nullptr, *image = nullptr;
     bool has_dirichlet = false;
+    bool use_amg = false;                      // AMG-preconditioned mixed PCG
+    AmgDev amg{};
+    std::vector<int64_t> amg_rows, amg_nnz, amg_nnz_p;   // per level (pg_poisson_layout_get)
+    int64_t a_nnz = 0, a_sell = 0;                       // stored nonzeros and SELL-32 entries of A
     bool phi_valid = false;
 
     // circuit (capacitance-matrix method)
@@ -319,6 +324,123 @@ std::vector<std::vector<int>> charge_sharing_sets(std::vector<pg_source> vs, int
 
 // ---- solver internals ------------------------------------------------------
 
+// Lanes per row of an AMG operator: SELL-32 with one thread per row up to 12
+// entries a row on average, else CSR with a power of two of lanes (at most
+// 32) giving each about three entries.
+static int lanes_per_row(const Csr &A) {
+    const double avg = A.n > 0 ? (double)A.ci.size() / (double)A.n : 0.0;
+    if (avg <= 12.0) return 1;
+    int g = 2;
+    while (g < 32 && 2.0 * g * 3.0 <= avg) g *= 2;
+    return g;
+}
+
+// Upload a CSR operator in FP32: SELL-32 (padding: column 0, value 0) when
+// g == 1, else CSR.
+static int upload_op(pg_sim *s, const Csr &A, int g, SpOp &out) {
+    const int64_t n = A.n;
+    int rc;
+    out.n = (int32_t)n;
+    out.g = g;
+    if (g > 1) {
+        std::vector<float> val(A.v.begin(), A.v.end());
+        if (val.empty()) val.push_back(0.0f);
+        std::vector<int32_t> col(A.ci);
+        if (col.empty()) col.push_back(0);
+        int64_t *d_ptr; int32_t *d_col; float *d_val;
+        if ((rc = upload(s, &d_ptr, A.rp)) || (rc = upload(s, &d_col, col)) || (rc = upload(s, &d_val, val))) return rc;
+        out.ptr = d_ptr; out.swidth = nullptr; out.col = d_col; out.val = d_val;
+        return PG_OK;
+    }
+    const int64_t nsl = (n + 31) / 32;
+    std::vector<int64_t> sptr(nsl + 1, 0);
+    std::vector<int32_t> swidth(nsl, 0);
+    for (int64_t sl = 0; sl < nsl; ++sl) {
+        int64_t w = 0;
+        for (int64_t r = 32 * sl; r < std::min(n, 32 * sl + 32); ++r) w = std::max(w, A.rp[r + 1] - A.rp[r]);
+        swidth[sl] = (int32_t)w;
+        sptr[sl + 1] = sptr[sl] + 32 * w;
+    }
+    std::vector<int32_t> col(std::max<int64_t>(1, sptr[nsl]), 0);
+    std::vector<float> val(std::max<int64_t>(1, sptr[nsl]), 0.0f);
+    for (int64_t sl = 0; sl < nsl; ++sl)
+        for (int lane = 0; lane < 32; ++lane) {
+            const int64_t r = 32 * sl + lane;
+            if (r >= n) continue;
+            const int64_t len = A.rp[r + 1] - A.rp[r];
+            for (int64_t k = 0; k < len; ++k) {
+                const int64_t o = sptr[sl] + 32 * k + lane;
+                col[o] = A.ci[A.rp[r] + k];
+                val[o] = (float)A.v[A.rp[r] + k];
+            }
+        }
+    int64_t *d_sptr; int32_t *d_sw, *d_col; float *d_val;
+    if ((rc = upload(s, &d_sptr, sptr)) || (rc = upload(s, &d_sw, swidth)) || (rc = upload(s, &d_col, col)) ||
+        (rc = upload(s, &d_val, val)))
+        return rc;
+    out.ptr = d_sptr; out.swidth = d_sw; out.col = d_col; out.val = d_val;
+    return PG_OK;
+}
+
+// Smoothed-aggregation hierarchy of the reduced Poisson matrix, on the
+// device.  Level 0 shares the solver's FP32 SELL-32 matrix and D^-1.
+static int setup_amg(pg_sim *s, const std::vector<int32_t> &arow, const std::vector<int32_t> &acol,
+                     const std::vector<double> &aval) {
+    Csr A0;
+    A0.n = A0.m = (int64_t)arow.size() - 1;
+    A0.rp.assign(arow.begin(), arow.end());
+    A0.ci = acol;
+    A0.v = aval;
+    AmgHierarchy h;
+    const int arc = amg_setup(A0, h, s->cfg.periodic != 0);
+    if (arc == 9) return fail(PG_ERR_ARG, "AMG: coarsening stalls above 4096 rows (use pcg_precond = 1)");
+    if (arc != 0) return fail(PG_ERR_SINGULAR, "AMG: coarsest operator is singular");
+    if ((int)h.levels.size() > kAmgMaxLevels) return fail(PG_ERR_ARG, "AMG: too many levels");
+    AmgDev &M = s->amg;
+    M = AmgDev{};
+    M.nlev = (int32_t)h.levels.size();
+    s->amg_rows.assign(M.nlev, 0);
+    s->amg_nnz.assign(M.nlev, 0);
+    s->amg_nnz_p.assign(M.nlev, 0);
+    int rc;
+    for (int l = 0; l < M.nlev; ++l) {
+        const AmgLevel &L = h.levels[l];
+        AmgLevelDev &D = M.lev[l];
+        s->amg_rows[l] = L.A.n;
+        s->amg_nnz[l] = (int64_t)L.A.ci.size();
+        if (l == 0) {
+            D.A.n = (int32_t)L.A.n; D.A.g = 1;
+            D.A.ptr = s->A_sptr; D.A.swidth = s->A_swidth; D.A.col = s->A_col; D.A.val = s->A_val32;
+            D.dinv = s->A_dinv32;
+        } else {
+            if ((rc = upload_op(s, L.A, lanes_per_row(L.A), D.A))) return rc;
+            std::vector<float> dinv(L.dinv.begin(), L.dinv.end());
+            float *d_dinv;
+            if ((rc = upload(s, &d_dinv, dinv))) return rc;
+            D.dinv = d_dinv;
+        }
+        if (l + 1 < M.nlev) {
+            s->amg_nnz_p[l] = (int64_t)L.S.ci.size();
+            if ((rc = upload_op(s, L.S, lanes_per_row(L.S), D.S)) || (rc = upload_op(s, L.ST, lanes_per_row(L.ST), D.ST)))
+                return rc;
+        }
+        D.omega = (float)L.omega;
+        if ((rc = dalloc(s, &D.b, L.A.n)) || (rc = dalloc(s, &D.t, L.A.n)) || (rc = dalloc(s, &D.y, L.A.n))) return rc;
+    }
+    // the coarsest inverse as a dense CSR operator, 32 lanes per row
+    const int64_t nc = h.levels.back().A.n;
+    Csr C;
+    C.n = C.m = nc;
+    C.rp.resize(nc + 1);
+    C.ci.resize(nc * nc);
+    for (int64_t i = 0; i <= nc; ++i) C.rp[i] = i * nc;
+    for (int64_t k = 0; k < nc * nc; ++k) C.ci[k] = (int32_t)(k % nc);
+    C.v = h.coarse_inv;
+    if ((rc = upload_op(s, C, 32, M.cinv))) return rc;
+    s->use_amg = true;
+    return PG_OK;
+}
+
 static int object_index(const pg_sim *s, int64_t bnd_id) {
     const int64_t k = bnd_id - 2;
     return (k >= 0 && k < s->n_obj) ? (int)k : -1;
@@ -354,7 +476,7 @@ static int poisson_solve_internal(pg_sim *s, const double *pot_h, bool zero_rho,
     int e;
     {
         StageScope t(s, "pcg");
-        e = launch_pcg(a, s->stream);
+        e = s->use_amg ? launch_pcg_amg(a, s->amg, s->stream) : launch_pcg(a, s->stream);
     }
     if (e) return fail(PG_ERR_CUDA, std::string("cooperative PCG launch: ") + cudaGetErrorString((cudaError_t)e));
     int32_t oi[2];
@@ -743,6 +865,7 @@ int pg_create(const pg_mesh *mesh, const pg_config *cfg_in, pg_sim **out) {
                 for (int64_t k = h.rowptr[i]; k < h.rowptr[i + 1]; ++k) {
                     const int64_t j = h.col[k];
                     if (kind[j] < 0) {
+                        if (h.K[k] == 0.0 && j != i) continue;   // exact zeros of K add nothing
                         acol.push_back((int32_t)j);
                         aval.push_back(h.K[k]);
                         if (j == i) dinv[i] = 1.0 / h.K[k];
@@ -785,13 +908,17 @@ int pg_create(const pg_mesh *mesh, const pg_config *cfg_in, pg_sim **out) {
             (rc = upload(s, &s->M_val, h.M)) || (rc = upload(s, &s->bc_kind, kind)) || (rc = upload(s, &s->bc_value, gval)) ||
             (rc = upload(s, &s->w_ext, wext)) || (rc = upload(s, &s->w_obj, wobj)))
             return bail(rc);
-        const int nb = pcg_grid_blocks();
+        const int nb = std::max(pcg_grid_blocks(), pcg_amg_grid_blocks());
         if ((rc = dalloc(s, &s->r, nd)) || (rc = dalloc(s, &s->z, nd)) || (rc = dalloc(s, &s->p0, nd)) ||
             (rc = dalloc(s, &s->p1, nd)) || (rc = dalloc(s, &s->Ap, nd)) || (rc = dalloc(s, &s->pcg_part, 4 * nb)) ||
             (rc = dalloc(s, &s->pcg_out_i, 2)) || (rc = dalloc(s, &s->pcg_out_d, 2)) ||
             (rc = dalloc(s, &s->obj_pot, std::max(1, s->n_obj))) || (rc = dalloc(s, &s->image, std::max(1, s->n_obj))))
             return bail(rc);
-        const int mode = cfg.pcg_precision == 0 ? (cfg.precision == PG_MIXED ? 2 : 1) : cfg.pcg_precision;
+        if (cfg.pcg_precond != 0 && cfg.pcg_precond != 1) return bail(fail(PG_ERR_ARG, "pg_create: unknown pcg_precond"));
+        const bool amg = cfg.pcg_precond == 0;
+        const int mode = amg ? 2 : (cfg.pcg_precision == 0 ? (cfg.precision == PG_MIXED ? 2 : 1) : cfg.pcg_precision);
+        s->a_nnz = (int64_t)acol.size();
+        s->a_sell = sptr[nsl];
         if (mode == 2) {
             std::vector<float> v32(sval.begin(), sval.end()), d32(dinv.begin(), dinv.end());
             if ((rc = upload(s, &s->A_val32, v32)) || (rc = upload(s, &s->A_dinv32, d32)) ||
@@ -801,6 +928,7 @@ int pg_create(const pg_mesh *mesh, const pg_config *cfg_in, pg_sim **out) {
         } else if (mode != 1) {
             return bail(fail(PG_ERR_ARG, "pg_create: unknown pcg_precision"));
         }
+        if (amg && (rc = setup_amg(s, arow, acol, aval))) return bail(rc);
     }
 
     // boundary facets
@@ -1461,6 +1589,22 @@ int pg_event_elapsed(pg_sim *s, int32_t a, int32_t b, double *ms) {
     float f = 0;
     PG_CUDA(cudaEventElapsedTime(&f, s->user_ev[a], s->user_ev[b]));
     *ms = f;
+    return PG_OK;
+}
+
+int pg_poisson_layout_get(pg_sim *s, pg_poisson_layout *out) {
+    if (!s || !out) return fail(PG_ERR_ARG, "pg_poisson_layout_get: null argument");
+    *out = pg_poisson_layout{};
+    out->n_rows = s->ndof;
+    out->nnz = s->a_nnz;
+    out->sell_entries = s->a_sell;
+    out->precond = s->cfg.pcg_precond;
+    out->levels = s->use_amg ? s->amg.nlev : 0;
+    for (int l = 0; l < out->levels && l < PG_MAX_AMG_LEVELS; ++l) {
+        out->level_rows[l] = s->amg_rows[l];
+        out->level_nnz[l] = s->amg_nnz[l];
+        out->level_nnz_p[l] = s->amg_nnz_p[l];
+    }
     return PG_OK;
 }
 

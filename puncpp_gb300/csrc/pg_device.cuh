@@ -150,6 +150,34 @@ struct PcgArgs {
     int32_t *out_updates;         // reliable updates done
 };
 
+// AMG hierarchy on the device: FP32 sparse operators, each either SELL-32
+// (one thread per row, g == 1) or CSR processed by g lanes per row (g a power
+// of two up to 32) for operators with long rows.
+struct SpOp {
+    int32_t n = 0;                       // rows
+    int32_t g = 1;                       // lanes per row
+    const int64_t *ptr = nullptr;        // SELL slice offsets [n_slices+1] or CSR row offsets [n+1]
+    const int32_t *swidth = nullptr;     // SELL slice widths (g == 1 only)
+    const int32_t *col = nullptr;
+    const float *val = nullptr;
+};
+
+constexpr int kAmgMaxLevels = 12;
+
+struct AmgLevelDev {
+    SpOp A;                              // level operator
+    SpOp S, ST;                          // S = (I - omega D^-1 A) P: n x n_next, and S^T
+    const float *dinv = nullptr;
+    float omega = 0.f;
+    float *b = nullptr, *t = nullptr, *y = nullptr;   // right-hand side, W b, V-cycle result
+};
+
+struct AmgDev {
+    int32_t nlev = 0;
+    AmgLevelDev lev[kAmgMaxLevels];
+    SpOp cinv;                           // dense inverse of the coarsest operator (CSR, 32 lanes per row)
+};
+
 // ---- launch wrappers (all on `stream`) -----------------------------------
 int sm_count();
 // Kernels launched by this library in this process (pg_launch_count).
@@ -193,6 +221,8 @@ void launch_set_bc(const int32_t *bc_kind, const double *bc_value, const double 
                    int32_t n, double *x, cudaStream_t st);
 int launch_pcg(const PcgArgs &a, cudaStream_t st);
 int pcg_grid_blocks();
+int launch_pcg_amg(const PcgArgs &a, const AmgDev &amg, cudaStream_t st);
+int pcg_amg_grid_blocks();
 struct Pots {
     int32_t n;
     double v[kMaxTags];

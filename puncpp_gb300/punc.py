@@ -121,12 +121,12 @@ class Population:
     def __init__(self, mesh: Mesh, precision: int = L.PG_FP64, periodic: bool = False, capacity: int = 0,
                  max_walk_steps: int = 0, sort_interval: int = 0, pcg_rtol: float = 0.0, pcg_atol: float = 0.0,
                  pcg_max_iter: int = 0, warm_start: bool = True, ext_E=(0.0, 0.0, 0.0),
-                 circuit_resolve: bool = False, pcg_precision: int = 0):
+                 circuit_resolve: bool = False, pcg_precision: int = 0, pcg_precond: int = 0):
         lib = L.load()
         self.mesh = mesh
         cfg = L.Config(precision, 1 if periodic else 0, mesh.eps0, capacity, max_walk_steps, sort_interval,
                        pcg_rtol, pcg_atol, pcg_max_iter, 1 if warm_start else 0, (C.c_double * 3)(*ext_E),
-                       1 if circuit_resolve else 0, pcg_precision)
+                       1 if circuit_resolve else 0, pcg_precision, pcg_precond)
         h = C.c_void_p()
         L.check(lib.pg_create(mesh.handle, C.byref(cfg), C.byref(h)))
         self.handle = h
@@ -345,6 +345,17 @@ def stage_times(pop: Population) -> dict:
     ms = np.zeros(32)
     L.check(lib.pg_stage_times(pop.handle, L.dptr(ms), 32, C.byref(n)))
     return {lib.pg_stage_name(pop.handle, k).decode(): float(ms[k]) for k in range(n.value)}
+
+
+def poisson_layout(pop: Population) -> dict:
+    """Stored size of the Poisson operator and of its AMG levels."""
+    lib = L.load()
+    out = L.PoissonLayout()
+    L.check(lib.pg_poisson_layout_get(pop.handle, C.byref(out)))
+    n = out.levels
+    return {"n_rows": out.n_rows, "nnz": out.nnz, "sell_entries": out.sell_entries, "precond": out.precond,
+            "levels": [{"rows": out.level_rows[l], "nnz": out.level_nnz[l], "nnz_p": out.level_nnz_p[l]}
+                       for l in range(n)]}
 
 
 def set_profiling(pop: Population, on: bool):

@@ -1,0 +1,201 @@
+"""Host-side smoothed-aggregation hierarchy of the Poisson preconditioner
+(puncpp_gb300/csrc/amg.cpp), checked on the CPU: Galerkin coarse operators,
+R = P^T, the coarsest inverse, the constant null space of periodic meshes,
+and the iteration count of CG preconditioned by the same V-cycle the device
+kernel runs (restated here in FP64 numpy)."""
+import ctypes as C
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from puncpp_gb300 import meshgen
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, "puncpp_gb300", "csrc")
+
+
+@pytest.fixture(scope="module")
+def amgd(tmp_path_factory):
+    if not shutil.which("g++"):
+        pytest.skip("g++ not available")
+    so = tmp_path_factory.mktemp("amg") / "libamgd.so"
+    r = subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-ffp-contract=off", "-I" + CSRC,
+                        os.path.join(ROOT, "tests", "cpp", "amg_dump.cpp"), os.path.join(CSRC, "amg.cpp"),
+                        "-o", str(so)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    d = C.CDLL(str(so))
+    d.amgd_setup.restype = C.c_void_p
+    d.amgd_setup.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double,
+                             C.c_int64, C.POINTER(C.c_int)]
+    d.amgd_levels.argtypes = [C.c_void_p]
+    d.amgd_shape.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    d.amgd_copy.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    d.amgd_omega.argtypes = [C.c_void_p, C.c_int]
+    d.amgd_omega.restype = C.c_double
+    d.amgd_coarse_inv.argtypes = [C.c_void_p, C.c_void_p]
+    d.amgd_free.argtypes = [C.c_void_p]
+    return d
+
+
+def hierarchy(d, A, nullspace=False, theta=-1.0, theta_factor=0.0, coarse_max=0):
+    A = sp.csr_matrix(A)
+    A.sort_indices()
+    rp = A.indptr.astype(np.int64)
+    ci = A.indices.astype(np.int32)
+    v = A.data.astype(np.float64)
+    rc = C.c_int(-1)
+    h = d.amgd_setup(A.shape[0], rp.ctypes.data, ci.ctypes.data, v.ctypes.data, 1 if nullspace else 0, theta,
+                     theta_factor, coarse_max, C.byref(rc))
+    try:
+        assert rc.value == 0
+        levels = []
+        for l in range(d.amgd_levels(h)):
+            ops = {}
+            for which, name in enumerate(["A", "P", "R", "S", "ST"]):
+                shape = np.zeros(3, np.int64)
+                d.amgd_shape(h, l, which, shape.ctypes.data)
+                n, m, nnz = (int(x) for x in shape)
+                if n == 0:
+                    continue
+                orp = np.zeros(n + 1, np.int64)
+                oci = np.zeros(max(nnz, 1), np.int32)
+                ov = np.zeros(max(nnz, 1))
+                d.amgd_copy(h, l, which, orp.ctypes.data, oci.ctypes.data, ov.ctypes.data)
+                ops[name] = sp.csr_matrix((ov[:nnz], oci[:nnz], orp), shape=(n, m))
+            ops["omega"] = d.amgd_omega(h, l)
+            levels.append(ops)
+        nc = levels[-1]["A"].shape[0]
+        cinv = np.zeros(nc * nc)
+        d.amgd_coarse_inv(h, cinv.ctypes.data)
+        return levels, cinv.reshape(nc, nc)
+    finally:
+        d.amgd_free(h)
+
+
+def reduced_operator(oracle_mod, ma, periodic=False):
+    """The solver's matrix: Dirichlet rows and columns replaced by identity."""
+    o = oracle_mod.Oracle(ma)
+    K, _ = o.matrices()
+    kind, _ = o.dirichlet(periodic)
+    free = (kind < 0).astype(float)
+    A = sp.diags(free) @ K @ sp.diags(free) + sp.diags(1.0 - free)
+    A = sp.csr_matrix(A)
+    A.eliminate_zeros()
+    return A
+
+
+def vcycle_textbook(levels, cinv, b, l=0):
+    """One V-cycle: a weighted-Jacobi sweep from zero, restriction, coarse
+    correction, prolongation, one more sweep."""
+    L = levels[l]
+    if l == len(levels) - 1:
+        return cinv @ b
+    dinv = 1.0 / L["A"].diagonal()
+    x = L["omega"] * dinv * b
+    r = b - L["A"] @ x
+    x = x + L["P"] @ vcycle_textbook(levels, cinv, L["R"] @ r, l + 1)
+    return x + L["omega"] * dinv * (b - L["A"] @ x)
+
+
+def vcycle(levels, cinv, b, l=0):
+    """The same V-cycle as the device applies it: B b = W b + S B_c S^T b with
+    W = w D^-1 (2 I - A w D^-1) and S = (I - w D^-1 A) P."""
+    L = levels[l]
+    if l == len(levels) - 1:
+        return cinv @ b
+    m = L["omega"] / L["A"].diagonal()
+    t = m * (2.0 * b - L["A"] @ (m * b))
+    return t + L["S"] @ vcycle(levels, cinv, L["ST"] @ b, l + 1)
+
+
+def pcg(A, b, prec, rtol):
+    x = np.zeros_like(b)
+    r = b.copy()
+    z = prec(r)
+    p = z.copy()
+    rz = r @ z
+    tol = rtol * np.linalg.norm(b)
+    for it in range(1, 5000):
+        Ap = A @ p
+        a = rz / (p @ Ap)
+        x += a * p
+        r -= a * Ap
+        if np.linalg.norm(r) <= tol:
+            return x, it
+        z = prec(r)
+        rz, rz_old = r @ z, rz
+        p = z + (rz / rz_old) * p
+    raise AssertionError("no convergence")
+
+
+@pytest.fixture(scope="module")
+def probe(oracle_mod):
+    ma = meshgen.probe_box(14, 4.0, 0.8)
+    return ma, reduced_operator(oracle_mod, ma)
+
+
+def test_levels_coarsen_and_are_galerkin(amgd, probe):
+    ma, A = probe
+    levels, cinv = hierarchy(amgd, A)
+    assert len(levels) >= 2
+    sizes = [L["A"].shape[0] for L in levels]
+    assert sizes[-1] <= 400
+    assert all(sizes[k + 1] * 4 < sizes[k] for k in range(len(sizes) - 1)), sizes
+    for k in range(len(levels) - 1):
+        L, N = levels[k], levels[k + 1]
+        assert abs(L["R"] - L["P"].T).max() == 0.0
+        G = L["R"] @ L["A"] @ L["P"]
+        assert abs(G - N["A"]).max() <= 1e-12 * abs(N["A"]).max()
+        assert abs(N["A"] - N["A"].T).max() <= 1e-12 * abs(N["A"]).max()
+        assert 0.0 < L["omega"] < 2.0
+    Ac = levels[-1]["A"].toarray()
+    np.testing.assert_allclose(cinv @ Ac, np.eye(len(Ac)), atol=1e-9)
+
+
+def test_transfer_operators_give_the_textbook_vcycle(amgd, probe):
+    ma, A = probe
+    levels, cinv = hierarchy(amgd, A)
+    for L in levels[:-1]:
+        m = L["omega"] / L["A"].diagonal()
+        S = L["P"] - sp.diags(m) @ (L["A"] @ L["P"])
+        assert abs(S - L["S"]).max() <= 1e-12 * abs(L["P"]).max()
+        assert abs(L["ST"] - L["S"].T).max() == 0.0
+    b = np.random.default_rng(7).standard_normal(A.shape[0])
+    np.testing.assert_allclose(vcycle(levels, cinv, b), vcycle_textbook(levels, cinv, b), rtol=0, atol=1e-10)
+
+
+def test_vcycle_preconditioner_beats_jacobi(amgd, probe):
+    ma, A = probe
+    levels, cinv = hierarchy(amgd, A)
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal(A.shape[0])
+    x, it_amg = pcg(A, b, lambda r: vcycle(levels, cinv, r), 1e-10)
+    assert np.linalg.norm(b - A @ x) <= 1e-10 * np.linalg.norm(b)
+    dinv = 1.0 / A.diagonal()
+    _, it_jac = pcg(A, b, lambda r: dinv * r, 1e-10)
+    assert it_amg < 25 and it_amg * 4 < it_jac, (it_amg, it_jac)
+
+
+def test_periodic_constant_null_space(amgd, oracle_mod):
+    ma = meshgen.langmuir_cube(10)
+    A = reduced_operator(oracle_mod, ma, periodic=True)
+    assert abs(A @ np.ones(A.shape[0])).max() < 1e-12 * abs(A).max()
+    levels, cinv = hierarchy(amgd, A, nullspace=True)
+    for L in levels[:-1]:
+        ones_c = np.ones(L["P"].shape[1])
+        np.testing.assert_allclose(L["P"] @ ones_c, 1.0, atol=1e-12)
+    Ac = levels[-1]["A"].toarray()
+    nc = len(Ac)
+    assert abs(Ac @ np.ones(nc)).max() < 1e-10 * abs(Ac).max()
+    reg = Ac + np.trace(Ac) / nc ** 2 * np.ones((nc, nc))
+    np.testing.assert_allclose(cinv @ reg, np.eye(nc), atol=1e-9)
+    # singular but consistent: CG on the mean-free right-hand side converges
+    rng = np.random.default_rng(4)
+    b = rng.standard_normal(A.shape[0])
+    b -= b.mean()
+    x, it = pcg(A, b, lambda r: vcycle(levels, cinv, r), 1e-10)
+    assert it < 25

@@ -126,8 +126,13 @@ def test_distribute_cg1(geom, lib, oracle_mod):
     np.testing.assert_array_equal(punc.Function(pop, "rho").vector(), rho_g)
 
 
-def test_poisson_dirichlet_and_objects(lib, oracle_mod):
-    ma, mesh, pop, o, rng = probe_setup(lib, oracle_mod, pcg_rtol=1e-14, pcg_atol=1e-30, pcg_max_iter=5000)
+PRECONDS = {"amg": 0, "jacobi": 1}
+
+
+@pytest.mark.parametrize("precond", sorted(PRECONDS))
+def test_poisson_dirichlet_and_objects(precond, lib, oracle_mod):
+    ma, mesh, pop, o, rng = probe_setup(lib, oracle_mod, pcg_rtol=1e-14, pcg_atol=1e-30, pcg_max_iter=5000,
+                                        pcg_precond=PRECONDS[precond])
     rho = punc.distribute_cg1(pop)
     objs = [punc.Object(2, potential=-2.0)]
     solver = punc.PoissonSolver(pop, objs)
@@ -137,12 +142,13 @@ def test_poisson_dirichlet_and_objects(lib, oracle_mod):
     assert solver.last_info.iterations > 0
 
 
+@pytest.mark.parametrize("precond", sorted(PRECONDS))
 @pytest.mark.parametrize("rtol", [1e-10, 1e-13])
-def test_mixed_precision_pcg_meets_the_fp64_tolerance(rtol, lib, oracle_mod):
+def test_mixed_precision_pcg_meets_the_fp64_tolerance(rtol, precond, lib, oracle_mod):
     """FP32 recurrence with FP64 true-residual replacement: the returned FP64
     residual meets the same stopping test as the FP64 solver."""
     ma, mesh, pop, o, rng = probe_setup(lib, oracle_mod, pcg_rtol=rtol, pcg_atol=1e-30, pcg_max_iter=5000,
-                                        pcg_precision=2)
+                                        pcg_precision=2, pcg_precond=PRECONDS[precond])
     rho = punc.distribute_cg1(pop)
     objs = [punc.Object(2, potential=-2.0)]
     solver = punc.PoissonSolver(pop, objs)
@@ -153,13 +159,40 @@ def test_mixed_precision_pcg_meets_the_fp64_tolerance(rtol, lib, oracle_mod):
     assert rel(phi_g, phi_o) < 1e4 * rtol
 
 
-def test_poisson_periodic_null_space(lib, oracle_mod):
-    ma, mesh, pop, o, rng = periodic_setup(lib, oracle_mod, pcg_rtol=1e-14, pcg_atol=1e-30, pcg_max_iter=5000)
+@pytest.mark.parametrize("precond", sorted(PRECONDS))
+def test_poisson_periodic_null_space(precond, lib, oracle_mod):
+    ma, mesh, pop, o, rng = periodic_setup(lib, oracle_mod, pcg_rtol=1e-14, pcg_atol=1e-30, pcg_max_iter=5000,
+                                           pcg_precond=PRECONDS[precond])
     rho = punc.distribute_cg1(pop)
     phi_g = punc.PoissonSolver(pop).solve(punc.Function(pop, "phi"), punc.Function(pop, "rho"))
     phi_o = o.poisson_direct(rho, periodic=True)
     assert abs(phi_g.mean()) < 1e-13 * np.abs(phi_g).max()
     assert rel(phi_g, phi_o) < 1e-10
+
+
+def test_amg_needs_far_fewer_iterations_than_jacobi(lib, oracle_mod):
+    """Same system, same tolerance: the V-cycle preconditioner cuts the
+    iteration count several-fold and both meet the stopping test."""
+    its = {}
+    for name, code in PRECONDS.items():
+        ma, mesh, pop, o, rng = probe_setup(lib, oracle_mod, n=16, half=4.0, radius=0.8, n_particles=20000,
+                                            pcg_rtol=1e-10, pcg_atol=1e-30, pcg_max_iter=5000, pcg_precond=code)
+        punc.distribute_cg1(pop)
+        objs = [punc.Object(2, potential=-2.0)]
+        solver = punc.PoissonSolver(pop, objs)
+        solver.solve(punc.Function(pop, "phi"), punc.Function(pop, "rho"), objs)
+        info = solver.last_info
+        assert info.residual <= 1e-10 * info.rhs_norm
+        its[name] = info.iterations
+        lay = punc.poisson_layout(pop)
+        assert lay["n_rows"] == mesh.n_dofs and 0 < lay["nnz"] <= lay["sell_entries"]
+        if code == 0:
+            rows = [v["rows"] for v in lay["levels"]]
+            assert len(rows) >= 2 and rows[0] == mesh.n_dofs and rows == sorted(rows, reverse=True)
+            assert lay["levels"][-1]["nnz_p"] == 0 and all(v["nnz_p"] > 0 for v in lay["levels"][:-1])
+        else:
+            assert lay["levels"] == []
+    assert its["amg"] * 3 < its["jacobi"], its
 
 
 @pytest.mark.parametrize("resolve", [True, False])
