@@ -292,4 +292,53 @@ int amg_setup(const Csr &A0, AmgHierarchy &h, bool constant_nullspace, const Amg
     return 0;
 }
 
+void amg_cycle_operators(const AmgHierarchy &h, AmgCycle &c) {
+    c = AmgCycle{};
+    const int L = (int)h.levels.size() - 1;
+    if (L < 1) return;
+    const int64_t nL = h.levels[L].A.n;
+    // G = C^-1 S_{L-1}^T: column j of G is C^-1 (row j of S_{L-1})
+    const Csr &S = h.levels[L - 1].S;
+    std::vector<double> g((size_t)nL * S.n, 0.0);
+    for (int64_t j = 0; j < S.n; ++j)
+        for (int64_t k = S.rp[j]; k < S.rp[j + 1]; ++k) {
+            const int32_t col = S.ci[k];
+            const double v = S.v[k];
+            for (int64_t r = 0; r < nL; ++r) g[(size_t)r * S.n + j] += h.coarse_inv[(size_t)r * nL + col] * v;
+        }
+    c.G.n = nL;
+    c.G.m = S.n;
+    c.G.rp.assign(nL + 1, 0);
+    for (int64_t r = 0; r < nL; ++r) {
+        for (int64_t j = 0; j < S.n; ++j)
+            if (g[(size_t)r * S.n + j] != 0.0) { c.G.ci.push_back((int32_t)j); c.G.v.push_back(g[(size_t)r * S.n + j]); }
+        c.G.rp[r + 1] = (int64_t)c.G.ci.size();
+    }
+    c.stack_off.assign(L + 1, 0);
+    if (L < 2) {
+        c.stack_len = nL;
+        return;
+    }
+    for (int l = 2; l <= L; ++l) c.stack_off[l] = l == 2 ? 0 : c.stack_off[l - 1] + h.levels[l - 1].A.n;
+    c.stack_len = c.stack_off[L] + nL;
+    // blocks Q_l = S_1 ... S_{l-1}, l = 2..L
+    std::vector<Csr> Q;
+    Q.push_back(h.levels[1].S);
+    for (int l = 3; l <= L; ++l) Q.push_back(spgemm(Q.back(), h.levels[l - 1].S));
+    const int64_t n1 = h.levels[1].A.n;
+    c.U1.n = n1;
+    c.U1.m = c.stack_len;
+    c.U1.rp.assign(n1 + 1, 0);
+    for (int64_t i = 0; i < n1; ++i) {
+        for (int l = 2; l <= L; ++l) {
+            const Csr &q = Q[l - 2];
+            for (int64_t k = q.rp[i]; k < q.rp[i + 1]; ++k) {
+                c.U1.ci.push_back((int32_t)(q.ci[k] + c.stack_off[l]));
+                c.U1.v.push_back(q.v[k]);
+            }
+        }
+        c.U1.rp[i + 1] = (int64_t)c.U1.ci.size();
+    }
+}
+
 }  // namespace pg

@@ -326,12 +326,12 @@ std::vector<std::vector<int>> charge_sharing_sets(std::vector<pg_source> vs, int
 
 // Lanes per row of an AMG operator: SELL-32 with one thread per row up to 12
 // entries a row on average, else CSR with a power of two of lanes (at most
-// 32) giving each about three entries.
+// 512, the block) giving each lane three to six entries.
 static int lanes_per_row(const Csr &A) {
     const double avg = A.n > 0 ? (double)A.ci.size() / (double)A.n : 0.0;
     if (avg <= 12.0) return 1;
     int g = 2;
-    while (g < 32 && 2.0 * g * 3.0 <= avg) g *= 2;
+    while (g < 512 && 2.0 * g * 3.0 <= avg) g *= 2;
     return g;
 }
 
@@ -383,7 +383,8 @@ static int upload_op(pg_sim *s, const Csr &A, int g, SpOp &out) {
 }
 
 // Smoothed-aggregation hierarchy of the reduced Poisson matrix, on the
-// device.  Level 0 shares the solver's FP32 SELL-32 matrix and D^-1.
+// device, with the operators of the collapsed cycle.  Level 0 shares the
+// solver's FP32 SELL-32 matrix and D^-1.
 static int setup_amg(pg_sim *s, const std::vector<int32_t> &arow, const std::vector<int32_t> &acol,
                      const std::vector<double> &aval) {
     Csr A0;
@@ -396,47 +397,62 @@ static int setup_amg(pg_sim *s, const std::vector<int32_t> &arow, const std::vec
     if (arc == 9) return fail(PG_ERR_ARG, "AMG: coarsening stalls above 4096 rows (use pcg_precond = 1)");
     if (arc != 0) return fail(PG_ERR_SINGULAR, "AMG: coarsest operator is singular");
     if ((int)h.levels.size() > kAmgMaxLevels) return fail(PG_ERR_ARG, "AMG: too many levels");
+    AmgCycle cyc;
+    amg_cycle_operators(h, cyc);
     AmgDev &M = s->amg;
     M = AmgDev{};
     M.nlev = (int32_t)h.levels.size();
+    const int L = M.nlev - 1;
     s->amg_rows.assign(M.nlev, 0);
     s->amg_nnz.assign(M.nlev, 0);
     s->amg_nnz_p.assign(M.nlev, 0);
     int rc;
+    if (L >= 1 && (rc = dalloc(s, &M.stack, cyc.stack_len))) return rc;
     for (int l = 0; l < M.nlev; ++l) {
-        const AmgLevel &L = h.levels[l];
+        const AmgLevel &Lv = h.levels[l];
+        s->amg_rows[l] = Lv.A.n;
+        s->amg_nnz[l] = (int64_t)Lv.A.ci.size();
+        if (l < L) s->amg_nnz_p[l] = (int64_t)Lv.S.ci.size();
         AmgLevelDev &D = M.lev[l];
-        s->amg_rows[l] = L.A.n;
-        s->amg_nnz[l] = (int64_t)L.A.ci.size();
         if (l == 0) {
-            D.A.n = (int32_t)L.A.n; D.A.g = 1;
+            // the PCG's own product reads level 0's operator, also when L == 0
+            D.A.n = (int32_t)Lv.A.n; D.A.g = 1;
             D.A.ptr = s->A_sptr; D.A.swidth = s->A_swidth; D.A.col = s->A_col; D.A.val = s->A_val32;
             D.dinv = s->A_dinv32;
-        } else {
-            if ((rc = upload_op(s, L.A, lanes_per_row(L.A), D.A))) return rc;
-            std::vector<float> dinv(L.dinv.begin(), L.dinv.end());
+        }
+        if (l == L) break;   // the coarsest level lives in G (or cinv when L == 0)
+        if (l > 0) {
+            if ((rc = upload_op(s, Lv.A, lanes_per_row(Lv.A), D.A))) return rc;
+            std::vector<float> dinv(Lv.dinv.begin(), Lv.dinv.end());
             float *d_dinv;
-            if ((rc = upload(s, &d_dinv, dinv))) return rc;
+            if ((rc = upload(s, &d_dinv, dinv)) || (rc = dalloc(s, &D.b, Lv.A.n))) return rc;
             D.dinv = d_dinv;
         }
-        if (l + 1 < M.nlev) {
-            s->amg_nnz_p[l] = (int64_t)L.S.ci.size();
-            if ((rc = upload_op(s, L.S, lanes_per_row(L.S), D.S)) || (rc = upload_op(s, L.ST, lanes_per_row(L.ST), D.ST)))
-                return rc;
-        }
-        D.omega = (float)L.omega;
-        if ((rc = dalloc(s, &D.b, L.A.n)) || (rc = dalloc(s, &D.t, L.A.n)) || (rc = dalloc(s, &D.y, L.A.n))) return rc;
+        D.omega = (float)Lv.omega;
+        if (l < L - 1 && (rc = upload_op(s, Lv.ST, lanes_per_row(Lv.ST), D.ST))) return rc;
+        if (l >= 2) D.t = M.stack + cyc.stack_off[l];
+        else if ((rc = dalloc(s, &D.t, Lv.A.n))) return rc;
     }
-    // the coarsest inverse as a dense CSR operator, 32 lanes per row
-    const int64_t nc = h.levels.back().A.n;
-    Csr C;
-    C.n = C.m = nc;
-    C.rp.resize(nc + 1);
-    C.ci.resize(nc * nc);
-    for (int64_t i = 0; i <= nc; ++i) C.rp[i] = i * nc;
-    for (int64_t k = 0; k < nc * nc; ++k) C.ci[k] = (int32_t)(k % nc);
-    C.v = h.coarse_inv;
-    if ((rc = upload_op(s, C, 32, M.cinv))) return rc;
+    if (L == 0) {
+        // the whole operator is the coarsest: z = C^-1 r
+        const int64_t nc = h.levels[0].A.n;
+        Csr C;
+        C.n = C.m = nc;
+        C.rp.resize(nc + 1);
+        C.ci.resize(nc * nc);
+        for (int64_t i = 0; i <= nc; ++i) C.rp[i] = i * nc;
+        for (int64_t k = 0; k < nc * nc; ++k) C.ci[k] = (int32_t)(k % nc);
+        C.v = h.coarse_inv;
+        if ((rc = upload_op(s, C, lanes_per_row(C), M.cinv))) return rc;
+    } else {
+        if ((rc = upload_op(s, h.levels[0].S, lanes_per_row(h.levels[0].S), M.S0)) ||
+            (rc = upload_op(s, cyc.G, lanes_per_row(cyc.G), M.G)))
+            return rc;
+        M.yL = L >= 2 ? M.stack + cyc.stack_off[L] : M.stack;
+        if (L >= 2 && ((rc = upload_op(s, cyc.U1, lanes_per_row(cyc.U1), M.U1)) ||
+                       (rc = dalloc(s, &M.y1, h.levels[1].A.n))))
+            return rc;
+    }
     s->use_amg = true;
     return PG_OK;
 }

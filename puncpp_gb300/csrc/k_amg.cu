@@ -10,11 +10,12 @@
 // inverse) is applied in the algebraically identical form
 //     B_l b = W_l b + S_l B_{l+1} S_l^T b,   W = w D^-1 (2 I - A w D^-1),
 //     S = (I - w D^-1 A) P,
-// so each level costs two grid-wide phases (down: W b and S^T b from b; up:
-// t + S y) instead of four.  The product A z of the search direction update
-// is folded into the next matrix phase (A p = A z + beta A p_old), and r.z
-// into the last V-cycle phase: an iteration is 2 L + 3 grid barriers for L
-// levels above the coarsest.
+// with the last restriction and the coarse solve in one product
+// (G = C^-1 S^T) and the up-sweep of levels >= 1 collapsed into one product
+// (U1 = [S_1 | S_1 S_2 | ...]): L + 1 grid-wide phases for L >= 2 levels
+// above the coarsest.  The product A z of the search direction update is
+// folded into the next matrix phase (A p = A z + beta A p_old) and r.z into
+// the last V-cycle phase: an iteration is L + 3 grid barriers.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -27,13 +28,77 @@ namespace pg {
 
 namespace {
 
+// Vectors written inside the kernel are read with plain (L1-cached) loads
+// only after a grid barrier, whose acquire makes the other blocks' writes
+// visible; never through the read-only path (__ldg).
+//
 // epi(i, sum_j S_ij xv(j)) for every row i of S, spread over the whole grid.
 // SELL operators take one thread per row, two rows at a time; CSR operators g
-// lanes per row with a shuffle reduction.  The loads of four entries are
+// lanes per row, reduced by warp shuffles (g <= 32) and through shared memory
+// (g = 64..512, the warps of one block).  The loads of four entries are
 // issued before their products so that a lane keeps several gathers in
 // flight (the kernel runs at 32 warps per SM and is latency-bound otherwise).
 // Every thread of the grid must call this (the CSR path runs the same number
 // of rounds in all lanes so the shuffles are full-warp).
+// This lane's share (entries lane, lane + g, ...) of row i of a CSR operator,
+// four entries' loads issued before their products.
+template <class XV>
+__device__ __forceinline__ float csr_lane_sum(const SpOp &S, int i, int lane, int g, XV xv) {
+    const int64_t k0 = __ldg(S.ptr + i);
+    const int len = (int)(__ldg(S.ptr + i + 1) - k0);
+    const int32_t *cp = S.col + k0;
+    const float *vp = S.val + k0;
+    float s0 = 0.0f, s1 = 0.0f;
+    int k = lane;
+    for (; k + 3 * g < len; k += 4 * g) {
+        const int c0 = __ldg(cp + k), c1 = __ldg(cp + k + g);
+        const int c2 = __ldg(cp + k + 2 * g), c3 = __ldg(cp + k + 3 * g);
+        const float v0 = __ldg(vp + k), v1 = __ldg(vp + k + g);
+        const float v2 = __ldg(vp + k + 2 * g), v3 = __ldg(vp + k + 3 * g);
+        const float x0 = xv(c0), x1 = xv(c1), x2 = xv(c2), x3 = xv(c3);
+        s0 = fmaf(v0, x0, s0);
+        s1 = fmaf(v1, x1, s1);
+        s0 = fmaf(v2, x2, s0);
+        s1 = fmaf(v3, x3, s1);
+    }
+    for (; k < len; k += g) s0 = fmaf(__ldg(vp + k), xv(__ldg(cp + k)), s0);
+    return s0 + s1;
+}
+
+// Two rows' lane shares at once (row ib may be absent: ib < 0), so that a
+// lane keeps four gathers in flight across the two rows.
+template <class XV>
+__device__ __forceinline__ void csr_lane_sum2(const SpOp &S, int ia, int ib, int lane, int g, XV xv, float &ra,
+                                              float &rb) {
+    const int64_t ka = __ldg(S.ptr + ia);
+    const int la = (int)(__ldg(S.ptr + ia + 1) - ka);
+    int64_t kb = 0;
+    int lb = 0;
+    if (ib >= 0) {
+        kb = __ldg(S.ptr + ib);
+        lb = (int)(__ldg(S.ptr + ib + 1) - kb);
+    }
+    const int32_t *ca = S.col + ka, *cb = S.col + kb;
+    const float *va = S.val + ka, *vb = S.val + kb;
+    const int len = la > lb ? la : lb;
+    float sa = 0.0f, sb = 0.0f;
+    for (int k = lane; k < len; k += 2 * g) {
+        const int k1 = k + g;
+        const int c0 = k < la ? __ldg(ca + k) : -1, c1 = k1 < la ? __ldg(ca + k1) : -1;
+        const int d0 = k < lb ? __ldg(cb + k) : -1, d1 = k1 < lb ? __ldg(cb + k1) : -1;
+        const float v0 = k < la ? __ldg(va + k) : 0.0f, v1 = k1 < la ? __ldg(va + k1) : 0.0f;
+        const float w0 = k < lb ? __ldg(vb + k) : 0.0f, w1 = k1 < lb ? __ldg(vb + k1) : 0.0f;
+        const float x0 = c0 >= 0 ? xv(c0) : 0.0f, x1 = c1 >= 0 ? xv(c1) : 0.0f;
+        const float y0 = d0 >= 0 ? xv(d0) : 0.0f, y1 = d1 >= 0 ? xv(d1) : 0.0f;
+        sa = fmaf(v0, x0, sa);
+        sb = fmaf(w0, y0, sb);
+        sa = fmaf(v1, x1, sa);
+        sb = fmaf(w1, y1, sb);
+    }
+    ra = sa;
+    rb = sb;
+}
+
 template <class XV, class EPI>
 __device__ __forceinline__ void apply(const SpOp &S, XV xv, EPI epi, int t0, int ts) {
     if (S.g == 1) {
@@ -64,83 +129,89 @@ __device__ __forceinline__ void apply(const SpOp &S, XV xv, EPI epi, int t0, int
             epi(i, sa);
             if (two) epi(i2, sb);
         }
-    } else {
+    } else if (S.g <= 32) {
         const int g = S.g;
         const int lane = t0 & (g - 1);
         const int grp = t0 / g, ngrp = ts / g;
         const int rounds = (S.n + ngrp - 1) / ngrp;
+        for (int t = 0; t < rounds; t += 2) {
+            // rounds t and t + 1 together
+            const int i = grp + t * ngrp, i2 = i + ngrp;
+            float s = 0.0f, s2 = 0.0f;
+            if (i < S.n) csr_lane_sum2(S, i, i2 < S.n ? i2 : -1, lane, g, xv, s, s2);
+            for (int o = g >> 1; o > 0; o >>= 1) {
+                s += __shfl_xor_sync(0xffffffffu, s, o);
+                s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+            }
+            if (lane == 0 && i < S.n) epi(i, s);
+            if (lane == 0 && i2 < S.n) epi(i2, s2);
+        }
+    } else {
+        // g / 32 warps of one block per row; partial sums meet in shared memory
+        __shared__ float red[kPcgThreads / 32];
+        const int g = S.g;
+        const int per_block = blockDim.x / g;
+        const int lane = threadIdx.x & (g - 1);
+        const int grp = blockIdx.x * per_block + threadIdx.x / g;
+        const int ngrp = gridDim.x * per_block;
+        const int rounds = (S.n + ngrp - 1) / ngrp;
         for (int t = 0; t < rounds; ++t) {
             const int i = grp + t * ngrp;
-            float s0 = 0.0f, s1 = 0.0f;
-            if (i < S.n) {
-                const int64_t k0 = __ldg(S.ptr + i);
-                const int len = (int)(__ldg(S.ptr + i + 1) - k0);
-                const int32_t *cp = S.col + k0;
-                const float *vp = S.val + k0;
-                int k = lane;
-                for (; k + 3 * g < len; k += 4 * g) {
-                    const int c0 = __ldg(cp + k), c1 = __ldg(cp + k + g);
-                    const int c2 = __ldg(cp + k + 2 * g), c3 = __ldg(cp + k + 3 * g);
-                    const float v0 = __ldg(vp + k), v1 = __ldg(vp + k + g);
-                    const float v2 = __ldg(vp + k + 2 * g), v3 = __ldg(vp + k + 3 * g);
-                    const float x0 = xv(c0), x1 = xv(c1), x2 = xv(c2), x3 = xv(c3);
-                    s0 = fmaf(v0, x0, s0);
-                    s1 = fmaf(v1, x1, s1);
-                    s0 = fmaf(v2, x2, s0);
-                    s1 = fmaf(v3, x3, s1);
-                }
-                for (; k < len; k += g) s0 = fmaf(__ldg(vp + k), xv(__ldg(cp + k)), s0);
+            float s = i < S.n ? csr_lane_sum(S, i, lane, g, xv) : 0.0f;
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+            __syncthreads();
+            if (lane == 0 && i < S.n) {
+                float tot = 0.0f;
+                for (int w = 0; w < g / 32; ++w) tot += red[(threadIdx.x >> 5) + w];
+                epi(i, tot);
             }
-            float s = s0 + s1;
-            for (int o = g >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0 && i < S.n) epi(i, s);
+            __syncthreads();
         }
     }
 }
 
 // z = B r over the whole grid, r complete on entry; returns this thread's
-// share of r.z.  Level 0's b and y are r and z, t_l is kept in lev[l].t.
+// share of r.z.  Level 0's b is r.
 __device__ double vcycle(const AmgDev &M, const float *r, float *z, cg::grid_group &grid, int t0, int ts) {
     const int L = M.nlev - 1;
+    double rz = 0.0;
+    if (L == 0) {
+        apply(M.cinv, [=](int j) { return r[j]; },
+              [&](int i, float s) { z[i] = s; rz = fma((double)s, (double)r[i], rz); }, t0, ts);
+        return rz;
+    }
     for (int l = 0; l < L; ++l) {
         const float *b = l == 0 ? r : M.lev[l].b;
         const float om = M.lev[l].omega;
         const float *dinv = M.lev[l].dinv;
         float *t = M.lev[l].t;
-        apply(M.lev[l].A, [=](int j) { return om * __ldg(dinv + j) * __ldcg(b + j); },
-              [=](int i, float s) { t[i] = om * __ldg(dinv + i) * (2.0f * __ldcg(b + i) - s); }, t0, ts);
-        float *bn = M.lev[l + 1].b;
-        apply(M.lev[l].ST, [=](int j) { return __ldcg(b + j); }, [=](int i, float s) { bn[i] = s; }, t0, ts);
+        apply(M.lev[l].A, [=](int j) { return om * __ldg(dinv + j) * b[j]; },
+              [=](int i, float s) { t[i] = om * __ldg(dinv + i) * (2.0f * b[i] - s); }, t0, ts);
+        if (l < L - 1) {
+            float *bn = M.lev[l + 1].b;
+            apply(M.lev[l].ST, [=](int j) { return b[j]; }, [=](int i, float s) { bn[i] = s; }, t0, ts);
+        } else {
+            float *yL = M.yL;
+            apply(M.G, [=](int j) { return b[j]; }, [=](int i, float s) { yL[i] = s; }, t0, ts);
+        }
         grid.sync();
     }
-    double rz = 0.0;
-    {
-        const float *bc = L == 0 ? r : M.lev[L].b;
-        float *yc = L == 0 ? z : M.lev[L].y;
-        if (L == 0)
-            apply(M.cinv, [=](int j) { return __ldcg(bc + j); },
-                  [&](int i, float s) { yc[i] = s; rz = fma((double)s, (double)__ldcg(r + i), rz); }, t0, ts);
-        else
-            apply(M.cinv, [=](int j) { return __ldcg(bc + j); }, [=](int i, float s) { yc[i] = s; }, t0, ts);
-        if (L > 0) grid.sync();
+    const float *yup = M.yL;
+    if (L >= 2) {
+        const float *t1 = M.lev[1].t, *st = M.stack;
+        float *y1 = M.y1;
+        apply(M.U1, [=](int j) { return st[j]; }, [=](int i, float s) { y1[i] = t1[i] + s; }, t0, ts);
+        grid.sync();
+        yup = M.y1;
     }
-    for (int l = L - 1; l >= 0; --l) {
-        const float *yn = M.lev[l + 1].y;
-        const float *t = M.lev[l].t;
-        if (l > 0) {
-            float *y = M.lev[l].y;
-            apply(M.lev[l].S, [=](int j) { return __ldcg(yn + j); }, [=](int i, float s) { y[i] = __ldcg(t + i) + s; },
-                  t0, ts);
-            grid.sync();
-        } else {
-            apply(M.lev[0].S, [=](int j) { return __ldcg(yn + j); },
-                  [&](int i, float s) {
-                      const float zi = __ldcg(t + i) + s;
-                      z[i] = zi;
-                      rz = fma((double)zi, (double)__ldcg(r + i), rz);
-                  }, t0, ts);
-        }
-    }
+    const float *tz = M.lev[0].t;
+    apply(M.S0, [=](int j) { return yup[j]; },
+          [&](int i, float s) {
+              const float zi = tz[i] + s;
+              z[i] = zi;
+              rz = fma((double)zi, (double)r[i], rz);
+          }, t0, ts);
     return rz;
 }
 
@@ -180,8 +251,14 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M)
         grid_sum2(partA, nullptr, nb, sh, ra, rb);
         __syncthreads();
     };
-    double t_rz = 0.0, t_tol2 = 0.0, t_rr = 0.0, t_bb = 0.0, t_rmax = 0.0;
-    int t_it = 0, t_status = 1, t_updates = 0;
+    // solver scalars, kept by thread 0 in shared memory (no registers held
+    // across the loop by the other threads)
+    __shared__ double t_rz, t_tol2, t_rr, t_bb, t_rmax;
+    __shared__ int t_it, t_status, t_updates;
+    if (threadIdx.x == 0) {
+        t_rz = t_tol2 = t_rr = t_bb = t_rmax = 0.0;
+        t_it = 0; t_status = 1; t_updates = 0;
+    }
     for (int pass = 0;; ++pass) {
         // true residual in FP64 into the FP32 recurrence
         double rr = 0.0, bb = 0.0;
@@ -233,11 +310,11 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M)
             {
                 const float *z = a.z32;
                 float *p = a.p32, *Ap = a.Ap32;
-                apply(A0, [=](int j) { return __ldcg(z + j); },
+                apply(A0, [=](int j) { return z[j]; },
                       [&](int i, float s) {
-                          const float zi = __ldcg(z + i);
-                          const float pi = first ? zi : fmaf(beta, __ldcg(p + i), zi);
-                          const float api = first ? s : fmaf(beta, __ldcg(Ap + i), s);
+                          const float zi = z[i];
+                          const float pi = first ? zi : fmaf(beta, p[i], zi);
+                          const float api = first ? s : fmaf(beta, Ap[i], s);
                           p[i] = pi;
                           Ap[i] = api;
                           pap32 = fmaf(pi, api, pap32);
@@ -264,9 +341,9 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M)
                 const int i2 = i + gstride;
                 const bool two = i2 < n;
                 const double x1 = a.x[i];
-                const float p1 = __ldcg(a.p32 + i), q1 = __ldcg(a.Ap32 + i), r1 = a.r32[i];
+                const float p1 = a.p32[i], q1 = a.Ap32[i], r1 = a.r32[i];
                 const double x2 = two ? a.x[i2] : 0.0;
-                const float p2 = two ? __ldcg(a.p32 + i2) : 0.0f, q2 = two ? __ldcg(a.Ap32 + i2) : 0.0f;
+                const float p2 = two ? a.p32[i2] : 0.0f, q2 = two ? a.Ap32[i2] : 0.0f;
                 const float r2 = two ? a.r32[i2] : 0.0f;
                 const float n1 = fmaf(-alpha32, q1, r1), n2 = fmaf(-alpha32, q2, r2);
                 a.x[i] = fma(alpha, (double)p1, x1);
@@ -284,7 +361,7 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M)
             grid_sum2(partC, nullptr, nb, sh, ra, rb);
             if (threadIdx.x == 0) {
                 const double rr_rec = ra;
-                scal[2] = (rr_rec <= 1e-4 * t_rmax || rr_rec <= t_tol2 || t_it >= a.max_iter) ? 1.0 : 0.0;
+                scal[2] = (rr_rec <= 1e-6 * t_rmax || rr_rec <= t_tol2 || t_it >= a.max_iter) ? 1.0 : 0.0;
             }
             __syncthreads();
             if (scal[2] != 0.0) break;   // replace the residual (next pass)

@@ -34,6 +34,21 @@ struct AmgHierarchy {
     std::vector<double> coarse_inv;  // dense inverse of the coarsest operator
 };
 
+// Operators of the device cycle, for L = levels - 1 >= 1 levels above the
+// coarsest: G = C^-1 S_{L-1}^T (n_L x n_{L-1}, the last restriction and the
+// coarse solve in one product) and, when L >= 2, the collapsed up-sweep of
+// levels 1..L-1,
+//     y_1 = t_1 + U1 [t_2; ...; t_{L-1}; y_L],
+//     U1 = [S_1 | S_1 S_2 | ... | S_1 ... S_{L-1}],
+// acting on the stacked vector whose level-l block starts at stack_off[l]
+// (l = 2..L; for L = 1, y_1 = G b_0 is the whole stack).
+struct AmgCycle {
+    Csr G, U1;
+    std::vector<int64_t> stack_off;  // [L + 1], entries 0, 1 unused
+    int64_t stack_len = 0;
+};
+void amg_cycle_operators(const AmgHierarchy &h, AmgCycle &c);
+
 // Returns 0; 8 when the coarsest operator is singular; 9 when coarsening
 // stalls above AmgParams::dense_max rows.  With
 // `constant_nullspace` (periodic meshes: A 1 = 0) the coarsest inverse is

@@ -152,7 +152,8 @@ struct PcgArgs {
 
 // AMG hierarchy on the device: FP32 sparse operators, each either SELL-32
 // (one thread per row, g == 1) or CSR processed by g lanes per row (g a power
-// of two up to 32) for operators with long rows.
+// of two: up to 32 within a warp, 64..512 across the warps of one block) for
+// operators with long rows.
 struct SpOp {
     int32_t n = 0;                       // rows
     int32_t g = 1;                       // lanes per row
@@ -165,17 +166,25 @@ struct SpOp {
 constexpr int kAmgMaxLevels = 12;
 
 struct AmgLevelDev {
-    SpOp A;                              // level operator
-    SpOp S, ST;                          // S = (I - omega D^-1 A) P: n x n_next, and S^T
+    SpOp A;                              // level operator (level 0: the solver's FP32 matrix)
+    SpOp ST;                             // S^T to the next level, S = (I - omega D^-1 A) P (not on the last two)
     const float *dinv = nullptr;
     float omega = 0.f;
-    float *b = nullptr, *t = nullptr, *y = nullptr;   // right-hand side, W b, V-cycle result
+    float *b = nullptr;                  // right-hand side (levels >= 1)
+    float *t = nullptr;                  // W b
 };
 
+// The cycle for L = nlev - 1 levels above the coarsest: down-sweep phases
+// t_l = W_l b_l with b_{l+1} = S_l^T b_l, the last one y_L = G b_{L-1}
+// (G = C^-1 S_{L-1}^T); then y_1 = t_1 + U1 [t_2 .. t_{L-1}, y_L] (L >= 2)
+// and z = t_0 + S_0 y_1.  L == 0: z = C^-1 r.
 struct AmgDev {
     int32_t nlev = 0;
     AmgLevelDev lev[kAmgMaxLevels];
-    SpOp cinv;                           // dense inverse of the coarsest operator (CSR, 32 lanes per row)
+    SpOp S0, G, U1, cinv;
+    float *stack = nullptr;              // [t_2 .. t_{L-1}, y_L] (L >= 2) or y_1 (L == 1)
+    float *yL = nullptr;                 // y_L inside the stack
+    float *y1 = nullptr;                 // level-1 result (L >= 2)
 };
 
 // ---- launch wrappers (all on `stream`) -----------------------------------

@@ -57,4 +57,31 @@ void amgd_coarse_inv(void *p, double *out) {
 }
 
 void amgd_free(void *p) { delete static_cast<AmgHierarchy *>(p); }
+
+// the device cycle's operators: which 0 = G, 1 = U1
+void *amgd_cycle(void *p) {
+    auto *c = new pg::AmgCycle;
+    pg::amg_cycle_operators(*static_cast<AmgHierarchy *>(p), *c);
+    return c;
+}
+void amgd_cycle_shape(void *p, int which, int64_t out[3]) {
+    const auto *c = static_cast<pg::AmgCycle *>(p);
+    const Csr &M = which == 0 ? c->G : c->U1;
+    out[0] = M.n;
+    out[1] = M.m;
+    out[2] = (int64_t)M.ci.size();
+}
+void amgd_cycle_copy(void *p, int which, int64_t *rp, int32_t *ci, double *v) {
+    const auto *c = static_cast<pg::AmgCycle *>(p);
+    const Csr &M = which == 0 ? c->G : c->U1;
+    std::memcpy(rp, M.rp.data(), sizeof(int64_t) * M.rp.size());
+    std::memcpy(ci, M.ci.data(), sizeof(int32_t) * M.ci.size());
+    std::memcpy(v, M.v.data(), sizeof(double) * M.v.size());
+}
+int amgd_cycle_offsets(void *p, int64_t *out) {
+    const auto *c = static_cast<pg::AmgCycle *>(p);
+    std::memcpy(out, c->stack_off.data(), sizeof(int64_t) * c->stack_off.size());
+    return (int)c->stack_off.size();
+}
+void amgd_cycle_free(void *p) { delete static_cast<pg::AmgCycle *>(p); }
 }

@@ -38,10 +38,31 @@ def amgd(tmp_path_factory):
     d.amgd_omega.restype = C.c_double
     d.amgd_coarse_inv.argtypes = [C.c_void_p, C.c_void_p]
     d.amgd_free.argtypes = [C.c_void_p]
+    d.amgd_cycle.restype = C.c_void_p
+    d.amgd_cycle.argtypes = [C.c_void_p]
+    d.amgd_cycle_shape.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    d.amgd_cycle_copy.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    d.amgd_cycle_offsets.argtypes = [C.c_void_p, C.c_void_p]
+    d.amgd_cycle_free.argtypes = [C.c_void_p]
     return d
 
 
-def hierarchy(d, A, nullspace=False, theta=-1.0, theta_factor=0.0, coarse_max=0):
+def _csr_out(shape_fn, copy_fn):
+    shape = np.zeros(3, np.int64)
+    shape_fn(shape.ctypes.data)
+    n, m, nnz = (int(x) for x in shape)
+    if n == 0:
+        return None
+    orp = np.zeros(n + 1, np.int64)
+    oci = np.zeros(max(nnz, 1), np.int32)
+    ov = np.zeros(max(nnz, 1))
+    copy_fn(orp.ctypes.data, oci.ctypes.data, ov.ctypes.data)
+    return sp.csr_matrix((ov[:nnz], oci[:nnz], orp), shape=(n, m))
+
+
+def hierarchy(d, A, nullspace=False, theta=-1.0, theta_factor=0.0, coarse_max=0, cycle=None):
+    """Levels and coarsest inverse; fills `cycle` (a dict) with the device
+    cycle's operators G, U1 and the stack offsets when given."""
     A = sp.csr_matrix(A)
     A.sort_indices()
     rp = A.indptr.astype(np.int64)
@@ -56,21 +77,24 @@ def hierarchy(d, A, nullspace=False, theta=-1.0, theta_factor=0.0, coarse_max=0)
         for l in range(d.amgd_levels(h)):
             ops = {}
             for which, name in enumerate(["A", "P", "R", "S", "ST"]):
-                shape = np.zeros(3, np.int64)
-                d.amgd_shape(h, l, which, shape.ctypes.data)
-                n, m, nnz = (int(x) for x in shape)
-                if n == 0:
-                    continue
-                orp = np.zeros(n + 1, np.int64)
-                oci = np.zeros(max(nnz, 1), np.int32)
-                ov = np.zeros(max(nnz, 1))
-                d.amgd_copy(h, l, which, orp.ctypes.data, oci.ctypes.data, ov.ctypes.data)
-                ops[name] = sp.csr_matrix((ov[:nnz], oci[:nnz], orp), shape=(n, m))
+                M = _csr_out(lambda o: d.amgd_shape(h, l, which, o), lambda a, b, c: d.amgd_copy(h, l, which, a, b, c))
+                if M is not None:
+                    ops[name] = M
             ops["omega"] = d.amgd_omega(h, l)
             levels.append(ops)
         nc = levels[-1]["A"].shape[0]
         cinv = np.zeros(nc * nc)
         d.amgd_coarse_inv(h, cinv.ctypes.data)
+        if cycle is not None:
+            c = d.amgd_cycle(h)
+            try:
+                for which, name in enumerate(["G", "U1"]):
+                    cycle[name] = _csr_out(lambda o: d.amgd_cycle_shape(c, which, o),
+                                           lambda a, b, cc: d.amgd_cycle_copy(c, which, a, b, cc))
+                off = np.zeros(len(levels) + 1, np.int64)
+                cycle["off"] = off[:d.amgd_cycle_offsets(c, off.ctypes.data)]
+            finally:
+                d.amgd_cycle_free(c)
         return levels, cinv.reshape(nc, nc)
     finally:
         d.amgd_free(h)
@@ -110,6 +134,28 @@ def vcycle(levels, cinv, b, l=0):
     m = L["omega"] / L["A"].diagonal()
     t = m * (2.0 * b - L["A"] @ (m * b))
     return t + L["S"] @ vcycle(levels, cinv, L["ST"] @ b, l + 1)
+
+
+def vcycle_collapsed(levels, cinv, cyc, b):
+    """The cycle as the device kernel runs it: one down-sweep phase per level
+    (t_l = W_l b_l and the restriction; the last one G b = C^-1 S^T b), the
+    up-sweep of levels >= 1 in one product with U1, then level 0."""
+    L = len(levels) - 1
+    if L == 0:
+        return cinv @ b
+    t, bl = [], b
+    for l in range(L):
+        m = levels[l]["omega"] / levels[l]["A"].diagonal()
+        t.append(m * (2.0 * bl - levels[l]["A"] @ (m * bl)))
+        if l < L - 1:
+            bl = levels[l]["ST"] @ bl
+        else:
+            yL = cyc["G"] @ bl
+    if L >= 2:
+        y1 = t[1] + cyc["U1"] @ np.concatenate(t[2:L] + [yL])
+    else:
+        y1 = yL
+    return t[0] + levels[0]["S"] @ y1
 
 
 def pcg(A, b, prec, rtol):
@@ -166,6 +212,33 @@ def test_transfer_operators_give_the_textbook_vcycle(amgd, probe):
         assert abs(L["ST"] - L["S"].T).max() == 0.0
     b = np.random.default_rng(7).standard_normal(A.shape[0])
     np.testing.assert_allclose(vcycle(levels, cinv, b), vcycle_textbook(levels, cinv, b), rtol=0, atol=1e-10)
+
+
+@pytest.fixture(scope="module")
+def probe22(oracle_mod):
+    ma = meshgen.probe_box(22, 4.0, 0.8)
+    return ma, reduced_operator(oracle_mod, ma)
+
+
+@pytest.mark.parametrize("coarse_max,depth", [(3000, 1), (400, 2), (10, 3)])
+def test_collapsed_cycle_equals_the_vcycle(coarse_max, depth, amgd, probe22):
+    """G = C^-1 S^T and U1 = [S_1 | S_1 S_2 | ...] reproduce the V-cycle for
+    hierarchies with 1, 2 and 3 levels above the coarsest."""
+    ma, A = probe22
+    cyc = {}
+    levels, cinv = hierarchy(amgd, A, coarse_max=coarse_max, cycle=cyc)
+    L = len(levels) - 1
+    assert L == depth
+    G = cyc["G"]
+    assert G.shape == (levels[L]["A"].shape[0], levels[L - 1]["A"].shape[0])
+    np.testing.assert_allclose(G.toarray(), cinv @ levels[L - 1]["ST"].toarray(), atol=1e-12 * abs(cinv).max())
+    if L >= 2:
+        assert cyc["U1"].shape == (levels[1]["A"].shape[0], sum(levels[l]["A"].shape[0] for l in range(2, L + 1)))
+    else:
+        assert cyc["U1"] is None
+    b = np.random.default_rng(8).standard_normal(A.shape[0])
+    ref = vcycle_textbook(levels, cinv, b)
+    np.testing.assert_allclose(vcycle_collapsed(levels, cinv, cyc, b), ref, rtol=0, atol=1e-10 * abs(ref).max())
 
 
 def test_vcycle_preconditioner_beats_jacobi(amgd, probe):
