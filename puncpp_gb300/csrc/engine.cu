@@ -76,6 +76,7 @@ struct pg_sim {
     pg_species inj[kMaxSpecies]{};
     double *flux_num = nullptr, *pdf_max = nullptr;
     std::vector<double> flux_num_h;
+    std::vector<double> flux_sum_h;            // per injected species: sum over facets of flux_num
     int64_t *inj_counts = nullptr, *inj_offsets = nullptr, *scan_tmp = nullptr;
     int64_t scan_tmp_n = 0;
 
@@ -725,7 +726,8 @@ static int inject_internal(pg_sim *s, double dt, uint64_t seed, uint64_t step, b
         I.vth2 = S.vth * S.vth;
         I.factor = 1.0 / std::pow(std::sqrt(2. * M_PI * I.vth2), 3);
         I.q = S.q;
-        for (int j = 0; j < s->n_ext; ++j) bound += (int64_t)(s->flux_num_h[(size_t)k * s->n_ext + j] * I.ndt) + 1;
+        // sum_j (floor(f_j n dt) + 1) <= n dt sum_j f_j + n_facets
+        bound += (int64_t)std::ceil(s->flux_sum_h[k] * I.ndt) + s->n_ext;
     }
     int rc = ensure_capacity(s, s->n_slots + bound);
     if (rc) return rc;
@@ -1485,6 +1487,9 @@ int pg_create_flux(pg_sim *s, const pg_species *sp, int32_t n) {
         PG_CUDA(cudaMemcpy(s->pdf_max, pmax.data(), sizeof(double) * pmax.size(), cudaMemcpyHostToDevice));
     }
     s->flux_num_h = num;
+    s->flux_sum_h.assign(nmax, 0.0);
+    for (int k = 0; k < nmax; ++k)
+        for (int64_t j = 0; j < nf; ++j) s->flux_sum_h[k] += num[(size_t)k * nf + j];
     s->n_inj_species = nmax;
     for (int k = 0; k < nmax; ++k) s->inj[k] = tab[k];
     s->flux_ready = true;

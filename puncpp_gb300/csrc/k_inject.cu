@@ -18,13 +18,16 @@
 // one particle at once and keeps the lowest accepted index, which is exactly
 // the sequential loop's choice.  The particle is kept if the facet walk from
 // the facet's cell stays in the mesh.  Built with --fmad=false; exp is the
-// portable series, so accept/reject decisions equal a CPU evaluation.
+// portable series, so accept/reject decisions equal a CPU evaluation.  Each
+// candidate is first decided in FP32 with an error bound (pg_screen.h); the
+// FP64 test runs only when the FP32 margin is inside the bound.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 
 #include "pg_device.cuh"
 #include "pg_math.h"
+#include "pg_screen.h"
 #include "pg_walk.cuh"
 
 namespace pg {
@@ -79,32 +82,38 @@ __global__ void k_inject_generate(DevMesh m, DevParticles p, InjectParams ip, co
         const double nx = F[10], ny = F[11], nz = F[12];
         const uint32_t c1 = (uint32_t)j, c2 = (uint32_t)(s + 8 * (k + 1)), c3 = ip.step;
         const double pmax = pdf_max[idx];
-        // rejection sampling, 32 candidates per round
+        // rejection sampling, 32 candidates per round; each candidate is
+        // screened in FP32 and only undecided ones take the FP64 test
+        FluxBox B;
+        for (int c = 0; c < 3; ++c) { B.lo[c] = S.domain_lo[c]; B.w[c] = S.domain_w[c]; B.vd[c] = S.vd[c]; }
+        B.vth2 = S.vth2;
+        B.factor = S.factor;
+        const FluxBox32 B32 = flux_box32(B);
+        const float nx32 = (float)nx, ny32 = (float)ny, nz32 = (float)nz, pmax32 = (float)pmax;
+        const uint32_t k0 = uint32_t(ip.seed), k1 = uint32_t(ip.seed >> 32);
         double vx = 0, vy = 0, vz = 0;
         int found = -1;
         for (int round = 0; round < kMaxRounds && found < 0; ++round) {
             const uint32_t cand = (uint32_t)round * 32u + (uint32_t)lane;
-            double a, b, c, u;
-            uniforms2(ip.seed, 2u + 2u * cand, c1, c2, c3, a, b);
-            uniforms2(ip.seed, 3u + 2u * cand, c1, c2, c3, c, u);
-            const double tx = S.domain_lo[0] + S.domain_w[0] * a;
-            const double ty = S.domain_lo[1] + S.domain_w[1] * b;
-            const double tz = S.domain_lo[2] + S.domain_w[2] * c;
-            double vn = 0.0;
-            vn += tx * nx; vn += ty * ny; vn += tz * nz;
-            double vs = 0.0;
-            vs += (tx - S.vd[0]) * (tx - S.vd[0]);
-            vs += (ty - S.vd[1]) * (ty - S.vd[1]);
-            vs += (tz - S.vd[2]) * (tz - S.vd[2]);
-            const double f = S.factor * exp_portable(-0.5 * vs / S.vth2);
-            const double pdf = (double)(vn > 0.0) * vn * f;
-            const unsigned acc = __ballot_sync(0xffffffffu, u * pmax < pdf);
+            const Philox4 ra = philox4x32_10(2u + 2u * cand, c1, c2, c3, k0, k1);
+            const Philox4 rb = philox4x32_10(3u + 2u * cand, c1, c2, c3, k0, k1);
+            int dec = flux_screen_fp32(B32, nx32, ny32, nz32, pmax32, ra.v[0], ra.v[2], rb.v[0], rb.v[2]);
+            double t[3];
+            if (dec < 0)
+                dec = flux_accept_fp64(B, nx, ny, nz, pmax, u01_from(ra.v[0], ra.v[1]), u01_from(ra.v[2], ra.v[3]),
+                                       u01_from(rb.v[0], rb.v[1]), u01_from(rb.v[2], rb.v[3]), t) ? 1 : 0;
+            const unsigned acc = __ballot_sync(0xffffffffu, dec == 1);
             if (acc) {
                 const int first = __ffs(acc) - 1;
                 found = first;
-                vx = __shfl_sync(0xffffffffu, tx, first);
-                vy = __shfl_sync(0xffffffffu, ty, first);
-                vz = __shfl_sync(0xffffffffu, tz, first);
+                if (lane == first) {
+                    t[0] = B.lo[0] + B.w[0] * u01_from(ra.v[0], ra.v[1]);
+                    t[1] = B.lo[1] + B.w[1] * u01_from(ra.v[2], ra.v[3]);
+                    t[2] = B.lo[2] + B.w[2] * u01_from(rb.v[0], rb.v[1]);
+                }
+                vx = __shfl_sync(0xffffffffu, t[0], first);
+                vy = __shfl_sync(0xffffffffu, t[1], first);
+                vz = __shfl_sync(0xffffffffu, t[2], first);
             }
         }
         if (lane != 0) continue;
