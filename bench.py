@@ -257,23 +257,24 @@ def run_ours(args):
 
 
 def amg_iteration_bytes(lay):
-    """Algorithmic bytes of one AMG-preconditioned PCG iteration, every operator
-    read once per use (FP32 value + int32 column = 8 B an entry):
-    level 0: the PCG product plus two smoother products of A, restriction and
-    prolongation, and 104 B of FP32/FP64 vector traffic per row; coarser
-    levels: two products of A, R and P, 52 B per row; the dense coarsest
-    inverse once."""
+    """Algorithmic bytes of one AMG-preconditioned PCG iteration, each operator
+    read once per use (FP32 value + int32 column = 8 B an entry), vectors in
+    FP32 except the FP64 solution:
+      level 0: A twice (PCG product, smoother), S and S^T once, 88 B per row
+               (p, Ap, z, r, t, x, D^-1 streams of the five phases);
+      levels 1..L-1: A and S^T once, 16 B per row;
+      G (last restriction + coarse solve) and the collapsed up-sweep U1 once,
+      8 B per level-1 row."""
     lv = lay["levels"]
-    b = 0
-    for l, v in enumerate(lv):
-        if l == len(lv) - 1:
-            b += v["rows"] * v["rows"] * 8 + v["rows"] * 8
-        elif l == 0:
-            b += 3 * v["nnz"] * 8 + 2 * v["nnz_p"] * 8 + 104 * v["rows"]
-        else:
-            b += 2 * v["nnz"] * 8 + 2 * v["nnz_p"] * 8 + 52 * v["rows"]
-    return b, ("per iteration: level 0 3*nnz*8 + 2*nnzP*8 + 104*rows; levels 1.. 2*nnz*8 + 2*nnzP*8 + 52*rows; "
-               "coarsest rows^2*8 (operators re-read from L2 count each time)")
+    if not lv:
+        return 0, "no AMG levels"
+    L = len(lv) - 1
+    b = 2 * lv[0]["nnz"] * 8 + 2 * lv[0]["nnz_p"] * 8 + 88 * lv[0]["rows"]
+    for l in range(1, L):
+        b += lv[l]["nnz"] * 8 + lv[l]["nnz_p"] * 8 + 16 * lv[l]["rows"]
+    b += (lay["cycle_nnz_g"] + lay["cycle_nnz_u1"]) * 8 + (8 * lv[1]["rows"] if L >= 2 else 0)
+    return b, ("per iteration: level 0 2*nnz(A)*8 + 2*nnz(S)*8 + 88*rows; levels 1..L-1 (nnz(A)+nnz(S^T))*8 + "
+               "16*rows; (nnz(G)+nnz(U1))*8 + 8*rows(1); operators re-read from L2 count each time")
 
 
 def ctypes_ms(lib, pop, a, b):

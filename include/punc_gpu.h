@@ -277,6 +277,8 @@ typedef struct pg_poisson_layout {
     int64_t level_nnz[PG_MAX_AMG_LEVELS];    /* operator nonzeros per level */
     int64_t level_nnz_p[PG_MAX_AMG_LEVELS];  /* nonzeros of the transfer operator S = (I - w D^-1 A) P
                                                 to the next level (0 on the coarsest level) */
+    int64_t cycle_nnz_g;                     /* entries of G = C^-1 S^T (last restriction + coarse solve) */
+    int64_t cycle_nnz_u1;                    /* entries of the collapsed up-sweep operator of levels >= 1 */
 } pg_poisson_layout;
 int pg_poisson_layout_get(pg_sim *sim, pg_poisson_layout *out);
 

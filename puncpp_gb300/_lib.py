@@ -88,7 +88,8 @@ class PoissonLayout(C.Structure):
     _fields_ = [("n_rows", C.c_int64), ("nnz", C.c_int64), ("sell_entries", C.c_int64),
                 ("precond", C.c_int32), ("levels", C.c_int32),
                 ("level_rows", C.c_int64 * MAX_AMG_LEVELS), ("level_nnz", C.c_int64 * MAX_AMG_LEVELS),
-                ("level_nnz_p", C.c_int64 * MAX_AMG_LEVELS)]
+                ("level_nnz_p", C.c_int64 * MAX_AMG_LEVELS), ("cycle_nnz_g", C.c_int64),
+                ("cycle_nnz_u1", C.c_int64)]
 
 
 # Every entry point of include/punc_gpu.h with its argument types.

@@ -59,6 +59,7 @@ struct pg_sim {
     AmgDev amg{};
     std::vector<int64_t> amg_rows, amg_nnz, amg_nnz_p;   // per level (pg_poisson_layout_get)
     int64_t a_nnz = 0, a_sell = 0;                       // stored nonzeros and SELL-32 entries of A
+    int64_t amg_nnz_g = 0, amg_nnz_u1 = 0;               // cycle operators G and U1
     bool phi_valid = false;
 
     // circuit (capacitance-matrix method)
@@ -400,6 +401,8 @@ static int setup_amg(pg_sim *s, const std::vector<int32_t> &arow, const std::vec
     if ((int)h.levels.size() > kAmgMaxLevels) return fail(PG_ERR_ARG, "AMG: too many levels");
     AmgCycle cyc;
     amg_cycle_operators(h, cyc);
+    s->amg_nnz_g = (int64_t)cyc.G.ci.size();
+    s->amg_nnz_u1 = (int64_t)cyc.U1.ci.size();
     AmgDev &M = s->amg;
     M = AmgDev{};
     M.nlev = (int32_t)h.levels.size();
@@ -1626,6 +1629,8 @@ int pg_poisson_layout_get(pg_sim *s, pg_poisson_layout *out) {
         out->level_nnz[l] = s->amg_nnz[l];
         out->level_nnz_p[l] = s->amg_nnz_p[l];
     }
+    out->cycle_nnz_g = s->use_amg ? s->amg_nnz_g : 0;
+    out->cycle_nnz_u1 = s->use_amg ? s->amg_nnz_u1 : 0;
     return PG_OK;
 }
 

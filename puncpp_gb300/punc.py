@@ -355,7 +355,8 @@ def poisson_layout(pop: Population) -> dict:
     n = out.levels
     return {"n_rows": out.n_rows, "nnz": out.nnz, "sell_entries": out.sell_entries, "precond": out.precond,
             "levels": [{"rows": out.level_rows[l], "nnz": out.level_nnz[l], "nnz_p": out.level_nnz_p[l]}
-                       for l in range(n)]}
+                       for l in range(n)],
+            "cycle_nnz_g": out.cycle_nnz_g, "cycle_nnz_u1": out.cycle_nnz_u1}
 
 
 def set_profiling(pop: Population, on: bool):
