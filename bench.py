@@ -149,7 +149,8 @@ def run_ours(args):
 
     def one(first=False):
         nonlocal step_no, n_now
-        r = punc.step(pop, objs, DT, first_step=first, inject=True, seed=0x5EED0002, step_no=step_no)
+        r = punc.step(pop, objs, DT, first_step=first, inject=True, seed=0x5EED0002, step_no=step_no,
+                      efield_cg1=args.efield == "cg1")
         step_no += 1
         pushed = n_now
         n_now = r.n_particles
@@ -245,7 +246,7 @@ def run_ours(args):
         "precision_form": args.precision,
         "data": "synthetic: seeded uniform/Maxwellian particles on a generated Kuhn probe mesh (no dataset)",
         "config": {"workload": workload_name(args.n_side, args.n_per), "precision": args.precision,
-                   "pcg_precond": args.pcg_precond, "cells": nc, "dofs": nv, "nnz": nnz,
+                   "pcg_precond": args.pcg_precond, "efield": args.efield, "cells": nc, "dofs": nv, "nnz": nnz,
                    "amg_levels": [[v["rows"], v["nnz"]] for v in lay["levels"]], "particles_initial": n0,
                    "particles_mean_pushed": round(n_avg), "pcg_iterations_per_step": round(iters / args.steps, 1),
                    "l2": "inputs larger than L2 (particle SoA ~250 MB, mesh tables ~0.9 GB)"},
@@ -394,6 +395,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="probe-80", help="probe-N: N^3 sub-cubes, particles scaled by (N/80)^3")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--efield", default="dg0", choices=["dg0", "cg1"],
+                    help="field path: EFieldDG0 + accel/boris, or ESolver (CG1) + accel_cg1/boris_cg1")
     ap.add_argument("--pcg-precond", default="amg", choices=sorted(PRECONDS),
                     help="Poisson preconditioner: one AMG V-cycle or Jacobi per iteration")
     args = ap.parse_args()

@@ -145,7 +145,10 @@ typedef struct pg_step_args {
     int32_t inject;          /* 1: flux injection after update */
     uint64_t seed;           /* injection RNG key */
     uint64_t step;           /* injection RNG counter (time step number) */
-    double E0[3];            /* uniform external field added to the cell field */
+    double E0[3];            /* uniform external field added to the cell (or vertex) field */
+    int32_t efield_cg1;      /* 1: CG1 field by ESolver and accel_cg1 / boris_cg1, the reference
+                                time loop's default (interaction/interaction.cpp:361-389);
+                                0: DG0 field (EFieldDG0) and accel / boris */
 } pg_step_args;
 
 typedef struct pg_step_result {
@@ -260,6 +263,20 @@ int pg_event_record(pg_sim *sim, int32_t slot);
 int pg_event_elapsed(pg_sim *sim, int32_t from_slot, int32_t to_slot, double *ms);
 /* Wait until all work queued on the engine stream has finished. */
 int pg_synchronize(pg_sim *sim);
+/* ESolver::solve (punc/src/efield.cpp:70-75, punc/ufl/EField3D.ufl): the CG1
+ * field E = L2 projection of -grad(phi) (phi: the current potential), solved
+ * by CG on the consistent mass matrix for the three components; FP64 form to
+ * rel 1e-12 / abs 1e-14 (the ESolver's tolerances, efield.cpp:62-64), mixed
+ * form in FP32 to rel 1e-6.  E (optional): [Ndof][3] on return. */
+int pg_esolver_solve(pg_sim *sim, double *E, pg_solve_info *info);
+int pg_set_efield_cg1(pg_sim *sim, const double *E);   /* [Ndof][3] */
+int pg_get_efield_cg1(pg_sim *sim, double *E);         /* [Ndof][3] */
+/* accel_cg1 / boris_cg1 (punc/include/punc/pusher.h:154-201, 282-372): the
+ * push with the CG1 field interpolated at each particle; returns KE as
+ * pg_accel / pg_boris. */
+int pg_accel_cg1(pg_sim *sim, double dt, double *KE);
+int pg_boris_cg1(pg_sim *sim, const double B[3], double dt, double *KE);
+
 /* Number of kernels this library has launched in this process. */
 int pg_launch_count(int64_t *n);
 

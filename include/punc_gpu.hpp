@@ -143,14 +143,15 @@ private:
     }
 };
 
-// A field of the engine: E (DG0 vector), rho or phi (CG1).
+// A field of the engine: E (DG0 vector), ECG1 (CG1 vector), rho or phi (CG1).
 class Function {
 public:
-    enum Kind { E, Rho, Phi };
+    enum Kind { E, ECG1, Rho, Phi };
     Function(Population<3> &pop, Kind k) : pop_(pop), kind_(k) {}
     std::vector<double> vector(std::size_t n) const {
         std::vector<double> out(n);
         if (kind_ == E) check(pg_get_efield(pop_.handle, out.data()));
+        else if (kind_ == ECG1) check(pg_get_efield_cg1(pop_.handle, out.data()));
         else if (kind_ == Rho) check(pg_get_rho(pop_.handle, out.data()));
         else check(pg_get_phi(pop_.handle, out.data()));
         return out;
@@ -173,6 +174,17 @@ inline double boris(Population<3> &pop, const Function &, const std::vector<doub
     check(pg_boris(pop.handle, B.data(), dt, &ke));
     return ke;
 }
+// pusher.h:154-201, 282-372
+inline double accel_cg1(Population<3> &pop, const Function &, double dt) {
+    double ke = 0;
+    check(pg_accel_cg1(pop.handle, dt, &ke));
+    return ke;
+}
+inline double boris_cg1(Population<3> &pop, const Function &, const std::vector<double> &B, double dt) {
+    double ke = 0;
+    check(pg_boris_cg1(pop.handle, B.data(), dt, &ke));
+    return ke;
+}
 inline void move(Population<3> &pop, double dt) { check(pg_move(pop.handle, dt)); }
 inline void move_periodic(Population<3> &pop, double dt, const std::vector<double> &Ld) {
     check(pg_move_periodic(pop.handle, dt, Ld.data()));
@@ -190,6 +202,11 @@ inline double kinetic_energy(Population<3> &pop) {
 // EFieldDG0 (punc/src/efield.cpp:77-99)
 struct EFieldDG0 {
     void solve(Function &E, const Function &) { check(pg_efield_dg0(E.pop().handle, nullptr)); }
+};
+
+// ESolver (punc/src/efield.cpp:41-75): CG1 projection of -grad(phi)
+struct ESolver {
+    void solve(Function &E, const Function &) { check(pg_esolver_solve(E.pop().handle, nullptr, nullptr)); }
 };
 
 // CircuitCM (punc/src/object_CM.cpp:135-197)

@@ -634,6 +634,94 @@ double or_accel(void *h, const double *E, double dt, int32_t nthreads) {
     return KE;
 }
 
+// ESolver right-hand side (punc/src/efield.cpp:70-75, punc/ufl/EField3D.ufl:
+// L = inner(-grad(phi), v) dx): for a P1 phi the gradient is constant on a
+// cell, and the integral of lambda_i over the cell is vol/4, so
+// b[d][c] = sum over the cells T of dof d of (vol_T / 4) (-grad phi_T)_c.
+// The gradient uses the DG0 field's arithmetic (or_efield_dg0 with E0 = 0).
+void or_esolver_rhs(void *h, const double *phi, double *b) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    std::vector<double> E(3 * (size_t)o.nc);
+    or_efield_dg0(h, phi, nullptr, E.data());
+    for (int64_t i = 0; i < 3 * o.ndof; ++i) b[i] = 0.0;
+    for (const Cell &c : o.cells) {
+        const double w = 0.25 * c.volume;
+        for (int i = 0; i < 4; ++i)
+            for (int d = 0; d < 3; ++d) b[3 * c.dofs[i] + d] += w * E[3 * c.id + d];
+    }
+}
+
+// CG1 field at a particle: Ei = sum_i coeffs[i] * values[j*4 + i], values the
+// cell's vertex values of component j (pusher.h:178-186, 318-326).
+static void cg1_field(const Cell &cell, const double *Ev, const double *x, double *Ei) {
+    double coeffs[4];
+    cell.barycentric(x, coeffs);
+    for (int j = 0; j < 3; j++) {
+        Ei[j] = 0.0;
+        for (int i = 0; i < 4; ++i) Ei[j] += coeffs[i] * Ev[3 * cell.dofs[i] + j];
+    }
+}
+
+// accel_cg1 (punc/include/punc/pusher.h:154-201); Ev: [ndof][3].
+double or_accel_cg1(void *h, const double *Ev, double dt, int32_t nthreads) {
+    Oracle &o = *static_cast<Oracle *>(h);
+    std::vector<double> part(std::max(1, nthreads), 0.0);
+    for_cells(o.nc, nthreads, [&](int64_t cb, int64_t ce, int t) {
+        double KE = 0.0;
+        for (int64_t cid = cb; cid < ce; ++cid) {
+            Cell &cell = o.cells[cid];
+            for (auto &particle : cell.particles) {
+                const double m = particle.m, q = particle.q;
+                double Ei[3];
+                cg1_field(cell, Ev, particle.x, Ei);
+                for (int j = 0; j < 3; j++) {
+                    Ei[j] *= dt * (q / m);
+                    KE += 0.5 * m * particle.v[j] * (particle.v[j] + Ei[j]);
+                    particle.v[j] += Ei[j];
+                }
+            }
+        }
+        part[t] = KE;
+    });
+    double KE = 0.0;
+    for (double p : part) KE += p;
+    return KE;
+}
+
+// boris_cg1 (punc/include/punc/pusher.h:282-372); Ev: [ndof][3].
+double or_boris_cg1(void *h, const double *Ev, const double *B, double dt, int32_t nthreads) {
+    Oracle &o = *static_cast<Oracle *>(h);
+    std::vector<double> part(std::max(1, nthreads), 0.0);
+    for_cells(o.nc, nthreads, [&](int64_t cb, int64_t ce, int t) {
+        double KE = 0.0;
+        double v_minus[3], v_prime[3], v_plus[3], tt[3], s[3], Ei[3];
+        for (int64_t cid = cb; cid < ce; ++cid) {
+            Cell &cell = o.cells[cid];
+            for (auto &particle : cell.particles) {
+                const double m = particle.m, q = particle.q;
+                const double *vel = particle.v;
+                cg1_field(cell, Ev, particle.x, Ei);
+                double t_mag2 = 0.0;
+                for (int i = 0; i < 3; ++i) { tt[i] = std::tan((dt * q / (2.0 * m)) * B[i]); t_mag2 += tt[i] * tt[i]; }
+                for (int i = 0; i < 3; ++i) s[i] = 2 * tt[i] / (1 + t_mag2);
+                for (int i = 0; i < 3; ++i) v_minus[i] = vel[i] + 0.5 * dt * (q / m) * Ei[i];
+                for (int i = 0; i < 3; i++) KE += 0.5 * m * v_minus[i] * v_minus[i];
+                const double c1[3] = {v_minus[1] * tt[2] - v_minus[2] * tt[1], -v_minus[0] * tt[2] + v_minus[2] * tt[0],
+                                      v_minus[0] * tt[1] - v_minus[1] * tt[0]};
+                for (int i = 0; i < 3; ++i) v_prime[i] = v_minus[i] + c1[i];
+                const double c2[3] = {v_prime[1] * s[2] - v_prime[2] * s[1], -v_prime[0] * s[2] + v_prime[2] * s[0],
+                                      v_prime[0] * s[1] - v_prime[1] * s[0]};
+                for (int i = 0; i < 3; ++i) v_plus[i] = v_minus[i] + c2[i];
+                for (int i = 0; i < 3; ++i) particle.v[i] = v_plus[i] + 0.5 * dt * (q / m) * Ei[i];
+            }
+        }
+        part[t] = KE;
+    });
+    double KE = 0.0;
+    for (double p : part) KE += p;
+    return KE;
+}
+
 // move / move_periodic (punc/include/punc/pusher.h:648-681).
 void or_move(void *h, double dt, const double *Ld, int32_t nthreads) {
     Oracle &o = *static_cast<Oracle *>(h);

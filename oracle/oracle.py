@@ -36,6 +36,9 @@ _SIG = {
     "or_efield_dg0": ([C.c_void_p, _D, _D, _D], None),
     "or_boris": ([C.c_void_p, _D, _D, C.c_double, C.c_int32], C.c_double),
     "or_accel": ([C.c_void_p, _D, C.c_double, C.c_int32], C.c_double),
+    "or_esolver_rhs": ([C.c_void_p, _D, _D], None),
+    "or_accel_cg1": ([C.c_void_p, _D, C.c_double, C.c_int32], C.c_double),
+    "or_boris_cg1": ([C.c_void_p, _D, _D, C.c_double, C.c_int32], C.c_double),
     "or_move": ([C.c_void_p, C.c_double, _D, C.c_int32], None),
     "or_update": ([C.c_void_p, _D, C.c_int32, C.c_double, C.c_int32, _I64, C.c_int32], C.c_int32),
     "or_distribute_cg1": ([C.c_void_p, _D, C.c_int32], None),
@@ -167,6 +170,23 @@ class Oracle:
 
     def accel(self, E, dt, nthreads=1):
         return float(lib().or_accel(self.h, _d(E), dt, nthreads))
+
+    def esolver(self, phi):
+        """ESolver::solve (punc/src/efield.cpp:70-75): CG1 projection of
+        -grad(phi), M E_c = b_c solved directly (scipy SuperLU); [ndof][3]."""
+        import scipy.sparse.linalg as spla
+        b = np.zeros((self.ndof, 3))
+        lib().or_esolver_rhs(self.h, _d(np.ascontiguousarray(phi, float)), _d(b))
+        _, M = self.matrices()
+        lu = spla.splu(M.tocsc())
+        return np.ascontiguousarray(np.stack([lu.solve(b[:, c]) for c in range(3)], axis=1))
+
+    def accel_cg1(self, Ev, dt, nthreads=1):
+        return float(lib().or_accel_cg1(self.h, _d(np.ascontiguousarray(Ev, float)), dt, nthreads))
+
+    def boris_cg1(self, Ev, B, dt, nthreads=1):
+        return float(lib().or_boris_cg1(self.h, _d(np.ascontiguousarray(Ev, float)), _d(np.asarray(B, float)), dt,
+                                        nthreads))
 
     def move(self, dt, Ld=None, nthreads=1):
         lib().or_move(self.h, dt, _d(None if Ld is None else np.asarray(Ld, float)), nthreads)

@@ -73,7 +73,8 @@ class SolveInfo(C.Structure):
 class StepArgs(C.Structure):
     _fields_ = [("dt", C.c_double), ("B", C.c_double * 3), ("first_step", C.c_int32),
                 ("use_accel", C.c_int32), ("periodic_move", C.c_int32), ("Ld", C.c_double * 3),
-                ("inject", C.c_int32), ("seed", C.c_uint64), ("step", C.c_uint64), ("E0", C.c_double * 3)]
+                ("inject", C.c_int32), ("seed", C.c_uint64), ("step", C.c_uint64), ("E0", C.c_double * 3),
+                ("efield_cg1", C.c_int32)]
 
 
 class StepResult(C.Structure):
@@ -139,6 +140,11 @@ SIGNATURES = {
     "pg_event_elapsed": ([_P, C.c_int32, C.c_int32, _D], C.c_int),
     "pg_synchronize": ([_P], C.c_int),
     "pg_launch_count": ([_I64], C.c_int),
+    "pg_esolver_solve": ([_P, _D, C.POINTER(SolveInfo)], C.c_int),
+    "pg_set_efield_cg1": ([_P, _D], C.c_int),
+    "pg_get_efield_cg1": ([_P, _D], C.c_int),
+    "pg_accel_cg1": ([_P, C.c_double, _D], C.c_int),
+    "pg_boris_cg1": ([_P, _D, C.c_double, _D], C.c_int),
     "pg_poisson_layout_get": ([_P, C.POINTER(PoissonLayout)], C.c_int),
     "pg_pcg_solve_noalloc": ([C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                               C.c_double, C.c_int32, C.c_void_p, _I32, _D], C.c_int),

@@ -34,6 +34,7 @@ CU_UNITS = {
     "k_mixed.cu": ["--fmad=true"],
     "k_noalloc.cu": [],
     "k_amg.cu": [],
+    "k_esolve.cu": ["--fmad=true"],
 }
 CPP_UNITS = ["mesh_tables.cpp", "amg.cpp"]
 

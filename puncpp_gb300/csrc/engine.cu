@@ -60,6 +60,16 @@ struct pg_sim {
     std::vector<int64_t> amg_rows, amg_nnz, amg_nnz_p;   // per level (pg_poisson_layout_get)
     int64_t a_nnz = 0, a_sell = 0;                       // stored nonzeros and SELL-32 entries of A
     int64_t amg_nnz_g = 0, amg_nnz_u1 = 0;               // cycle operators G and U1
+
+    // ESolver (CG1 field): dof -> cell adjacency, cell volumes, mass-matrix
+    // D^-1 (and FP32 values), CG work arrays, the packed vertex field
+    int64_t *es_adj_ptr = nullptr;
+    int32_t *es_adj_cell = nullptr;
+    double *es_vol = nullptr, *M_dinv = nullptr, *es_buf = nullptr, *es_part = nullptr, *es_out_d = nullptr;
+    float *M_val32 = nullptr, *M_dinv32 = nullptr, *es_buf32 = nullptr;
+    int32_t *es_out_i = nullptr;
+    double *Ev = nullptr;
+    float *Evf = nullptr;
     bool phi_valid = false;
 
     // circuit (capacitance-matrix method)
@@ -952,6 +962,42 @@ int pg_create(const pg_mesh *mesh, const pg_config *cfg_in, pg_sim **out) {
         if (amg && (rc = setup_amg(s, arow, acol, aval))) return bail(rc);
     }
 
+    // ESolver: dof -> cell adjacency in ascending cell order, volumes, D^-1 of
+    // the mass matrix, work arrays, the packed vertex field
+    {
+        const int64_t nd = h.ndof, ncell = h.nc;
+        std::vector<int64_t> aptr(nd + 1, 0);
+        for (int64_t k = 0; k < 4 * ncell; ++k) aptr[h.cell_dofs[k] + 1]++;
+        for (int64_t d = 0; d < nd; ++d) aptr[d + 1] += aptr[d];
+        std::vector<int32_t> acell(4 * ncell);
+        std::vector<int64_t> cur(aptr.begin(), aptr.end() - 1);
+        for (int64_t c = 0; c < ncell; ++c)
+            for (int i = 0; i < 4; ++i) acell[cur[h.cell_dofs[4 * c + i]]++] = (int32_t)c;
+        std::vector<double> mdinv(nd, 1.0);
+        for (int64_t i = 0; i < nd; ++i)
+            for (int64_t k = h.rowptr[i]; k < h.rowptr[i + 1]; ++k)
+                if (h.col[k] == i && h.M[k] != 0.0) mdinv[i] = 1.0 / h.M[k];
+        if ((rc = upload(s, &s->es_adj_ptr, aptr)) || (rc = upload(s, &s->es_adj_cell, acell)) ||
+            (rc = upload(s, &s->es_vol, h.volume)) || (rc = upload(s, &s->M_dinv, mdinv)) ||
+            (rc = dalloc(s, &s->es_part, 12 * std::max(1, esolve_grid_blocks()))) || (rc = dalloc(s, &s->es_out_i, 2)) ||
+            (rc = dalloc(s, &s->es_out_d, 6)) || (rc = dalloc(s, &s->Ev, 4 * nd)))
+            return bail(rc);
+        cudaMemset(s->Ev, 0, sizeof(double) * 4 * nd);
+        if (cfg.precision == PG_MIXED) {
+            std::vector<float> m32(h.M.begin(), h.M.end()), d32(mdinv.begin(), mdinv.end());
+            if ((rc = upload(s, &s->M_val32, m32)) || (rc = upload(s, &s->M_dinv32, d32)) ||
+                (rc = dalloc(s, &s->es_buf32, 18 * nd)) || (rc = dalloc(s, &s->Evf, 4 * nd)))
+                return bail(rc);
+            cudaMemset(s->es_buf32, 0, sizeof(float) * 18 * nd);
+            cudaMemset(s->Evf, 0, sizeof(float) * 4 * nd);
+        } else {
+            if ((rc = dalloc(s, &s->es_buf, 18 * nd))) return bail(rc);
+            cudaMemset(s->es_buf, 0, sizeof(double) * 18 * nd);
+        }
+        s->dm.Ev = s->Ev;
+        s->dm.Evf = s->Evf;
+    }
+
     // boundary facets
     s->ext_facets_h = h.ext_facets;
     s->obj_facets_h = h.obj_facets;
@@ -1169,6 +1215,94 @@ int pg_locate(pg_sim *s, const double *xs, int64_t n, int64_t *cells) {
     return PG_OK;
 }
 
+// ESolver::solve (punc/src/efield.cpp:70-75): E = L2 projection of -grad(phi)
+// onto CG1 vector fields, plus the uniform E0, into the packed vertex field.
+// FP64 form: FP64 CG to the reference's tolerances (rel 1e-12, abs 1e-14);
+// mixed form: FP32 CG to rel 1e-6 (the FP32 push reads the field in FP32).
+static int esolver_internal(pg_sim *s, const double E0[3], pg_solve_info *info) {
+    const double zero[3] = {0, 0, 0};
+    launch_efield(s->dm, s->phi, zero, s->stream);
+    EsolveArgs e{};
+    e.n = s->ndof;
+    e.fp32 = is_mixed(s) ? 1 : 0;
+    e.adj_ptr = s->es_adj_ptr; e.adj_cell = s->es_adj_cell; e.vol = s->es_vol; e.E_cell = s->dm.E;
+    e.row = s->M_row; e.col = s->M_col; e.val = s->M_val; e.dinv = s->M_dinv;
+    e.val32 = s->M_val32; e.dinv32 = s->M_dinv32;
+    const size_t n3 = 3 * (size_t)s->ndof;
+    if (e.fp32) {
+        float *b = s->es_buf32;
+        e.b32 = b; e.x32 = b + n3; e.r32 = b + 2 * n3; e.z32 = b + 3 * n3; e.p32 = b + 4 * n3; e.Ap32 = b + 5 * n3;
+        e.rtol = 1e-6;
+    } else {
+        double *b = s->es_buf;
+        e.b = b; e.x = b + n3; e.r = b + 2 * n3; e.z = b + 3 * n3; e.p = b + 4 * n3; e.Ap = b + 5 * n3;
+        e.rtol = 1e-12;
+    }
+    e.atol = 1e-14;
+    e.max_iter = 1000;
+    e.partials = s->es_part;
+    e.out_iter = s->es_out_i; e.out_status = s->es_out_i + 1;
+    e.out_rr = s->es_out_d; e.out_bb = s->es_out_d + 3;
+    for (int j = 0; j < 3; ++j) e.E0[j] = E0 ? E0[j] : 0.0;
+    e.ev = s->Ev;
+    e.evf = s->Evf;
+    int err;
+    {
+        StageScope t(s, "efield");
+        err = launch_esolve(e, s->stream);
+    }
+    if (err) return fail(PG_ERR_CUDA, std::string("ESolver launch: ") + cudaGetErrorString((cudaError_t)err));
+    int32_t oi[2];
+    double od[6];
+    PG_CUDA(cudaMemcpyAsync(oi, s->es_out_i, sizeof(oi), cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaMemcpyAsync(od, s->es_out_d, sizeof(od), cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    if (info) {
+        info->iterations = oi[0];
+        info->solves = 1;
+        info->residual = std::sqrt(od[0] + od[1] + od[2]);
+        info->rhs_norm = std::sqrt(od[3] + od[4] + od[5]);
+    }
+    if (oi[1] != 0) return fail(PG_ERR_NOT_CONVERGED, "ESolver: CG on the mass matrix did not converge");
+    return PG_OK;
+}
+
+int pg_esolver_solve(pg_sim *s, double *E, pg_solve_info *info) {
+    if (!s) return fail(PG_ERR_ARG, "NULL handle");
+    int rc = esolver_internal(s, nullptr, info);
+    if (rc) return rc;
+    return E ? pg_get_efield_cg1(s, E) : PG_OK;
+}
+
+int pg_set_efield_cg1(pg_sim *s, const double *E) {
+    if (!s || !E) return fail(PG_ERR_ARG, "pg_set_efield_cg1: NULL argument");
+    const size_t n = (size_t)s->ndof;
+    std::vector<double> x3(3 * n);
+    for (size_t d = 0; d < n; ++d)
+        for (int j = 0; j < 3; ++j) x3[j * n + d] = E[3 * d + j];
+    double *tmp = nullptr;
+    PG_CUDA(cudaMalloc(&tmp, sizeof(double) * x3.size()));
+    cudaError_t e = cudaMemcpy(tmp, x3.data(), sizeof(double) * x3.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        const double zero[3] = {0, 0, 0};
+        launch_pack_ev64(s->ndof, tmp, zero, s->Ev, s->Evf, s->stream);
+        e = cudaStreamSynchronize(s->stream);
+    }
+    cudaFree(tmp);
+    if (e != cudaSuccess) return fail(PG_ERR_CUDA, cudaGetErrorString(e));
+    return PG_OK;
+}
+
+int pg_get_efield_cg1(pg_sim *s, double *E) {
+    if (!s || !E) return fail(PG_ERR_ARG, "pg_get_efield_cg1: NULL argument");
+    std::vector<double> e4(4 * (size_t)s->ndof);
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    PG_CUDA(cudaMemcpy(e4.data(), s->Ev, sizeof(double) * e4.size(), cudaMemcpyDeviceToHost));
+    for (int64_t d = 0; d < s->ndof; ++d)
+        for (int j = 0; j < 3; ++j) E[3 * d + j] = e4[4 * d + j];
+    return PG_OK;
+}
+
 int pg_efield_dg0(pg_sim *s, const double *phi) {
     if (!s) return fail(PG_ERR_ARG, "NULL handle");
     if (phi) {
@@ -1200,14 +1334,16 @@ int pg_get_efield(pg_sim *s, double *E) {
     return PG_OK;
 }
 
-static int push_common(pg_sim *s, const double *B, double dt, bool accel, double *KE) {
+static int push_common(pg_sim *s, const double *B, double dt, bool accel, double *KE, bool cg1 = false) {
     if (!s) return fail(PG_ERR_ARG, "NULL handle");
     PushParams pp;
     fill_push(s, pp, dt, B, accel);
+    pp.cg1 = cg1 ? 1 : 0;
     if (s->n_slots > 0) {
         if (is_mixed(s)) {
             MixedParams mp;
             fill_mixed(s, mp, dt, B, accel, 0.0, false, nullptr);
+            mp.cg1 = cg1 ? 1 : 0;
             launch_mixed_pass(s->dm, s->P[s->cur], s->n_slots, mp, true, false, false, false, s->cfg.max_walk_steps,
                               s->rho_fixed, s->state, s->partials, s->n_part, s->ke_dev, s->stream);
         } else {
@@ -1225,6 +1361,8 @@ static int push_common(pg_sim *s, const double *B, double dt, bool accel, double
 
 int pg_accel(pg_sim *s, double dt, double *KE) { return push_common(s, nullptr, dt, true, KE); }
 int pg_boris(pg_sim *s, const double B[3], double dt, double *KE) { return push_common(s, B, dt, false, KE); }
+int pg_accel_cg1(pg_sim *s, double dt, double *KE) { return push_common(s, nullptr, dt, true, KE, true); }
+int pg_boris_cg1(pg_sim *s, const double B[3], double dt, double *KE) { return push_common(s, B, dt, false, KE, true); }
 
 static void move_mixed(pg_sim *s, double dt, bool periodic, const double *Ld) {
     MixedParams mp;
@@ -1542,7 +1680,10 @@ int pg_step(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_obje
         out.pcg_residual = info.residual;
         if (rc) return rc;
     }
-    {
+    if (a->efield_cg1) {
+        rc = esolver_internal(s, a->E0, nullptr);
+        if (rc) return rc;
+    } else {
         StageScope t(s, "efield");
         launch_efield(s->dm, s->phi, a->E0, s->stream);
     }
@@ -1552,6 +1693,7 @@ int pg_step(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_obje
         const double dt_push = a->first_step ? 0.5 * a->dt : a->dt;
         PushParams pp;
         fill_push(s, pp, dt_push, a->B, a->use_accel != 0);
+        pp.cg1 = a->efield_cg1 ? 1 : 0;
         MoveParams mp{};
         mp.dt = a->dt;
         mp.periodic = a->periodic_move;
@@ -1561,6 +1703,7 @@ int pg_step(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_obje
             PG_CUDA(cudaMemsetAsync(s->rho_fixed, 0, sizeof(unsigned long long) * s->ndof, s->stream));
             MixedParams xp;
             fill_mixed(s, xp, dt_push, a->B, a->use_accel != 0, a->dt, a->periodic_move != 0, a->Ld);
+            xp.cg1 = a->efield_cg1 ? 1 : 0;
             if (s->n_slots > 0)
                 launch_mixed_pass(s->dm, s->P[s->cur], s->n_slots, xp, true, true, true, true, s->cfg.max_walk_steps,
                                   s->rho_fixed, s->state, s->partials, s->n_part, s->ke_dev, s->stream);

@@ -48,7 +48,25 @@ __global__ void __launch_bounds__(kThreads) k_mixed(DevMesh m, DevParticles p, i
         if (PUSH || MOVE) {
             float vx = p.vxf[i], vy = p.vyf[i], vz = p.vzf[i];
             if (PUSH) {
-                const float4 E = __ldg(reinterpret_cast<const float4 *>(m.E_f) + c);
+                float4 E;
+                if (mp.cg1) {
+                    // CG1 vertex field interpolated at the FP32 position
+                    const float4 *A = reinterpret_cast<const float4 *>(m.bary_f) + 3 * (size_t)c;
+                    const float4 r0 = __ldg(A), r1 = __ldg(A + 1), r2 = __ldg(A + 2);
+                    const float l0 = fmaf(r0.w, z, fmaf(r0.z, y, fmaf(r0.y, x, r0.x)));
+                    const float l1 = fmaf(r1.w, z, fmaf(r1.z, y, fmaf(r1.y, x, r1.x)));
+                    const float l2 = fmaf(r2.w, z, fmaf(r2.z, y, fmaf(r2.y, x, r2.x)));
+                    const float l3 = 1.0f - l0 - l1 - l2;
+                    const int4 d = __ldg(m.dofs + c);
+                    const float4 *V = reinterpret_cast<const float4 *>(m.Evf);
+                    const float4 v0 = __ldg(V + d.x), v1 = __ldg(V + d.y), v2 = __ldg(V + d.z), v3 = __ldg(V + d.w);
+                    E.x = fmaf(l3, v3.x, fmaf(l2, v2.x, fmaf(l1, v1.x, l0 * v0.x)));
+                    E.y = fmaf(l3, v3.y, fmaf(l2, v2.y, fmaf(l1, v1.y, l0 * v0.y)));
+                    E.z = fmaf(l3, v3.z, fmaf(l2, v2.z, fmaf(l1, v1.z, l0 * v0.z)));
+                    E.w = 0.0f;
+                } else {
+                    E = __ldg(reinterpret_cast<const float4 *>(m.E_f) + c);
+                }
                 const float coef = mp.coef[s], hm = mp.half_m[s];
                 if (ACCEL) {
                     const float ax = E.x * coef, ay = E.y * coef, az = E.z * coef;

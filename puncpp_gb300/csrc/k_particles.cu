@@ -1,4 +1,4 @@
-// FP64 particle kernels: DG0 field gather + Boris/accel push, move, facet-walk
+// FP64 particle kernels: DG0 or CG1 field gather + Boris/accel push, move, facet-walk
 // relocation with absorption, CG1 deposition, point location, cell sort.
 //
 // Built with --fmad=false: every multiply and add rounds on its own, in the
@@ -60,10 +60,27 @@ __global__ void __launch_bounds__(kThreads) k_particles(DevMesh m, DevParticles 
         if (PUSH || MOVE) {
             double vx = p.vx[i], vy = p.vy[i], vz = p.vz[i];
             if (PUSH) {
-                const double2 *Ec = reinterpret_cast<const double2 *>(m.E) + 2 * (size_t)c;
-                const double2 e01 = __ldg(Ec);
-                const double2 e2_ = __ldg(Ec + 1);
-                const double ex = e01.x, ey = e01.y, ez = e2_.x;
+                double ex, ey, ez;
+                if (pp.cg1) {
+                    // accel_cg1 / boris_cg1 (punc/include/punc/pusher.h:154-201, 282-372):
+                    // Ei = sum_i coeffs[i] * values[j*4 + i] over the cell's vertices
+                    double l0, l1, l2, l3;
+                    barycentric_fp64(m, c, x, y, z, l0, l1, l2, l3);
+                    const int4 d = __ldg(m.dofs + c);
+                    const double2 *V = reinterpret_cast<const double2 *>(m.Ev);
+                    const double2 a0 = __ldg(V + 2 * (size_t)d.x), b0 = __ldg(V + 2 * (size_t)d.x + 1);
+                    const double2 a1 = __ldg(V + 2 * (size_t)d.y), b1 = __ldg(V + 2 * (size_t)d.y + 1);
+                    const double2 a2 = __ldg(V + 2 * (size_t)d.z), b2 = __ldg(V + 2 * (size_t)d.z + 1);
+                    const double2 a3 = __ldg(V + 2 * (size_t)d.w), b3 = __ldg(V + 2 * (size_t)d.w + 1);
+                    ex = l0 * a0.x; ex = ex + l1 * a1.x; ex = ex + l2 * a2.x; ex = ex + l3 * a3.x;
+                    ey = l0 * a0.y; ey = ey + l1 * a1.y; ey = ey + l2 * a2.y; ey = ey + l3 * a3.y;
+                    ez = l0 * b0.x; ez = ez + l1 * b1.x; ez = ez + l2 * b2.x; ez = ez + l3 * b3.x;
+                } else {
+                    const double2 *Ec = reinterpret_cast<const double2 *>(m.E) + 2 * (size_t)c;
+                    const double2 e01 = __ldg(Ec);
+                    const double2 e2_ = __ldg(Ec + 1);
+                    ex = e01.x; ey = e01.y; ez = e2_.x;
+                }
                 const double coef = pp.coef[s], hm = pp.half_m[s];
                 if (ACCEL) {
                     // accel (punc/include/punc/pusher.h:66-130): Ei *= dt*(q/m);

@@ -33,6 +33,9 @@ struct DevMesh {
     const float *planes_f = nullptr;  // [nc][16]
     const float *bary_f = nullptr;    // [nc][12] padded to 16
     float *E_f = nullptr;             // [nc][4]
+    // CG1 (vertex) field of the ESolver path: [ndof][4] (x, y, z, 0)
+    const double *Ev = nullptr;
+    const float *Evf = nullptr;
     // point-location bins
     double lo[3] = {0, 0, 0}, bin_h[3] = {1, 1, 1};
     int32_t nbin[3] = {1, 1, 1};
@@ -73,6 +76,7 @@ struct PushParams {
     double s[kMaxSpecies][3];
     int32_t has_B;
     int32_t accel;                // 1: accel() update rule
+    int32_t cg1;                  // 1: field interpolated from the CG1 vertex field (accel_cg1 / boris_cg1)
 };
 
 struct MoveParams {
@@ -115,6 +119,31 @@ struct MixedParams {
     float dt;
     int32_t periodic;
     float Ld[3];
+    int32_t cg1;                  // 1: field interpolated from the CG1 vertex field
+};
+
+// ESolver: rhs gather, three-component Jacobi-CG on the mass matrix, packing
+// of the vertex field (+ E0).  fp32 selects the FP32 arrays.
+struct EsolveArgs {
+    int32_t n;                    // dofs
+    int32_t fp32;
+    const int64_t *adj_ptr;       // dof -> cells, [n + 1]
+    const int32_t *adj_cell;
+    const double *vol;            // [nc]
+    const double *E_cell;         // [nc][4], -grad phi per cell
+    const int32_t *row, *col;     // mass matrix CSR
+    const double *val, *dinv;
+    const float *val32, *dinv32;
+    double *b, *x, *r, *z, *p, *Ap;          // [3][n] (FP64 form)
+    float *b32, *x32, *r32, *z32, *p32, *Ap32;  // [3][n] (mixed form)
+    double *partials;             // [12][grid]
+    double rtol, atol;
+    int32_t max_iter;
+    int32_t *out_iter, *out_status;
+    double *out_rr, *out_bb;      // [3] each
+    double E0[3];
+    double *ev;                   // [n][4] or null
+    float *evf;                   // [n][4] or null
 };
 
 // PCG on the Dirichlet-reduced symmetric matrix, one cooperative launch.
@@ -231,6 +260,9 @@ void launch_set_bc(const int32_t *bc_kind, const double *bc_value, const double 
 int launch_pcg(const PcgArgs &a, cudaStream_t st);
 int pcg_grid_blocks();
 int launch_pcg_amg(const PcgArgs &a, const AmgDev &amg, cudaStream_t st);
+int esolve_grid_blocks();
+int launch_esolve(const EsolveArgs &e, cudaStream_t st);
+void launch_pack_ev64(int32_t n, const double *x3, const double E0[3], double *ev, float *evf, cudaStream_t st);
 int pcg_amg_grid_blocks();
 struct Pots {
     int32_t n;

@@ -197,10 +197,11 @@ class Population:
 
 
 class Function:
-    """A field of the Population's engine: 'E' (DG0 vector), 'rho' or 'phi' (CG1)."""
+    """A field of the Population's engine: 'E' (DG0 vector), 'E_cg1' (CG1
+    vector, [Ndof][3]), 'rho' or 'phi' (CG1)."""
 
     def __init__(self, pop: Population, kind: str):
-        assert kind in ("E", "rho", "phi")
+        assert kind in ("E", "E_cg1", "rho", "phi")
         self.pop, self.kind = pop, kind
 
     def vector(self) -> np.ndarray:
@@ -208,6 +209,9 @@ class Function:
         if self.kind == "E":
             out = np.zeros((self.pop.num_cells, 3))
             L.check(lib.pg_get_efield(self.pop.handle, L.dptr(out)))
+        elif self.kind == "E_cg1":
+            out = np.zeros((self.pop.ndof, 3))
+            L.check(lib.pg_get_efield_cg1(self.pop.handle, L.dptr(out)))
         else:
             out = np.zeros(self.pop.ndof)
             fn = lib.pg_get_rho if self.kind == "rho" else lib.pg_get_phi
@@ -219,6 +223,8 @@ class Function:
         lib = L.load()
         if self.kind == "E":
             L.check(lib.pg_set_efield(self.pop.handle, L.dptr(v.reshape(-1, 3))))
+        elif self.kind == "E_cg1":
+            L.check(lib.pg_set_efield_cg1(self.pop.handle, L.dptr(v.reshape(-1, 3))))
         elif self.kind == "rho":
             L.check(lib.pg_set_rho(self.pop.handle, L.dptr(v)))
         else:
@@ -237,6 +243,21 @@ def boris(pop: Population, E: Function, B, dt: float) -> float:
     b = np.ascontiguousarray(B, np.float64)
     ke = C.c_double()
     L.check(L.load().pg_boris(pop.handle, L.dptr(b), dt, C.byref(ke)))
+    return ke.value
+
+
+def accel_cg1(pop: Population, E: Function, dt: float) -> float:
+    """accel_cg1 with the CG1 field (punc/include/punc/pusher.h:154-201)."""
+    ke = C.c_double()
+    L.check(L.load().pg_accel_cg1(pop.handle, dt, C.byref(ke)))
+    return ke.value
+
+
+def boris_cg1(pop: Population, E: Function, B, dt: float) -> float:
+    """boris_cg1 with the CG1 field and uniform B (punc/include/punc/pusher.h:282-372)."""
+    b = np.ascontiguousarray(B, np.float64)
+    ke = C.c_double()
+    L.check(L.load().pg_boris_cg1(pop.handle, L.dptr(b), dt, C.byref(ke)))
     return ke.value
 
 
@@ -268,6 +289,20 @@ class EFieldDG0:
 
     def solve(self, E: Function, phi: Function):
         L.check(L.load().pg_efield_dg0(E.pop.handle, None))
+
+
+class ESolver:
+    """ESolver (punc/src/efield.cpp:41-75): CG1 projection of -grad(phi)."""
+
+    def __init__(self, pop: Population):
+        self.pop = pop
+        self.last_info = None
+
+    def solve(self, E: Function, phi: Function) -> np.ndarray:
+        info = L.SolveInfo()
+        L.check(L.load().pg_esolver_solve(self.pop.handle, None, C.byref(info)))
+        self.last_info = info
+        return E.vector()
 
 
 class CircuitCM:
@@ -327,11 +362,12 @@ def inject_particles(pop: Population, species, facets, dt: float, seed: int = 0,
 
 
 def step(pop: Population, objects, dt: float, B=(0.0, 0.0, 0.0), first_step=False, use_accel=False, Ld=None,
-         inject=False, seed=0, step_no=0, E0=(0.0, 0.0, 0.0)) -> L.StepResult:
-    """One fused timestep in the order of interaction.cpp:342-480."""
+         inject=False, seed=0, step_no=0, E0=(0.0, 0.0, 0.0), efield_cg1=False) -> L.StepResult:
+    """One fused timestep in the order of interaction.cpp:342-480 (efield_cg1:
+    ESolver + accel_cg1/boris_cg1, else EFieldDG0 + accel/boris)."""
     a = L.StepArgs(dt, (C.c_double * 3)(*B), 1 if first_step else 0, 1 if use_accel else 0,
                    0 if Ld is None else 1, (C.c_double * 3)(*(Ld if Ld is not None else (0.0, 0.0, 0.0))),
-                   1 if inject else 0, seed, step_no, (C.c_double * 3)(*E0))
+                   1 if inject else 0, seed, step_no, (C.c_double * 3)(*E0), 1 if efield_cg1 else 0)
     arr = _objects_in(objects)
     res = L.StepResult()
     L.check(L.load().pg_step(pop.handle, C.byref(a), arr, len(objects), C.byref(res)))

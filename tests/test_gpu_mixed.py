@@ -122,3 +122,34 @@ def test_mixed_fused_steps_track_the_fp64_form(lib, oracle_mod):
     phi64 = punc.Function(pops[L.PG_FP64], "phi").vector()
     phi32 = punc.Function(pops[L.PG_MIXED], "phi").vector()
     assert rel(phi32, phi64) < 1e-5
+
+
+def test_mixed_cg1_field_and_push_close_to_fp64(lib, oracle_mod):
+    """Mixed form with the CG1 field: the FP32 ESolver within 1e-5 of the FP64
+    one, and a fused CG1 step keeps rho within 1e-5 of the FP64 form."""
+    ma = meshgen.probe_box(8, 2.0, 0.6)
+    mesh = punc.Mesh(ma)
+    rng = np.random.default_rng(21)
+    xs = uniform_points(ma, 20000, rng)
+    vs = maxwellian_velocities(20000, 1.0, rng)
+    xi = uniform_points(ma, 20000, rng)
+    vi = maxwellian_velocities(20000, 0.05, rng)
+    pops = {}
+    for prec in (L.PG_FP64, L.PG_MIXED):
+        pop = punc.Population(mesh, precision=prec, pcg_rtol=1e-12)
+        pop.add_particles(f32(xs), f32(vs), -1.0, 1.0)
+        pop.add_particles(f32(xi), f32(vi), 1.0, 100.0)
+        pops[prec] = pop
+    phi = rng.normal(size=mesh.n_dofs)
+    E = {}
+    for prec, pop in pops.items():
+        punc.Function(pop, "phi").set_local(phi)
+        E[prec] = punc.ESolver(pop).solve(punc.Function(pop, "E_cg1"), punc.Function(pop, "phi"))
+    assert rel(E[L.PG_MIXED], E[L.PG_FP64]) < 1e-5
+    objs = {p: [punc.Object(2, potential=-1.0)] for p in pops}
+    for n in range(2):
+        for p in pops:
+            punc.step(pops[p], objs[p], 0.1, first_step=(n == 0), efield_cg1=True)
+        rho64 = punc.Function(pops[L.PG_FP64], "rho").vector()
+        rho32 = punc.Function(pops[L.PG_MIXED], "rho").vector()
+        assert rel(rho32, rho64) < 1e-5, n

@@ -333,3 +333,68 @@ def test_walk_limit_is_reported_and_engine_stays_usable(lib, oracle_mod):
     # the error was reported once; the engine answers further calls
     assert pop.status() == (0, 0)
     assert pop.num_of_particles() > 0
+
+
+@pytest.mark.parametrize("geom", ["probe", "periodic"])
+def test_esolver_matches_a_direct_solve(geom, lib, oracle_mod):
+    """ESolver (CG1 projection of -grad phi): device CG on the mass matrix to
+    rel 1e-12 against the oracle's direct solve of the same system."""
+    setup = probe_setup if geom == "probe" else periodic_setup
+    ma, mesh, pop, o, rng = setup(lib, oracle_mod)
+    phi = rng.normal(size=mesh.n_dofs)
+    punc.Function(pop, "phi").set_local(phi)
+    E = punc.Function(pop, "E_cg1")
+    es = punc.ESolver(pop)
+    Eg = es.solve(E, punc.Function(pop, "phi"))
+    Eo = o.esolver(phi)
+    assert Eg.shape == (mesh.n_dofs, 3)
+    assert rel(Eg, Eo) < 1e-10
+    info = es.last_info
+    assert 0 < info.iterations < 100 and info.residual <= 1e-12 * info.rhs_norm * 1.0001
+
+
+@pytest.mark.parametrize("geom", ["probe", "periodic"])
+def test_cg1_push_bitwise(geom, lib, oracle_mod):
+    """accel_cg1 / boris_cg1 with the same vertex field: velocities bitwise."""
+    setup = probe_setup if geom == "probe" else periodic_setup
+    ma, mesh, pop, o, rng = setup(lib, oracle_mod)
+    Ev = rng.normal(size=(mesh.n_dofs, 3))
+    E = punc.Function(pop, "E_cg1")
+    E.set_local(Ev)
+    assert np.array_equal(E.vector(), Ev)
+    dt = 0.07
+    assert rel(punc.boris_cg1(pop, E, (0.0, 0.0, 0.0), dt), o.boris_cg1(Ev, (0.0, 0.0, 0.0), dt)) < RTOL
+    compare_particles(pop.particles(), o.particles())
+    B = (0.3, -0.2, 0.9)
+    assert rel(punc.boris_cg1(pop, E, B, dt), o.boris_cg1(Ev, B, dt)) < RTOL
+    compare_particles(pop.particles(), o.particles())
+    assert rel(punc.accel_cg1(pop, E, dt), o.accel_cg1(Ev, dt)) < RTOL
+    compare_particles(pop.particles(), o.particles())
+
+
+def test_fused_cg1_steps_in_lockstep_with_oracle(lib, oracle_mod):
+    """pg_step with the CG1 field (the reference time loop's default): the
+    oracle starts from the engine's particles and pushes with the engine's
+    vertex field; particles end bit-identical, the field within 1e-10 of the
+    oracle's projection of the engine's potential."""
+    ma, mesh, pop, o, rng = probe_setup(lib, oracle_mod, pcg_rtol=1e-12)
+    sp = [punc.Species(-1.0, 1.0, n=20.0, vth=1.0), punc.Species(1.0, 100.0, n=20.0, vth=0.1)]
+    punc.create_flux(pop, sp)
+    o.create_flux([dict(q=s.q, m=s.m, n=s.n, vth=s.vth) for s in sp])
+    objs = [punc.Object(2, potential=-1.0)]
+    dt = 0.2
+    for n in range(3):
+        o.set_particles(pop.particles())
+        res = punc.step(pop, objs, dt, first_step=(n == 0), inject=True, seed=7, step_no=n, efield_cg1=True)
+        phi = punc.Function(pop, "phi").vector()
+        Ev = punc.Function(pop, "E_cg1").vector()
+        assert rel(Ev, o.esolver(phi)) < 1e-10
+        ke = o.boris_cg1(Ev, (0, 0, 0), dt * (0.5 if n == 0 else 1.0))
+        o.move(dt)
+        oobjs = [dict(bnd_id=2, charge=0.0, current=0.0, potential=-1.0)]
+        absorbed = o.update(oobjs, dt)
+        assert res.n_absorbed == absorbed.sum()
+        assert rel(res.KE, ke) < RTOL
+        ko, _ = o.inject(dt, 7, n)
+        assert res.n_injected == ko
+        compare_particles(pop.particles(), o.particles())

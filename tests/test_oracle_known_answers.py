@@ -144,3 +144,34 @@ def test_update_absorbs_at_object_and_tallies_current(oracle_mod):
     assert absorbed[2] == 1 and absorbed[1] == 1
     assert objs[0]["charge"] == 1.0 - 2.0 and objs[0]["current"] == -2.0 / 0.5
     assert o.num_particles() == 1
+
+
+def test_esolver_projects_a_uniform_field_exactly(oracle_mod):
+    """ESolver of a linear potential: -grad(phi) is a constant, which the CG1
+    L2 projection reproduces at every vertex; the CG1 push of a uniform field
+    then equals the DG0 push of the same field (the barycentric weights sum
+    to one)."""
+    from helpers import maxwellian_velocities, uniform_points
+    for ma in (meshgen.probe_box(6, 2.0, 0.6), meshgen.langmuir_cube(5)):
+        o = oracle_mod.Oracle(ma)
+        a = np.array([0.3, -1.2, 0.7])
+        phi = np.zeros(ma.n_dofs)
+        phi[ma.vertex_to_dof] = ma.coords @ a + 0.5
+        if ma.n_dofs < ma.n_vertices:
+            # periodic: a linear phi is not periodic; project a zero field instead
+            a = np.zeros(3)
+            phi[:] = 0.25
+        Ev = o.esolver(phi)
+        np.testing.assert_allclose(Ev, np.broadcast_to(-a, Ev.shape), rtol=0, atol=1e-12)
+        rng = np.random.default_rng(11)
+        x = uniform_points(ma, 2000, rng)
+        v = maxwellian_velocities(2000, 1.0, rng)
+        o2 = oracle_mod.Oracle(ma)
+        o.add_particles(x, v, -1.0, 1.0)
+        o2.add_particles(x, v, -1.0, 1.0)
+        Ev = np.broadcast_to(np.array([0.2, 0.1, -0.4]), (ma.n_dofs, 3)).copy()
+        Ec = np.broadcast_to(np.array([0.2, 0.1, -0.4]), (ma.n_cells, 3)).copy()
+        ke1 = o.boris_cg1(Ev, (0.1, 0.0, 0.3), 0.05)
+        ke2 = o2.boris(Ec, (0.1, 0.0, 0.3), 0.05)
+        assert abs(ke1 - ke2) <= 1e-13 * abs(ke2)
+        np.testing.assert_allclose(o.particles()["v"], o2.particles()["v"], rtol=0, atol=1e-14)
