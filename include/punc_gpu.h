@@ -277,6 +277,19 @@ int pg_get_efield_cg1(pg_sim *sim, double *E);         /* [Ndof][3] */
 int pg_accel_cg1(pg_sim *sim, double dt, double *KE);
 int pg_boris_cg1(pg_sim *sim, const double B[3], double dt, double *KE);
 
+/* Diagnostics (punc/include/punc/diagnostics.h), on the device particles;
+ * species are told apart by the sign of q, as in the reference.
+ * particle_potential_energy_cg1 (diagnostics.h:379-412) with the current phi. */
+int pg_potential_energy(pg_sim *sim, double *PE);
+/* density_cg1 (diagnostics.h:492-555): ne, ni [Ndof], weights w_e, w_i. */
+int pg_density_cg1(pg_sim *sim, double weight_e, double weight_i, double *ne, double *ni);
+/* density_dg0 (diagnostics.h:433-465): ne, ni [Nc]. */
+int pg_density_dg0(pg_sim *sim, double weight_e, double weight_i, double *ne, double *ni);
+/* Population::statistics (population.h:746-805): mean speed and sample
+ * standard deviation of the negative particles, then of the positive ones
+ * (two-pass sums on the device; 0, 0 for a sign without particles). */
+int pg_statistics(pg_sim *sim, double *stats);
+
 /* Number of kernels this library has launched in this process. */
 int pg_launch_count(int64_t *n);
 

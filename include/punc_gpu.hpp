@@ -18,6 +18,7 @@
 #define PUNC_GPU_HPP
 
 #include <cstddef>
+#include <cstdio>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -131,6 +132,8 @@ public:
     std::size_t num_of_particles() { return counts(0); }
     std::size_t num_of_negatives() { return counts(1); }
     std::size_t num_of_positives() { return counts(2); }
+    // Population::statistics (population.h:746-805)
+    void statistics(double *stats) { check(pg_statistics(handle, stats)); }
 
     pg_sim *handle = nullptr;
     static constexpr std::size_t g_dim = 3;
@@ -198,6 +201,65 @@ inline double kinetic_energy(Population<3> &pop) {
     check(pg_kinetic_energy(pop.handle, &ke));
     return ke;
 }
+
+// diagnostics.h:379-412, 433-465, 492-555
+inline double particle_potential_energy_cg1(Population<3> &pop, const Function &) {
+    double pe = 0;
+    check(pg_potential_energy(pop.handle, &pe));
+    return pe;
+}
+inline void density_cg1(Population<3> &pop, double weight_e, double weight_i, std::vector<double> &ne,
+                        std::vector<double> &ni) {
+    check(pg_density_cg1(pop.handle, weight_e, weight_i, ne.data(), ni.data()));
+}
+inline void density_dg0(Population<3> &pop, double weight_e, double weight_i, std::vector<double> &ne,
+                        std::vector<double> &ni) {
+    check(pg_density_dg0(pop.handle, weight_e, weight_i, ne.data(), ni.data()));
+}
+
+// History (punc/src/diagnostics.cpp:70-140, diagnostics.h:119-168): the
+// history.dat preamble and rows in the reference's format.
+class History {
+public:
+    History(const std::string &fname, std::size_t n_objects, std::size_t dim, bool stats,
+            bool continue_simulation = false)
+        : stats_(stats), f_(std::fopen(fname.c_str(), continue_simulation ? "a" : "w")) {
+        if (!f_) throw std::runtime_error("History: cannot open " + fname);
+        if (continue_simulation) return;
+        std::fprintf(f_, "#:xaxis\tt\n#:name\tn\tt\tne\tni\tKE\tPE");
+        for (std::size_t i = 0; i < n_objects; ++i) std::fprintf(f_, "\tV[%zu]\tI[%zu]\tQ[%zu]", i, i, i);
+        if (stats) std::fprintf(f_, "\tmean_e\tstdev_e\tmean_i\tstdev_i");
+        std::fprintf(f_, "\n#:long\ttimestep\ttime\t\"number of electrons\"\t\"number of ions\"\t"
+                         "\"kinetic energy\"\t\"potential energy\"");
+        for (std::size_t i = 0; i < n_objects; ++i) std::fprintf(f_, "\tvoltage\tcurrent\tcharge");
+        if (stats)
+            std::fprintf(f_, "\tmean velocity of electrons\tstandard deviation of electron velocities"
+                             "\tmean velocity of ions\tstandard deviation of ion velocities");
+        std::fprintf(f_, "\n#:units\t1\ts\tm**(-3)\tm**(-3)\tJ\tJ");
+        const char *ui = dim == 1 ? "A/m**2" : dim == 2 ? "A/m" : "A";
+        for (std::size_t i = 0; i < n_objects; ++i) std::fprintf(f_, "\tV\t%s\tC", ui);
+        if (stats) std::fprintf(f_, "\tm/s\tm/s\tm/s\tm/s");
+        std::fprintf(f_, "\n");
+    }
+    ~History() { if (f_) std::fclose(f_); }
+    History(const History &) = delete;
+    History &operator=(const History &) = delete;
+    void save(std::size_t n, double t, double num_e, double num_i, double KE, double PE, const ObjectVector &objects,
+              Population<3> &pop) {
+        std::fprintf(f_, "%zu\t%.16e\t%.16e\t%.16e\t%.16e\t%.16e", n, t, num_e, num_i, KE, PE);
+        for (auto &o : objects) std::fprintf(f_, "\t%.16e\t%.16e\t%.16e", o->potential, o->current, o->charge);
+        if (stats_) {
+            double st[4];
+            pop.statistics(st);
+            for (double v : st) std::fprintf(f_, "\t%.16e", v);
+        }
+        std::fprintf(f_, "\n");
+    }
+
+private:
+    bool stats_;
+    std::FILE *f_;
+};
 
 // EFieldDG0 (punc/src/efield.cpp:77-99)
 struct EFieldDG0 {

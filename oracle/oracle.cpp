@@ -722,6 +722,88 @@ double or_boris_cg1(void *h, const double *Ev, const double *B, double dt, int32
     return KE;
 }
 
+// particle_potential_energy_cg1 (punc/include/punc/diagnostics.h:379-412).
+double or_potential_energy(void *h, const double *phi) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    double PE = 0.0, coeffs[4];
+    for (const Cell &cell : o.cells)
+        for (const auto &particle : cell.particles) {
+            cell.barycentric(particle.x, coeffs);
+            double phi_x = 0.0;
+            for (int i = 0; i < 4; ++i) phi_x += coeffs[i] * phi[cell.dofs[i]];
+            PE += 0.5 * particle.q * phi_x;
+        }
+    return PE;
+}
+
+// density_cg1 (punc/include/punc/diagnostics.h:492-555).
+void or_density_cg1(void *h, double weight_e, double weight_i, double *ne, double *ni) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    for (int64_t i = 0; i < o.ndof; ++i) ne[i] = ni[i] = 0.0;
+    double cell_coords[4];
+    for (const Cell &cell : o.cells) {
+        double accum_e[4] = {0, 0, 0, 0}, accum_i[4] = {0, 0, 0, 0};
+        for (const auto &particle : cell.particles) {
+            cell.barycentric(particle.x, cell_coords);
+            if (particle.q < 0) { for (int i = 0; i < 4; ++i) accum_e[i] += cell_coords[i]; }
+            else { for (int i = 0; i < 4; ++i) accum_i[i] += cell_coords[i]; }
+        }
+        for (int i = 0; i < 4; ++i) { ne[cell.dofs[i]] += accum_e[i]; ni[cell.dofs[i]] += accum_i[i]; }
+    }
+    for (int64_t i = 0; i < o.ndof; ++i) {
+        ne[i] *= o.dv_inv[i] * weight_e;
+        ni[i] *= o.dv_inv[i] * weight_i;
+    }
+}
+
+// density_dg0 (punc/include/punc/diagnostics.h:433-465).
+void or_density_dg0(void *h, double weight_e, double weight_i, double *ne, double *ni) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    for (const Cell &cell : o.cells) {
+        double accum_e = 0.0, accum_i = 0.0;
+        for (const auto &particle : cell.particles) {
+            if (particle.q > 0) accum_i += weight_i;
+            else accum_e += weight_e;
+        }
+        ne[cell.id] = accum_e / cell.volume;
+        ni[cell.id] = accum_i / cell.volume;
+    }
+}
+
+// Population::statistics (punc/include/punc/population.h:746-805): Welford.
+void or_statistics(void *h, double *stats) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    std::size_t m = 0, n = 0;
+    double m_e_old = 0, m_i_old = 0;
+    for (int k = 0; k < 4; ++k) stats[k] = 0.0;
+    for (const Cell &cell : o.cells)
+        for (const auto &particle : cell.particles) {
+            double v = 0;
+            for (int i = 0; i < 3; ++i) v += particle.v[i] * particle.v[i];
+            v = std::sqrt(v);
+            if (particle.q < 0) {
+                m++;
+                if (m == 1) { m_e_old = v; stats[0] = v; stats[1] = 0.0; }
+                else {
+                    stats[0] = m_e_old + (v - m_e_old) / m;
+                    stats[1] += (v - m_e_old) * (v - stats[0]);
+                    m_e_old = stats[0];
+                }
+            }
+            if (particle.q > 0) {
+                n++;
+                if (n == 1) { m_i_old = v; stats[2] = v; stats[3] = 0.0; }
+                else {
+                    stats[2] = m_i_old + (v - m_i_old) / n;
+                    stats[3] += (v - m_i_old) * (v - stats[2]);
+                    m_i_old = stats[2];
+                }
+            }
+        }
+    if (m > 0) stats[1] = std::sqrt(stats[1] / (m - 1));
+    if (n > 0) stats[3] = std::sqrt(stats[3] / (n - 1));
+}
+
 // move / move_periodic (punc/include/punc/pusher.h:648-681).
 void or_move(void *h, double dt, const double *Ld, int32_t nthreads) {
     Oracle &o = *static_cast<Oracle *>(h);

@@ -37,6 +37,10 @@ _SIG = {
     "or_boris": ([C.c_void_p, _D, _D, C.c_double, C.c_int32], C.c_double),
     "or_accel": ([C.c_void_p, _D, C.c_double, C.c_int32], C.c_double),
     "or_esolver_rhs": ([C.c_void_p, _D, _D], None),
+    "or_potential_energy": ([C.c_void_p, _D], C.c_double),
+    "or_density_cg1": ([C.c_void_p, C.c_double, C.c_double, _D, _D], None),
+    "or_density_dg0": ([C.c_void_p, C.c_double, C.c_double, _D, _D], None),
+    "or_statistics": ([C.c_void_p, _D], None),
     "or_accel_cg1": ([C.c_void_p, _D, C.c_double, C.c_int32], C.c_double),
     "or_boris_cg1": ([C.c_void_p, _D, _D, C.c_double, C.c_int32], C.c_double),
     "or_move": ([C.c_void_p, C.c_double, _D, C.c_int32], None),
@@ -180,6 +184,24 @@ class Oracle:
         _, M = self.matrices()
         lu = spla.splu(M.tocsc())
         return np.ascontiguousarray(np.stack([lu.solve(b[:, c]) for c in range(3)], axis=1))
+
+    def potential_energy(self, phi):
+        return float(lib().or_potential_energy(self.h, _d(np.ascontiguousarray(phi, float))))
+
+    def density_cg1(self, weight_e, weight_i):
+        ne, ni = np.zeros(self.ndof), np.zeros(self.ndof)
+        lib().or_density_cg1(self.h, weight_e, weight_i, _d(ne), _d(ni))
+        return ne, ni
+
+    def density_dg0(self, weight_e, weight_i):
+        ne, ni = np.zeros(self.nc), np.zeros(self.nc)
+        lib().or_density_dg0(self.h, weight_e, weight_i, _d(ne), _d(ni))
+        return ne, ni
+
+    def statistics(self):
+        out = np.zeros(4)
+        lib().or_statistics(self.h, _d(out))
+        return out
 
     def accel_cg1(self, Ev, dt, nthreads=1):
         return float(lib().or_accel_cg1(self.h, _d(np.ascontiguousarray(Ev, float)), dt, nthreads))

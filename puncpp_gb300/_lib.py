@@ -141,6 +141,10 @@ SIGNATURES = {
     "pg_synchronize": ([_P], C.c_int),
     "pg_launch_count": ([_I64], C.c_int),
     "pg_esolver_solve": ([_P, _D, C.POINTER(SolveInfo)], C.c_int),
+    "pg_potential_energy": ([_P, _D], C.c_int),
+    "pg_density_cg1": ([_P, C.c_double, C.c_double, _D, _D], C.c_int),
+    "pg_density_dg0": ([_P, C.c_double, C.c_double, _D, _D], C.c_int),
+    "pg_statistics": ([_P, _D], C.c_int),
     "pg_set_efield_cg1": ([_P, _D], C.c_int),
     "pg_get_efield_cg1": ([_P, _D], C.c_int),
     "pg_accel_cg1": ([_P, C.c_double, _D], C.c_int),

@@ -35,6 +35,7 @@ CU_UNITS = {
     "k_noalloc.cu": [],
     "k_amg.cu": [],
     "k_esolve.cu": ["--fmad=true"],
+    "k_diag.cu": [],
 }
 CPP_UNITS = ["mesh_tables.cpp", "amg.cpp"]
 

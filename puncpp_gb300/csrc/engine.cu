@@ -70,6 +70,10 @@ struct pg_sim {
     int32_t *es_out_i = nullptr;
     double *Ev = nullptr;
     float *Evf = nullptr;
+
+    // diagnostics scratch (allocated on first use)
+    double *diag_a = nullptr, *diag_b = nullptr, *diag_acc = nullptr;
+    unsigned long long *diag_cnt = nullptr;
     bool phi_valid = false;
 
     // circuit (capacitance-matrix method)
@@ -1300,6 +1304,68 @@ int pg_get_efield_cg1(pg_sim *s, double *E) {
     PG_CUDA(cudaMemcpy(e4.data(), s->Ev, sizeof(double) * e4.size(), cudaMemcpyDeviceToHost));
     for (int64_t d = 0; d < s->ndof; ++d)
         for (int j = 0; j < 3; ++j) E[3 * d + j] = e4[4 * d + j];
+    return PG_OK;
+}
+
+static int diag_scratch(pg_sim *s) {
+    if (s->diag_a) return PG_OK;
+    const size_t n = (size_t)std::max(s->ndof, s->nc);
+    int rc;
+    if ((rc = dalloc(s, &s->diag_a, n)) || (rc = dalloc(s, &s->diag_b, n)) || (rc = dalloc(s, &s->diag_acc, 8)) ||
+        (rc = dalloc(s, &s->diag_cnt, 2 * (size_t)s->nc)))
+        return rc;
+    return PG_OK;
+}
+
+int pg_potential_energy(pg_sim *s, double *PE) {
+    if (!s || !PE) return fail(PG_ERR_ARG, "pg_potential_energy: NULL argument");
+    int rc = diag_scratch(s);
+    if (rc) return rc;
+    launch_potential_energy(s->dm, s->P[s->cur], s->n_slots, is_mixed(s), s->d_q, s->phi, s->diag_acc, s->stream);
+    PG_CUDA(cudaMemcpyAsync(PE, s->diag_acc, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    return PG_OK;
+}
+
+int pg_density_cg1(pg_sim *s, double weight_e, double weight_i, double *ne, double *ni) {
+    if (!s || !ne || !ni) return fail(PG_ERR_ARG, "pg_density_cg1: NULL argument");
+    int rc = diag_scratch(s);
+    if (rc) return rc;
+    launch_density_cg1(s->dm, s->P[s->cur], s->n_slots, is_mixed(s), s->d_q, weight_e, weight_i, s->diag_a,
+                       s->diag_b, s->stream);
+    PG_CUDA(cudaMemcpyAsync(ne, s->diag_a, sizeof(double) * s->ndof, cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaMemcpyAsync(ni, s->diag_b, sizeof(double) * s->ndof, cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    return PG_OK;
+}
+
+int pg_density_dg0(pg_sim *s, double weight_e, double weight_i, double *ne, double *ni) {
+    if (!s || !ne || !ni) return fail(PG_ERR_ARG, "pg_density_dg0: NULL argument");
+    int rc = diag_scratch(s);
+    if (rc) return rc;
+    launch_density_dg0(s->dm, s->P[s->cur], s->n_slots, s->d_q, s->es_vol, weight_e, weight_i, s->diag_cnt,
+                       s->diag_a, s->diag_b, s->stream);
+    PG_CUDA(cudaMemcpyAsync(ne, s->diag_a, sizeof(double) * s->nc, cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaMemcpyAsync(ni, s->diag_b, sizeof(double) * s->nc, cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    return PG_OK;
+}
+
+int pg_statistics(pg_sim *s, double *stats) {
+    if (!s || !stats) return fail(PG_ERR_ARG, "pg_statistics: NULL argument");
+    int rc = diag_scratch(s);
+    if (rc) return rc;
+    launch_statistics(s->P[s->cur], s->n_slots, is_mixed(s), s->d_q, s->diag_acc, s->stream);
+    double acc[6];
+    PG_CUDA(cudaMemcpyAsync(acc, s->diag_acc, sizeof(acc), cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    // mean and sample standard deviation per sign (population.h:800-801); no
+    // particle of a sign: 0, 0
+    const double m = acc[0], n = acc[2];
+    stats[0] = m > 0 ? acc[1] / m : 0.0;
+    stats[1] = m > 0 ? std::sqrt(acc[4] / (m - 1)) : 0.0;
+    stats[2] = n > 0 ? acc[3] / n : 0.0;
+    stats[3] = n > 0 ? std::sqrt(acc[5] / (n - 1)) : 0.0;
     return PG_OK;
 }
 

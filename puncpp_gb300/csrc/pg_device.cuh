@@ -261,6 +261,16 @@ int launch_pcg(const PcgArgs &a, cudaStream_t st);
 int pcg_grid_blocks();
 int launch_pcg_amg(const PcgArgs &a, const AmgDev &amg, cudaStream_t st);
 int esolve_grid_blocks();
+// diagnostics (k_diag.cu)
+void launch_potential_energy(const DevMesh &m, const DevParticles &p, int64_t n_slots, bool mixed,
+                             const double *qsp, const double *phi, double *out, cudaStream_t st);
+void launch_density_cg1(const DevMesh &m, const DevParticles &p, int64_t n_slots, bool mixed, const double *qsp,
+                        double we, double wi, double *ne, double *ni, cudaStream_t st);
+void launch_density_dg0(const DevMesh &m, const DevParticles &p, int64_t n_slots, const double *qsp,
+                        const double *vol, double we, double wi, unsigned long long *cnt, double *ne, double *ni,
+                        cudaStream_t st);
+void launch_statistics(const DevParticles &p, int64_t n_slots, bool mixed, const double *qsp, double *acc,
+                       cudaStream_t st);
 int launch_esolve(const EsolveArgs &e, cudaStream_t st);
 void launch_pack_ev64(int32_t n, const double *x3, const double E0[3], double *ev, float *evf, cudaStream_t st);
 int pcg_amg_grid_blocks();

@@ -170,6 +170,14 @@ class Population:
     def num_of_positives(self) -> int:
         return self._counts()[2]
 
+    def statistics(self) -> np.ndarray:
+        """Population::statistics (punc/include/punc/population.h:746-805): mean
+        speed and sample standard deviation of the negative, then the positive
+        particles."""
+        out = np.zeros(4)
+        L.check(L.load().pg_statistics(self.handle, L.dptr(out)))
+        return out
+
     def particles(self) -> dict:
         """Live particles ordered by (cell, id): x, v, q, m, cell, id."""
         lib = L.load()
@@ -282,6 +290,73 @@ def kinetic_energy(pop: Population) -> float:
     ke = C.c_double()
     L.check(L.load().pg_kinetic_energy(pop.handle, C.byref(ke)))
     return ke.value
+
+
+def particle_potential_energy_cg1(pop: Population, phi: Function) -> float:
+    """particle_potential_energy_cg1 (punc/include/punc/diagnostics.h:379-412)
+    with the engine's current potential."""
+    pe = C.c_double()
+    L.check(L.load().pg_potential_energy(pop.handle, C.byref(pe)))
+    return pe.value
+
+
+def density_cg1(pop: Population, weight_e: float, weight_i: float):
+    """density_cg1 (punc/include/punc/diagnostics.h:492-555): (ne, ni) per dof."""
+    ne, ni = np.zeros(pop.ndof), np.zeros(pop.ndof)
+    L.check(L.load().pg_density_cg1(pop.handle, weight_e, weight_i, L.dptr(ne), L.dptr(ni)))
+    return ne, ni
+
+
+def density_dg0(pop: Population, weight_e: float, weight_i: float):
+    """density_dg0 (punc/include/punc/diagnostics.h:433-465): (ne, ni) per cell."""
+    ne, ni = np.zeros(pop.num_cells), np.zeros(pop.num_cells)
+    L.check(L.load().pg_density_dg0(pop.handle, weight_e, weight_i, L.dptr(ne), L.dptr(ni)))
+    return ne, ni
+
+
+class History:
+    """History (punc/src/diagnostics.cpp:70-140, punc/include/punc/diagnostics.h:
+    119-168): the history.dat preamble and one tab-separated row per step, the
+    step as an integer and the rest in scientific notation with 16 digits after
+    the point (std::setprecision(digits10 + 1) << std::scientific), as the
+    reference writes them."""
+
+    def __init__(self, fname: str, objects, dim: int = 3, stats: bool = False, continue_simulation: bool = False):
+        self.stats = stats
+        self.f = open(fname, "a" if continue_simulation else "w")
+        if not continue_simulation:
+            n = len(objects)
+            self.f.write("#:xaxis\tt\n")
+            self.f.write("#:name\tn\tt\tne\tni\tKE\tPE" + "".join(f"\tV[{i}]\tI[{i}]\tQ[{i}]" for i in range(n)))
+            if stats:
+                self.f.write("\tmean_e\tstdev_e\tmean_i\tstdev_i")
+            self.f.write("\n")
+            self.f.write('#:long\ttimestep\ttime\t"number of electrons"\t"number of ions"\t"kinetic energy"\t'
+                         '"potential energy"' + "\tvoltage\tcurrent\tcharge" * n)
+            if stats:
+                self.f.write("\tmean velocity of electrons\tstandard deviation of electron velocities"
+                             "\tmean velocity of ions\tstandard deviation of ion velocities")
+            self.f.write("\n")
+            unit_i = {1: "A/m**2", 2: "A/m", 3: "A"}.get(dim, "")
+            self.f.write("#:units\t1\ts\tm**(-3)\tm**(-3)\tJ\tJ" + f"\tV\t{unit_i}\tC" * n)
+            if stats:
+                self.f.write("\tm/s\tm/s\tm/s\tm/s")
+            self.f.write("\n")
+
+    @staticmethod
+    def _fmt(x: float) -> str:
+        return f"{x:.16e}"
+
+    def save(self, n: int, t: float, num_e: float, num_i: float, KE: float, PE: float, objects, pop=None):
+        row = f"{n}\t" + "\t".join(self._fmt(v) for v in (t, num_e, num_i, KE, PE))
+        for o in objects:
+            row += f"\t{self._fmt(o.potential)}\t{self._fmt(o.current)}\t{self._fmt(o.charge)}"
+        if self.stats:
+            row += "".join(f"\t{self._fmt(v)}" for v in pop.statistics())
+        self.f.write(row + "\n")
+
+    def close(self):
+        self.f.close()
 
 
 class EFieldDG0:

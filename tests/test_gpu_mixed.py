@@ -153,3 +153,28 @@ def test_mixed_cg1_field_and_push_close_to_fp64(lib, oracle_mod):
         rho64 = punc.Function(pops[L.PG_FP64], "rho").vector()
         rho32 = punc.Function(pops[L.PG_MIXED], "rho").vector()
         assert rel(rho32, rho64) < 1e-5, n
+
+
+def test_mixed_diagnostics_close_to_the_oracle(lib, oracle_mod):
+    """Diagnostics of the mixed form (FP32 positions and velocities) against
+    the oracle on the same FP32-rounded particles."""
+    ma = meshgen.probe_box(8, 2.0, 0.6)
+    mesh = punc.Mesh(ma)
+    rng = np.random.default_rng(23)
+    o = oracle_mod.Oracle(ma)
+    pop = punc.Population(mesh, precision=L.PG_MIXED)
+    for q, m, vth in ((-1.0, 1.0, 1.0), (1.0, 100.0, 0.1)):
+        xs = f32(uniform_points(ma, 20000, rng))
+        vs = f32(maxwellian_velocities(20000, vth, rng))
+        pop.add_particles(xs, vs, q, m)
+        o.add_particles(xs, vs, q, m)
+    phi = rng.normal(size=mesh.n_dofs)
+    punc.Function(pop, "phi").set_local(phi)
+    assert rel(punc.particle_potential_energy_cg1(pop, punc.Function(pop, "phi")), o.potential_energy(phi)) < 1e-5
+    ne, ni = punc.density_cg1(pop, 1.0, 1.0)
+    re, ri = o.density_cg1(1.0, 1.0)
+    assert rel(ne, re) < 1e-5 and rel(ni, ri) < 1e-5
+    ne, ni = punc.density_dg0(pop, 1.0, 1.0)
+    re, ri = o.density_dg0(1.0, 1.0)
+    assert rel(ne, re) < 1e-12 and rel(ni, ri) < 1e-12
+    assert np.allclose(pop.statistics(), o.statistics(), rtol=1e-6, atol=0)

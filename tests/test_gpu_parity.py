@@ -398,3 +398,20 @@ def test_fused_cg1_steps_in_lockstep_with_oracle(lib, oracle_mod):
         ko, _ = o.inject(dt, 7, n)
         assert res.n_injected == ko
         compare_particles(pop.particles(), o.particles())
+
+
+@pytest.mark.parametrize("geom", ["probe", "periodic"])
+def test_diagnostics_match_oracle(geom, lib, oracle_mod):
+    """particle_potential_energy_cg1, density_cg1, density_dg0 and
+    Population::statistics against the oracle's sequential restatements."""
+    setup = probe_setup if geom == "probe" else periodic_setup
+    ma, mesh, pop, o, rng = setup(lib, oracle_mod)
+    phi = rng.normal(size=mesh.n_dofs)
+    punc.Function(pop, "phi").set_local(phi)
+    assert rel(punc.particle_potential_energy_cg1(pop, punc.Function(pop, "phi")), o.potential_energy(phi)) < RTOL
+    we, wi = 0.37, 2.5
+    for g, r in ((punc.density_cg1(pop, we, wi), o.density_cg1(we, wi)),
+                 (punc.density_dg0(pop, we, wi), o.density_dg0(we, wi))):
+        assert rel(g[0], r[0]) < RTOL and rel(g[1], r[1]) < RTOL
+    st_g, st_o = pop.statistics(), o.statistics()
+    assert np.all(np.abs(st_g - st_o) <= 1e-12 * np.abs(st_o)), (st_g, st_o)
