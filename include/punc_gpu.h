@@ -193,6 +193,12 @@ int pg_num_particles(pg_sim *sim, int64_t *total, int64_t *negatives, int64_t *p
 /* Download live particles ordered by (cell, particle id).  Any output may be NULL. */
 int pg_get_particles(pg_sim *sim, int64_t capacity, double *x, double *v, double *q,
                      double *m, int64_t *cell, int64_t *pid, int64_t *n_out);
+/* Population::save_file / load_file (punc/include/punc/population.h:806-878):
+ * binary = 64-byte {x[3], v[3], q, m} records, text = "%.17g" columns; cells in
+ * order, by particle id inside a cell.  Loading adds the particles (grouped by
+ * q, m) as pg_add_particles; n_added may be NULL. */
+int pg_population_save(pg_sim *sim, const char *fname, int32_t binary);
+int pg_population_load(pg_sim *sim, const char *fname, int32_t binary, int64_t *n_added);
 /* Population::locate (punc/src/population.cpp:24-39), for n points. */
 int pg_locate(pg_sim *sim, const double *xs, int64_t n, int64_t *cells);
 

@@ -19,6 +19,8 @@
 
 #include <cstddef>
 #include <cstdio>
+#include <cstdlib>
+#include <utility>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -134,6 +136,11 @@ public:
     std::size_t num_of_positives() { return counts(2); }
     // Population::statistics (population.h:746-805)
     void statistics(double *stats) { check(pg_statistics(handle, stats)); }
+    // Population::save_file / load_file (population.h:806-878)
+    void save_file(const std::string &fname, bool binary) { check(pg_population_save(handle, fname.c_str(), binary)); }
+    void load_file(const std::string &fname, bool binary) {
+        check(pg_population_load(handle, fname.c_str(), binary, nullptr));
+    }
 
     pg_sim *handle = nullptr;
     static constexpr std::size_t g_dim = 3;
@@ -216,6 +223,36 @@ inline void density_dg0(Population<3> &pop, double weight_e, double weight_i, st
                         std::vector<double> &ni) {
     check(pg_density_dg0(pop.handle, weight_e, weight_i, ne.data(), ni.data()));
 }
+
+// State (punc/src/diagnostics.cpp:40-68): the resume file.
+class State {
+public:
+    explicit State(std::string fname) : fname_(std::move(fname)) {}
+    void save(std::size_t n, double t, const ObjectVector &objects) const {
+        std::FILE *f = std::fopen(fname_.c_str(), "w");
+        if (!f) throw std::runtime_error("State: cannot open " + fname_);
+        std::fprintf(f, "%zu\t%g\t", n + 1, t);
+        for (auto &o : objects) std::fprintf(f, "%g\t%g\n", o->charge, o->current);
+        std::fclose(f);
+    }
+    void load(std::size_t &n, double &t, ObjectVector &objects) const {
+        std::FILE *f = std::fopen(fname_.c_str(), "r");
+        if (!f) throw std::runtime_error("State: cannot open " + fname_);
+        char buf[4096] = {0};
+        if (!std::fgets(buf, sizeof(buf), f)) buf[0] = 0;
+        std::fclose(f);
+        char *s = buf;
+        n = std::strtoul(s, &s, 10);
+        t = std::strtod(s, &s);
+        for (auto &o : objects) {
+            o->charge = std::strtod(s, &s);
+            o->current = std::strtod(s, &s);
+        }
+    }
+
+private:
+    std::string fname_;
+};
 
 // History (punc/src/diagnostics.cpp:70-140, diagnostics.h:119-168): the
 // history.dat preamble and rows in the reference's format.

@@ -25,6 +25,7 @@
 #include <array>
 #include <climits>
 #include <cmath>
+#include <cstdio>
 #include <cstdint>
 #include <cstring>
 #include <map>
@@ -802,6 +803,28 @@ void or_statistics(void *h, double *stats) {
         }
     if (m > 0) stats[1] = std::sqrt(stats[1] / (m - 1));
     if (n > 0) stats[3] = std::sqrt(stats[3] / (n - 1));
+}
+
+// Population::save_file (punc/include/punc/population.h:806-837).
+int32_t or_save_population(void *h, const char *fname, int32_t binary) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    std::FILE *fout = std::fopen(fname, binary ? "wb" : "w");
+    if (!fout) return 1;
+    for (const Cell &cell : o.cells)
+        for (const auto &particle : cell.particles) {
+            if (binary) {
+                const double rec[8] = {particle.x[0], particle.x[1], particle.x[2], particle.v[0],
+                                       particle.v[1], particle.v[2], particle.q,    particle.m};
+                std::fwrite(rec, sizeof(rec), 1, fout);
+            } else {
+                for (int i = 0; i < 3; ++i) std::fprintf(fout, "%.17g\t", particle.x[i]);
+                for (int i = 0; i < 3; ++i) std::fprintf(fout, "%.17g\t", particle.v[i]);
+                std::fprintf(fout, "%.17g\t %.17g\t", particle.q, particle.m);
+                std::fprintf(fout, "\n");
+            }
+        }
+    std::fclose(fout);
+    return 0;
 }
 
 // move / move_periodic (punc/include/punc/pusher.h:648-681).

@@ -38,6 +38,7 @@ _SIG = {
     "or_accel": ([C.c_void_p, _D, C.c_double, C.c_int32], C.c_double),
     "or_esolver_rhs": ([C.c_void_p, _D, _D], None),
     "or_potential_energy": ([C.c_void_p, _D], C.c_double),
+    "or_save_population": ([C.c_void_p, C.c_char_p, C.c_int32], C.c_int32),
     "or_density_cg1": ([C.c_void_p, C.c_double, C.c_double, _D, _D], None),
     "or_density_dg0": ([C.c_void_p, C.c_double, C.c_double, _D, _D], None),
     "or_statistics": ([C.c_void_p, _D], None),
@@ -184,6 +185,9 @@ class Oracle:
         _, M = self.matrices()
         lu = spla.splu(M.tocsc())
         return np.ascontiguousarray(np.stack([lu.solve(b[:, c]) for c in range(3)], axis=1))
+
+    def save_file(self, fname, binary=True):
+        assert lib().or_save_population(self.h, str(fname).encode(), 1 if binary else 0) == 0
 
     def potential_energy(self, phi):
         return float(lib().or_potential_energy(self.h, _d(np.ascontiguousarray(phi, float))))

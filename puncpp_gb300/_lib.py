@@ -142,6 +142,8 @@ SIGNATURES = {
     "pg_launch_count": ([_I64], C.c_int),
     "pg_esolver_solve": ([_P, _D, C.POINTER(SolveInfo)], C.c_int),
     "pg_potential_energy": ([_P, _D], C.c_int),
+    "pg_population_save": ([_P, C.c_char_p, C.c_int32], C.c_int),
+    "pg_population_load": ([_P, C.c_char_p, C.c_int32, _I64], C.c_int),
     "pg_density_cg1": ([_P, C.c_double, C.c_double, _D, _D], C.c_int),
     "pg_density_dg0": ([_P, C.c_double, C.c_double, _D, _D], C.c_int),
     "pg_statistics": ([_P, _D], C.c_int),

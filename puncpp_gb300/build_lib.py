@@ -37,7 +37,7 @@ CU_UNITS = {
     "k_esolve.cu": ["--fmad=true"],
     "k_diag.cu": [],
 }
-CPP_UNITS = ["mesh_tables.cpp", "amg.cpp"]
+CPP_UNITS = ["mesh_tables.cpp", "amg.cpp", "checkpoint.cpp"]
 
 
 def _nvcc() -> str:

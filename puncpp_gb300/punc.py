@@ -170,6 +170,17 @@ class Population:
     def num_of_positives(self) -> int:
         return self._counts()[2]
 
+    def save_file(self, fname: str, binary: bool = True):
+        """Population::save_file (punc/include/punc/population.h:806-837)."""
+        L.check(L.load().pg_population_save(self.handle, str(fname).encode(), 1 if binary else 0))
+
+    def load_file(self, fname: str, binary: bool = True) -> int:
+        """Population::load_file (punc/include/punc/population.h:839-878); returns
+        the number of particles added."""
+        n = C.c_int64()
+        L.check(L.load().pg_population_load(self.handle, str(fname).encode(), 1 if binary else 0, C.byref(n)))
+        return n.value
+
     def statistics(self) -> np.ndarray:
         """Population::statistics (punc/include/punc/population.h:746-805): mean
         speed and sample standard deviation of the negative, then the positive
@@ -312,6 +323,34 @@ def density_dg0(pop: Population, weight_e: float, weight_i: float):
     ne, ni = np.zeros(pop.num_cells), np.zeros(pop.num_cells)
     L.check(L.load().pg_density_dg0(pop.handle, weight_e, weight_i, L.dptr(ne), L.dptr(ni)))
     return ne, ni
+
+
+class State:
+    """State (punc/src/diagnostics.cpp:40-68): the resume file holding the next
+    step number, the time and each object's charge and current, written with
+    the default stream format (six significant digits)."""
+
+    def __init__(self, fname: str):
+        self.fname = str(fname)
+
+    def save(self, n: int, t: float, objects):
+        with open(self.fname, "w") as f:
+            f.write(f"{n + 1}\t{t:g}\t")
+            for o in objects:
+                f.write(f"{o.charge:g}\t{o.current:g}\n")
+
+    def load(self, objects):
+        """Returns (n, t) and sets each object's charge and current from the
+        first line, as the reference parses it (objects whose values are not
+        on that line get 0)."""
+        with open(self.fname) as f:
+            tok = f.readline().split()
+        n, t = int(tok[0]), float(tok[1])
+        vals = [float(x) for x in tok[2:]]
+        for k, o in enumerate(objects):
+            o.charge = vals[2 * k] if 2 * k < len(vals) else 0.0
+            o.current = vals[2 * k + 1] if 2 * k + 1 < len(vals) else 0.0
+        return n, t
 
 
 class History:

@@ -37,3 +37,15 @@ def test_history_preamble_and_rows(tmp_path):
     h.close()
     lines = f.read_text().split("\n")
     assert lines[5].startswith("8\t4.0000000000000002e-01") and lines[6] == ""
+
+
+def test_state_file_round_trip(tmp_path):
+    """State::save / load (punc/src/diagnostics.cpp:40-68): next step, time,
+    charge and current of the object, default stream precision."""
+    f = tmp_path / "state.dat"
+    objs = [_Obj(0.0, 0.125, 3.5)]
+    punc.State(f).save(41, 2.05, objs)
+    assert f.read_text() == "42\t2.05\t3.5\t0.125\n"
+    back = [_Obj(0.0, 0.0, 0.0)]
+    n, t = punc.State(f).load(back)
+    assert (n, t, back[0].charge, back[0].current) == (42, 2.05, 3.5, 0.125)
