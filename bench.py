@@ -134,7 +134,8 @@ def run_ours(args):
     mesh = punc.Mesh(ma)
     prec = L.PG_MIXED if args.precision == "mixed" else L.PG_FP64
     pop = punc.Population(mesh, precision=prec, capacity=int(2.6 * args.n_per * 2), pcg_rtol=RTOL, pcg_atol=ATOL,
-                          pcg_max_iter=4000, pcg_precond=PRECONDS[args.pcg_precond])
+                          pcg_max_iter=4000, pcg_precond=PRECONDS[args.pcg_precond],
+                          warm_start=2 if args.warm_start == "extrapolate" else 1)
     for s, (x, v) in zip(species, loads):
         pop.add_particles(x, v, s["q"], s["m"])
     sp = [punc.Species(s["q"], s["m"], n=s["n"], vth=s["vth"]) for s in species]
@@ -158,35 +159,70 @@ def run_ours(args):
 
     for k in range(max(3, args.warmup)):
         one(first=(k == 0))
+    cg1 = args.efield == "cg1"
+    graph = args.step_mode == "graph"
+    if args.step_mode != "staged":
+        # capture the step graph (and run one more warm-up step) outside the timed region
+        rs = punc.run_steps(pop, objs, DT, 1, inject=True, seed=0x5EED0002, step_no=step_no, efield_cg1=cg1,
+                            use_graph=graph)
+        step_no += 1
+        n_now = rs[-1].n_particles
     L.check(lib.pg_synchronize(pop.handle))
-    punc.set_profiling(pop, True)
-    punc.stage_times(pop)  # reset
     launches0 = launch_count()
     pushed_total = 0
     iters = 0
     with ClockSampler() as clk:
         L.check(lib.pg_event_record(pop.handle, 0))
         t_wall = time.perf_counter()
-        for _ in range(args.steps):
-            r, pushed = one()
-            pushed_total += pushed
-            iters += r.pcg_iterations
+        if args.step_mode == "staged":
+            punc.set_profiling(pop, True)
+            punc.stage_times(pop)  # reset
+            for _ in range(args.steps):
+                r, pushed = one()
+                pushed_total += pushed
+                iters += r.pcg_iterations
+        else:
+            rs = punc.run_steps(pop, objs, DT, args.steps, inject=True, seed=0x5EED0002, step_no=step_no,
+                                efield_cg1=cg1, use_graph=graph)
+            step_no += args.steps
+            pushed_total = n_now + sum(r.n_particles for r in rs[:-1])
+            n_now = rs[-1].n_particles
+            iters = sum(r.pcg_iterations for r in rs)
         L.check(lib.pg_event_record(pop.handle, 1))
         ms = ctypes_ms(lib, pop, 0, 1)
         t_wall = time.perf_counter() - t_wall
     launches = launch_count() - launches0
-    stages = punc.stage_times(pop)
-    punc.set_profiling(pop, False)
+    if args.step_mode == "staged":
+        prof_steps = args.steps
+        stages = punc.stage_times(pop)
+        punc.set_profiling(pop, False)
+    else:
+        # stage shares from a separate profiled pass of staged steps (not timed)
+        prof_steps = min(args.steps, 10)
+        punc.set_profiling(pop, True)
+        punc.stage_times(pop)
+        prof_iters = 0
+        for _ in range(prof_steps):
+            r, _ = one()
+            prof_iters += r.pcg_iterations
+        stages = punc.stage_times(pop)
+        punc.set_profiling(pop, False)
     value = pushed_total / (ms / 1e3)
 
-    # e2e: the same steps through the C ABI with the step's outputs read back to
-    # host memory each step (potential, plus the history row in the result)
+    # e2e: step by step through the C ABI, each step's outputs read back to host
+    # memory (potential, objects, the result row)
     phi_host = np.zeros(mesh.n_dofs)
     L.check(lib.pg_synchronize(pop.handle))
     e2e_pushed = 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        r, pushed = one()
+        if args.step_mode == "staged":
+            r, pushed = one()
+        else:
+            r = punc.run_steps(pop, objs, DT, 1, inject=True, seed=0x5EED0002, step_no=step_no, efield_cg1=cg1,
+                               use_graph=graph)[0]
+            step_no += 1
+            pushed, n_now = n_now, r.n_particles
         e2e_pushed += pushed
         L.check(lib.pg_get_phi(pop.handle, L.dptr(phi_host)))
     L.check(lib.pg_synchronize(pop.handle))
@@ -194,6 +230,9 @@ def run_ours(args):
     import ctypes as C
     h2d = C.sizeof(L.StepArgs) + C.sizeof(L.Object) * len(objs)
     d2h = phi_host.nbytes + C.sizeof(L.StepResult) + C.sizeof(L.Object) * len(objs)
+    if args.step_mode != "staged":
+        h2d += 4 * 8 + 32 * len(objs)                   # device counters and object state
+        d2h += 4 * 8 + 32 * len(objs) + 8 * (6 + 3 * len(objs)) + 8
 
     # roofline of the dominant stage
     hbm, src = peaks()
@@ -202,8 +241,10 @@ def run_ours(args):
     nnz = lay["nnz"]
     n_avg = pushed_total / args.steps
     occ = nc * (1.0 - math.exp(-n_avg / nc))
-    part_ms = stages.get("push_move_update_deposit", 0.0)
-    pcg_ms = stages.get("pcg", 0.0)
+    # stage times of the profiled steps, scaled to the timed steps
+    sc = args.steps / max(1, prof_steps)
+    part_ms = stages.get("push_move_update_deposit", 0.0) * sc
+    pcg_ms = stages.get("pcg", 0.0) * sc
     mixed = args.precision == "mixed"
     # algorithmic bytes: particle pass per particle / occupied cell / dof,
     # PCG per iteration per nonzero / dof
@@ -232,9 +273,10 @@ def run_ours(args):
                   else "k_pcg (FP64 Jacobi PCG, one cooperative launch per solve)")
     r_pcg = roof_of(pcg_kernel, iters * kb, pcg_ms, kmodel)
     roof = r_pcg if pcg_ms >= part_ms else r_part
-    stages_share = {k: round(v / ms, 4) for k, v in stages.items()}
+    per_step = {k: v / max(1, prof_steps) for k, v in stages.items()}
+    stages_share = {k: round(v / (ms / args.steps), 4) for k, v in per_step.items()}
     # the particle stages alone (push + move + relocate + deposit, injection, charge finalise)
-    part_stage_ms = sum(stages.get(k, 0.0) for k in ("push_move_update_deposit", "injector", "distributor"))
+    part_stage_ms = sum(per_step.get(k, 0.0) for k in ("push_move_update_deposit", "injector", "distributor")) * args.steps
     particle_stages = {"value": round(pushed_total / (part_stage_ms / 1e3), 1) if part_stage_ms > 0 else None,
                        "unit": UNIT, "ms_per_step": round(part_stage_ms / args.steps, 4),
                        "stages": ["push_move_update_deposit", "injector", "distributor"]}
@@ -246,12 +288,15 @@ def run_ours(args):
         "precision_form": args.precision,
         "data": "synthetic: seeded uniform/Maxwellian particles on a generated Kuhn probe mesh (no dataset)",
         "config": {"workload": workload_name(args.n_side, args.n_per), "precision": args.precision,
-                   "pcg_precond": args.pcg_precond, "efield": args.efield, "cells": nc, "dofs": nv, "nnz": nnz,
+                   "pcg_precond": args.pcg_precond, "warm_start": args.warm_start, "efield": args.efield,
+                   "step_mode": args.step_mode, "cells": nc, "dofs": nv, "nnz": nnz,
                    "amg_levels": [[v["rows"], v["nnz"]] for v in lay["levels"]], "particles_initial": n0,
                    "particles_mean_pushed": round(n_avg), "pcg_iterations_per_step": round(iters / args.steps, 1),
                    "l2": "inputs larger than L2 (particle SoA ~250 MB, mesh tables ~0.9 GB)"},
         "particle_stages": particle_stages,
-        "stage_ms": {k: round(v, 3) for k, v in stages.items()}, "stage_share": stages_share,
+        "stage_ms_per_step": {k: round(v, 4) for k, v in per_step.items()},
+        "stage_share": stages_share, "stage_source": ("the timed steps" if args.step_mode == "staged"
+                                                      else f"{prof_steps} staged pg_step steps after the timed ones"),
         "roofline": roof, "roofline_particles": r_part, "roofline_pcg": r_pcg,
         "e2e": {"value": round(e2e_pushed / e2e_s, 1), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
@@ -395,6 +440,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="probe-80", help="probe-N: N^3 sub-cubes, particles scaled by (N/80)^3")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--step-mode", default="graph", choices=["graph", "stream", "staged"],
+                    help="graph: pg_run_steps replaying a captured CUDA graph; stream: pg_run_steps without the "
+                         "graph; staged: pg_step per step with stage timing")
+    ap.add_argument("--warm-start", default="prev", choices=["prev", "extrapolate"],
+                    help="PCG start: the previous potential, or 2 phi_n - phi_(n-1)")
     ap.add_argument("--efield", default="dg0", choices=["dg0", "cg1"],
                     help="field path: EFieldDG0 + accel/boris, or ESolver (CG1) + accel_cg1/boris_cg1")
     ap.add_argument("--pcg-precond", default="amg", choices=sorted(PRECONDS),

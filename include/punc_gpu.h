@@ -85,7 +85,8 @@ typedef struct pg_config {
     double pcg_rtol;            /* 0: 1e-12, PoissonSolver default (punc/src/poisson.cpp:326-328) */
     double pcg_atol;            /* 0: 1e-14 */
     int32_t pcg_max_iter;       /* 0: 1000 */
-    int32_t pcg_warm_start;     /* 1: start PCG from the previous potential */
+    int32_t pcg_warm_start;     /* 1: start PCG from the previous potential; 2: from the linear
+                                   extrapolation 2 phi_n - phi_(n-1) of the last two */
     double ext_E[3];            /* exterior Dirichlet value phi = x . ext_E (PhiBoundary) */
     int32_t circuit_resolve;    /* 1: CircuitCM correction by a second solve, as the reference
                                    (punc/src/poisson.cpp:373-375); 0: by superposition of the
@@ -253,6 +254,16 @@ int pg_inject(pg_sim *sim, double dt, uint64_t seed, uint64_t step, int64_t *n_i
  * circuit, E field (interaction/interaction.cpp:342-480). */
 int pg_step(pg_sim *sim, const pg_step_args *args, pg_object *objects, int32_t n_objects,
             pg_step_result *result);
+/* n_steps fused timesteps, as n_steps calls of pg_step (same operations and
+ * arithmetic; args->step is the first step's RNG counter, incremented per
+ * step; args->first_step applies to the first of them), with the particle
+ * counts, object charges, currents and potentials and the CircuitCM post-solve
+ * kept on the device: no host synchronisation until the end.  use_graph = 1
+ * captures a step as a CUDA graph once (per particle buffer and arguments)
+ * and replays it.  Cell sorts every sort_interval steps run in between.
+ * results (optional): [n_steps]. */
+int pg_run_steps(pg_sim *sim, const pg_step_args *args, pg_object *objects, int32_t n_objects,
+                 int32_t n_steps, int32_t use_graph, pg_step_result *results);
 /* Sort particles by cell and drop absorbed slots. */
 int pg_sort(pg_sim *sim);
 

@@ -133,6 +133,8 @@ SIGNATURES = {
     "pg_inject": ([_P, C.c_double, C.c_uint64, C.c_uint64, _I64], C.c_int),
     "pg_step": ([_P, C.POINTER(StepArgs), C.POINTER(Object), C.c_int32, C.POINTER(StepResult)], C.c_int),
     "pg_sort": ([_P], C.c_int),
+    "pg_run_steps": ([_P, C.POINTER(StepArgs), C.POINTER(Object), C.c_int32, C.c_int32, C.c_int32,
+                      C.POINTER(StepResult)], C.c_int),
     "pg_stage_times": ([_P, _D, C.c_int32, _I32], C.c_int),
     "pg_stage_name": ([_P, C.c_int32], C.c_char_p),
     "pg_set_profiling": ([_P, C.c_int32], C.c_int),

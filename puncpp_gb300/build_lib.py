@@ -36,6 +36,7 @@ CU_UNITS = {
     "k_amg.cu": [],
     "k_esolve.cu": ["--fmad=true"],
     "k_diag.cu": [],
+    "k_step.cu": [],
 }
 CPP_UNITS = ["mesh_tables.cpp", "amg.cpp", "checkpoint.cpp"]
 

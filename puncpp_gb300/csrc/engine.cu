@@ -45,6 +45,9 @@ struct pg_sim {
     double *A_val = nullptr, *A_dinv = nullptr, *M_val = nullptr;
     double *phi0 = nullptr;                    // zero-potential solution (superposition mode)
     bool phi0_valid = false;
+    double *x_prev = nullptr;                  // previous PCG solution (pcg_warm_start == 2)
+    const double *x_prev_of = nullptr;         // the solution vector x_prev belongs to
+    int x_prev_count = 0;                      // solutions seen for that vector (0, 1, 2+)
     double *lap = nullptr;                     // [n_obj][ndof] unit-potential Laplace solutions
     int32_t *bc_kind = nullptr;
     double *bc_value = nullptr, *w_ext = nullptr, *w_obj = nullptr;
@@ -70,6 +73,19 @@ struct pg_sim {
     int32_t *es_out_i = nullptr;
     double *Ev = nullptr;
     float *Evf = nullptr;
+
+    // multi-step runs (pg_run_steps): device counters [slots, next id, RNG
+    // step, result row], objects [n][charge, current, potential, -], tags,
+    // current sources, circuit matrices, result rows, captured step graphs
+    int64_t *run_counts = nullptr, *run_tags = nullptr;
+    double *run_obj = nullptr, *run_isrc = nullptr, *run_rows = nullptr;
+    int64_t run_rows_cap = 0;
+    CircuitDev circ_dev{};
+    bool circ_dev_ready = false;
+    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};   // one per particle buffer
+    std::string graph_key[2];
+    int64_t graph_cap[2] = {0, 0};
+    long long graph_launches = 0;                          // kernels per captured step
 
     // diagnostics scratch (allocated on first use)
     double *diag_a = nullptr, *diag_b = nullptr, *diag_acc = nullptr;
@@ -492,7 +508,20 @@ static int poisson_solve_internal(pg_sim *s, const double *pot_h, bool zero_rho,
     if (zero_rho) s->rho_valid = false;
     double *x = x_target ? x_target : s->phi;
     bool *valid = warm ? warm : &s->phi_valid;
-    if (!(s->cfg.pcg_warm_start && *valid) || zero_rho) PG_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * s->ndof, s->stream));
+    if (!(s->cfg.pcg_warm_start && *valid) || zero_rho) {
+        PG_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * s->ndof, s->stream));
+        if (s->x_prev_of == x) s->x_prev_count = 0;
+    } else if (s->cfg.pcg_warm_start == 2) {
+        // start from the linear extrapolation of the last two solutions
+        if (!s->x_prev) {
+            int rc = dalloc(s, &s->x_prev, s->ndof);
+            if (rc) return rc;
+        }
+        if (s->x_prev_of != x) { s->x_prev_of = x; s->x_prev_count = 0; }
+        if (s->x_prev_count >= 1) launch_extrapolate(x, s->x_prev, s->ndof, s->stream);
+        else PG_CUDA(cudaMemcpyAsync(s->x_prev, x, sizeof(double) * s->ndof, cudaMemcpyDeviceToDevice, s->stream));
+        ++s->x_prev_count;
+    }
     launch_set_bc(s->bc_kind, use_ext ? s->bc_value : nullptr, s->obj_pot, s->ndof, x, s->stream);
     PcgArgs a{};
     a.n = s->ndof;
@@ -1032,6 +1061,8 @@ int pg_create(const pg_mesh *mesh, const pg_config *cfg_in, pg_sim **out) {
 int pg_destroy(pg_sim *s) {
     if (!s) return PG_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
+    for (auto &g : s->graph_exec)
+        if (g) cudaGraphExecDestroy(g);
     for (void *p : s->allocs) cudaFree(p);
     free_particles(s->P[0]);
     free_particles(s->P[1]);
@@ -1713,6 +1744,354 @@ int pg_inject(pg_sim *s, double dt, uint64_t seed, uint64_t step, int64_t *n_inj
 int pg_sort(pg_sim *s) {
     if (!s) return fail(PG_ERR_ARG, "NULL handle");
     return do_sort(s);
+}
+
+// ---- multi-step runs: the step on the device only ------------------------
+
+// rhs, boundary values and one PCG launch into x; object potentials are read
+// from s->obj_pot on the device; no status read-back.
+static int pcg_enqueue(pg_sim *s, double *x) {
+    launch_rhs(s->dm, s->M_row, s->M_col, s->M_val, s->rho, s->bc_kind, s->bc_value, s->w_ext, s->w_obj, s->obj_pot,
+               s->n_obj, 1, s->b, s->stream);
+    launch_set_bc(s->bc_kind, s->bc_value, s->obj_pot, s->ndof, x, s->stream);
+    PcgArgs a{};
+    a.n = s->ndof;
+    a.slice_ptr = s->A_sptr; a.slice_width = s->A_swidth; a.col = s->A_col; a.val = s->A_val; a.dinv = s->A_dinv;
+    a.b = s->b; a.x = x; a.r = s->r; a.z = s->z; a.p0 = s->p0; a.p1 = s->p1; a.Ap = s->Ap;
+    a.partials = s->pcg_part;
+    a.rtol = s->cfg.pcg_rtol; a.atol = s->cfg.pcg_atol;
+    a.max_iter = s->cfg.pcg_max_iter;
+    a.remove_mean = s->cfg.periodic ? 1 : 0;
+    a.out_iter = s->pcg_out_i; a.out_status = s->pcg_out_i + 1;
+    a.out_rr = s->pcg_out_d; a.out_bb = s->pcg_out_d + 1;
+    a.val32 = s->A_val32; a.dinv32 = s->A_dinv32;
+    a.r32 = s->r32; a.z32 = s->z32; a.p32 = s->p32; a.Ap32 = s->Ap32;
+    a.out_updates = nullptr;
+    const int e = s->use_amg ? launch_pcg_amg(a, s->amg, s->stream) : launch_pcg(a, s->stream);
+    if (e) return fail(PG_ERR_CUDA, std::string("cooperative PCG launch: ") + cudaGetErrorString((cudaError_t)e));
+    return PG_OK;
+}
+
+// Per-step injection bound: sum over species of ceil(n dt sum_j flux_j) + facets.
+static int64_t inject_bound(const pg_sim *s, double dt) {
+    int64_t bound = 0;
+    for (int k = 0; k < s->n_inj_species; ++k)
+        bound += (int64_t)std::ceil(s->flux_sum_h[k] * s->inj[k].n * dt) + s->n_ext;
+    return bound;
+}
+
+// Injection with the slot base, id base and RNG step read from run_counts,
+// depositing into this step's accumulator; counters advanced on the device.
+static void inject_enqueue(pg_sim *s, const DevParticles &Pd, double dt, uint64_t seed) {
+    const int total = s->n_inj_species * s->n_ext;
+    if (total == 0) return;
+    InjectParams ip{};
+    ip.n_species = s->n_inj_species;
+    ip.n_facets = s->n_ext;
+    ip.seed = seed;
+    ip.dt = dt;
+    for (int k = 0; k < s->n_inj_species; ++k) {
+        const pg_species &S = s->inj[k];
+        InjectSpecies &I = ip.sp[k];
+        I.ndt = S.n * dt;
+        const double range = S.vdf_range > 0 ? S.vdf_range : 5.0;
+        for (int c = 0; c < 3; ++c) {
+            const double lo = S.vd[c] - range * S.vth, hi = S.vd[c] + range * S.vth;
+            I.domain_lo[c] = lo;
+            I.domain_w[c] = hi - lo;
+            I.vd[c] = S.vd[c];
+        }
+        I.vth2 = S.vth * S.vth;
+        I.factor = 1.0 / std::pow(std::sqrt(2. * M_PI * I.vth2), 3);
+        I.q = S.q;
+    }
+    ip.counts_dev = s->run_counts;
+    ip.rho_fixed = s->rho_fixed;
+    const double unit = fixed_unit(s);
+    for (int k = 0; k < s->n_species; ++k) ip.q_scaled[k] = (float)(s->q[k] / unit);
+    cudaMemsetAsync(s->inj_counts, 0, sizeof(int64_t) * (total + 1), s->stream);
+    cudaMemsetAsync(s->state->injected, 0, sizeof(s->state->injected), s->stream);
+    launch_inject_count(s->dm, ip, s->flux_num, s->inj_counts, s->stream);
+    launch_scan_i64(s->inj_counts, s->inj_offsets, total + 1, s->scan_tmp, s->stream);
+    launch_inject_generate(s->dm, Pd, ip, s->flux_num, s->pdf_max, s->d_ext_facets, s->inj_offsets,
+                           s->cfg.max_walk_steps, 1, s->d_q, s->rho_acc, s->state, inject_bound(s, dt), s->stream);
+    launch_inject_commit(s->run_counts, s->state, s->stream);
+}
+
+// One whole step on the stream, no host synchronisation: the same operations
+// and arithmetic as pg_step, with counts, objects and the circuit on the device.
+static int enqueue_step(pg_sim *s, const pg_step_args *a, bool first) {
+    DevParticles Pd = s->P[s->cur];
+    Pd.n_dev = s->run_counts;
+    const int64_t cap = Pd.capacity;
+    rho_from_acc(s);
+    int rc;
+    if (s->circuit_ready) {
+        launch_circuit_pre(s->run_isrc, (int)s->isrc.size(), s->circ_dt, s->n_obj, s->run_obj, s->obj_pot, s->stream);
+        const bool superpose = !s->cfg.circuit_resolve && s->lap;
+        if ((rc = pcg_enqueue(s, superpose ? s->phi0 : s->phi))) return rc;
+        launch_image_charge(s->dm, superpose ? s->phi0 : s->phi, s->d_ofacets, s->n_ofac, s->n_obj, s->cfg.eps0,
+                            s->image, s->stream);
+        launch_circuit_post(s->circ_dev, s->image, s->run_obj, s->obj_pot, s->stream);
+        if (superpose) launch_superpose_dev(s->phi0, s->lap, s->obj_pot, s->n_obj, s->ndof, s->phi, s->stream);
+        else if ((rc = pcg_enqueue(s, s->phi))) return rc;
+    } else {
+        if ((rc = pcg_enqueue(s, s->phi))) return rc;
+    }
+    if (a->efield_cg1) {
+        EsolveArgs e{};
+        const double zero[3] = {0, 0, 0};
+        launch_efield(s->dm, s->phi, zero, s->stream);
+        e.n = s->ndof;
+        e.fp32 = is_mixed(s) ? 1 : 0;
+        e.adj_ptr = s->es_adj_ptr; e.adj_cell = s->es_adj_cell; e.vol = s->es_vol; e.E_cell = s->dm.E;
+        e.row = s->M_row; e.col = s->M_col; e.val = s->M_val; e.dinv = s->M_dinv;
+        e.val32 = s->M_val32; e.dinv32 = s->M_dinv32;
+        const size_t n3 = 3 * (size_t)s->ndof;
+        if (e.fp32) {
+            float *b = s->es_buf32;
+            e.b32 = b; e.x32 = b + n3; e.r32 = b + 2 * n3; e.z32 = b + 3 * n3; e.p32 = b + 4 * n3; e.Ap32 = b + 5 * n3;
+            e.rtol = 1e-6;
+        } else {
+            double *b = s->es_buf;
+            e.b = b; e.x = b + n3; e.r = b + 2 * n3; e.z = b + 3 * n3; e.p = b + 4 * n3; e.Ap = b + 5 * n3;
+            e.rtol = 1e-12;
+        }
+        e.atol = 1e-14;
+        e.max_iter = 1000;
+        e.partials = s->es_part;
+        e.out_iter = s->es_out_i; e.out_status = s->es_out_i + 1;
+        e.out_rr = s->es_out_d; e.out_bb = s->es_out_d + 3;
+        for (int j = 0; j < 3; ++j) e.E0[j] = a->E0[j];
+        e.ev = s->Ev;
+        e.evf = s->Evf;
+        const int err = launch_esolve(e, s->stream);
+        if (err) return fail(PG_ERR_CUDA, std::string("ESolver launch: ") + cudaGetErrorString((cudaError_t)err));
+    } else {
+        launch_efield(s->dm, s->phi, a->E0, s->stream);
+    }
+    const double dt_push = first ? 0.5 * a->dt : a->dt;
+    cudaMemsetAsync(s->state->absorbed, 0, sizeof(s->state->absorbed), s->stream);
+    if (is_mixed(s)) {
+        cudaMemsetAsync(s->rho_fixed, 0, sizeof(unsigned long long) * s->ndof, s->stream);
+        MixedParams xp;
+        fill_mixed(s, xp, dt_push, a->B, a->use_accel != 0, a->dt, a->periodic_move != 0, a->Ld);
+        xp.cg1 = a->efield_cg1 ? 1 : 0;
+        launch_mixed_pass(s->dm, Pd, cap, xp, true, true, true, true, s->cfg.max_walk_steps, s->rho_fixed, s->state,
+                          s->partials, s->n_part, s->ke_dev, s->stream);
+    } else {
+        cudaMemsetAsync(s->rho_acc, 0, sizeof(double) * s->ndof, s->stream);
+        PushParams pp;
+        fill_push(s, pp, dt_push, a->B, a->use_accel != 0);
+        pp.cg1 = a->efield_cg1 ? 1 : 0;
+        MoveParams mp{};
+        mp.dt = a->dt;
+        mp.periodic = a->periodic_move;
+        for (int j = 0; j < 3; ++j) mp.Ld[j] = a->Ld[j];
+        launch_fused_step(s->dm, Pd, cap, pp, mp, s->cfg.max_walk_steps, s->d_q, s->rho_acc, s->state, s->partials,
+                          s->n_part, s->ke_dev, s->stream);
+    }
+    launch_objects_update(s->state, s->d_q, s->n_species, s->run_tags, s->n_obj, s->run_obj, a->dt, s->stream);
+    if (a->inject) inject_enqueue(s, Pd, a->dt, a->seed);
+    else cudaMemsetAsync(s->state->injected, 0, sizeof(s->state->injected), s->stream);
+    launch_step_record(s->run_rows, 6 + 3 * s->n_obj, s->run_counts, s->ke_dev, s->state, s->n_species, s->pcg_out_i,
+                       s->pcg_out_d, s->run_obj, s->n_obj, s->stream);
+    return PG_OK;
+}
+
+// Cell sort on the device with the counts of a run (no read-back).
+static void sort_enqueue(pg_sim *s) {
+    const int other = 1 - s->cur;
+    DevParticles Pd = s->P[s->cur];
+    Pd.n_dev = s->run_counts;
+    cudaMemsetAsync(s->sort_hist, 0, sizeof(int64_t) * (s->nc + 1), s->stream);
+    launch_sort_hist(Pd, Pd.capacity, s->sort_hist, s->stream);
+    launch_scan_i64(s->sort_hist, s->sort_cursor, s->nc + 1, s->scan_tmp, s->stream);
+    launch_sort_scatter(Pd, s->P[other], Pd.capacity, s->sort_cursor, s->stream);
+    launch_set_count(s->run_counts, s->sort_cursor, s->nc, s->stream);
+    s->cur = other;
+}
+
+static void drop_graphs(pg_sim *s) {
+    for (int k = 0; k < 2; ++k) {
+        if (s->graph_exec[k]) cudaGraphExecDestroy(s->graph_exec[k]);
+        s->graph_exec[k] = nullptr;
+        s->graph_key[k].clear();
+    }
+}
+
+// Device copies of the circuit matrices and groups (once per circuit set-up).
+static int upload_circuit(pg_sim *s) {
+    if (s->circ_dev_ready || !s->circuit_ready) return PG_OK;
+    const int n = s->n_obj;
+    std::vector<int32_t> gp{0}, gm, fp{0}, fm;
+    for (auto &g : s->groups) { for (int v : g) gm.push_back(v); gp.push_back((int32_t)gm.size()); }
+    for (auto &f : s->fixed_voltage) { for (int v : f) fm.push_back(v); fp.push_back((int32_t)fm.size()); }
+    int32_t *d_gp, *d_gm, *d_fp, *d_fm;
+    double *d_ic, *d_icc, *d_cv;
+    int rc;
+    if ((rc = upload(s, &d_gp, gp)) || (rc = upload(s, &d_gm, gm)) || (rc = upload(s, &d_fp, fp)) ||
+        (rc = upload(s, &d_fm, fm)) || (rc = upload(s, &d_ic, s->inv_cap)) || (rc = upload(s, &d_icc, s->inv_circ)) ||
+        (rc = upload(s, &d_cv, s->circ_vec)))
+        return rc;
+    CircuitDev &c = s->circ_dev;
+    c.n = n;
+    c.n_groups = (int32_t)s->groups.size();
+    c.n_fv = (int32_t)s->fixed_voltage.size();
+    c.g_ptr = d_gp; c.g_mem = d_gm; c.f_ptr = d_fp; c.f_mem = d_fm;
+    c.inv_cap = d_ic; c.inv_circ = d_icc; c.cv = d_cv;
+    std::vector<double> isrc;
+    for (auto &x : s->isrc) { isrc.push_back(x.node_a); isrc.push_back(x.node_b); isrc.push_back(x.value); }
+    if ((rc = upload(s, &s->run_isrc, isrc))) return rc;
+    s->circ_dev_ready = true;
+    return PG_OK;
+}
+
+int pg_run_steps(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_objects, int32_t n_steps,
+                 int32_t use_graph, pg_step_result *results) {
+    if (!s || !a || n_steps < 0 || (n_objects > 0 && !objects)) return fail(PG_ERR_ARG, "pg_run_steps: bad arguments");
+    if (n_steps == 0) return PG_OK;
+    const int n = s->n_obj;
+    std::vector<int> map(n, -1);
+    for (int k = 0; k < n_objects; ++k) {
+        const int i = object_index(s, objects[k].bnd_id);
+        if (i >= 0) map[i] = k;
+    }
+    if (s->circuit_ready)
+        for (int i = 0; i < n; ++i)
+            if (map[i] < 0) return fail(PG_ERR_ARG, "pg_run_steps: the circuit needs every object of the mesh");
+    if (a->inject && !s->flux_ready) return fail(PG_ERR_STATE, "pg_run_steps: call pg_create_flux first");
+    int rc;
+    if (!s->run_counts) {
+        if ((rc = dalloc(s, &s->run_counts, 4)) || (rc = dalloc(s, &s->run_obj, 4 * (size_t)std::max(1, n))) ||
+            (rc = dalloc(s, &s->run_tags, (size_t)std::max(1, n))))
+            return rc;
+        std::vector<int64_t> tags(std::max(1, n), 0);
+        for (int i = 0; i < n; ++i) tags[i] = i + 2;
+        PG_CUDA(cudaMemcpy(s->run_tags, tags.data(), sizeof(int64_t) * tags.size(), cudaMemcpyHostToDevice));
+    }
+    if ((rc = upload_circuit(s))) return rc;
+    const int row_len = 6 + 3 * n;
+    if (s->run_rows_cap < (int64_t)n_steps * row_len) {
+        if ((rc = dalloc(s, &s->run_rows, (size_t)n_steps * row_len))) return rc;
+        s->run_rows_cap = (int64_t)n_steps * row_len;
+    }
+    // capacity for the injections between two sorts, and scan scratch
+    const int per_chunk = std::min(n_steps, std::max(1, s->cfg.sort_interval));
+    const int64_t grow = a->inject ? inject_bound(s, a->dt) * per_chunk : 0;
+    const int64_t cap_before = s->P[0].capacity;
+    if ((rc = ensure_capacity(s, s->n_slots + grow))) return rc;
+    if (s->P[0].capacity != cap_before) drop_graphs(s);
+    if (a->inject && (rc = ensure_scan_tmp(s, s->n_inj_species * s->n_ext + 1))) return rc;
+    // device state: counts, objects, potentials of fixed-potential objects
+    const int64_t counts[4] = {s->n_slots, s->next_pid, (int64_t)a->step, 0};
+    PG_CUDA(cudaMemcpyAsync(s->run_counts, counts, sizeof(counts), cudaMemcpyHostToDevice, s->stream));
+    std::vector<double> obj(4 * (size_t)std::max(1, n), 0.0), pot(std::max(1, n), 0.0);
+    for (int i = 0; i < n; ++i)
+        if (map[i] >= 0) {
+            obj[4 * i] = objects[map[i]].charge;
+            obj[4 * i + 1] = objects[map[i]].current;
+            obj[4 * i + 2] = objects[map[i]].potential;
+            pot[i] = objects[map[i]].potential;
+        }
+    PG_CUDA(cudaMemcpyAsync(s->run_obj, obj.data(), sizeof(double) * obj.size(), cudaMemcpyHostToDevice, s->stream));
+    if (n > 0) PG_CUDA(cudaMemcpyAsync(s->obj_pot, pot.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s->stream));
+    if (!s->rho_valid && (rc = deposit_into_acc(s))) return rc;
+    // the circuit solve warm-starts from phi0; the plain solve from phi
+    if (!s->cfg.pcg_warm_start || !(s->circuit_ready && !s->cfg.circuit_resolve && s->lap ? s->phi0_valid : s->phi_valid))
+        PG_CUDA(cudaMemsetAsync(s->circuit_ready && !s->cfg.circuit_resolve && s->lap ? s->phi0 : s->phi, 0,
+                                sizeof(double) * s->ndof, s->stream));
+    const bool profiling = s->profiling;
+    s->profiling = false;
+    const long long launches0 = launches_so_far();
+    int k = 0;
+    if (a->first_step) {
+        if ((rc = enqueue_step(s, a, true))) { s->profiling = profiling; return rc; }
+        ++k;
+        ++s->step_count;
+        if (s->step_count % s->cfg.sort_interval == 0) sort_enqueue(s);
+    }
+    // a captured step is valid for these arguments and these buffers
+    pg_step_args ak = *a;
+    ak.step = 0;            // read from the device counters
+    ak.first_step = 0;
+    std::string key(reinterpret_cast<const char *>(&ak), sizeof(pg_step_args));
+    const void *bufs[] = {s->scan_tmp, s->inj_counts, s->inj_offsets, s->flux_num, s->pdf_max, s->run_rows};
+    key.append(reinterpret_cast<const char *>(bufs), sizeof(bufs));
+    const int32_t flags[] = {s->n_inj_species, s->flux_ready ? 1 : 0, s->circuit_ready ? 1 : 0, s->n_species};
+    key.append(reinterpret_cast<const char *>(flags), sizeof(flags));
+    while (k < n_steps) {
+        if (use_graph) {
+            const int c = s->cur;
+            if (!s->graph_exec[c] || s->graph_key[c] != key || s->graph_cap[c] != s->P[c].capacity) {
+                if (s->graph_exec[c]) cudaGraphExecDestroy(s->graph_exec[c]);
+                s->graph_exec[c] = nullptr;
+                cudaGraph_t g = nullptr;
+                const long long l0 = launches_so_far();
+                cudaError_t e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+                if (e == cudaSuccess) {
+                    rc = enqueue_step(s, a, false);
+                    e = cudaStreamEndCapture(s->stream, &g);
+                }
+                if (e == cudaSuccess && rc == PG_OK) e = cudaGraphInstantiate(&s->graph_exec[c], g, 0);
+                if (g) cudaGraphDestroy(g);
+                if (e != cudaSuccess || rc != PG_OK) {
+                    s->profiling = profiling;
+                    s->graph_exec[c] = nullptr;
+                    cudaGetLastError();
+                    return rc ? rc : fail(PG_ERR_CUDA, std::string("step graph capture: ") + cudaGetErrorString(e));
+                }
+                s->graph_launches = launches_so_far() - l0;
+                s->graph_key[c] = key;
+                s->graph_cap[c] = s->P[c].capacity;
+            }
+            PG_CUDA(cudaGraphLaunch(s->graph_exec[c], s->stream));
+            count_launches((int)s->graph_launches);
+        } else if ((rc = enqueue_step(s, a, false))) {
+            s->profiling = profiling;
+            return rc;
+        }
+        ++k;
+        ++s->step_count;
+        if (s->step_count % s->cfg.sort_interval == 0) sort_enqueue(s);
+    }
+    s->profiling = profiling;
+    (void)launches0;
+    // read back once
+    int64_t cnt[4];
+    std::vector<double> rows((size_t)n_steps * row_len);
+    PG_CUDA(cudaMemcpyAsync(cnt, s->run_counts, sizeof(cnt), cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaMemcpyAsync(obj.data(), s->run_obj, sizeof(double) * obj.size(), cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaMemcpyAsync(rows.data(), s->run_rows, sizeof(double) * rows.size(), cudaMemcpyDeviceToHost, s->stream));
+    rc = check_state(s);
+    s->n_slots = cnt[0];
+    s->next_pid = cnt[1];
+    s->rho_valid = true;
+    s->phi_valid = true;
+    if (s->circuit_ready && !s->cfg.circuit_resolve && s->lap) s->phi0_valid = true;
+    for (int i = 0; i < n; ++i)
+        if (map[i] >= 0) {
+            objects[map[i]].charge = obj[4 * i];
+            objects[map[i]].current = obj[4 * i + 1];
+            objects[map[i]].potential = obj[4 * i + 2];
+        }
+    if (results)
+        for (int j = 0; j < n_steps; ++j) {
+            const double *r = rows.data() + (size_t)j * row_len;
+            pg_step_result &o = results[j];
+            o = pg_step_result{};
+            o.KE = r[0];
+            o.n_particles = (int64_t)r[1];
+            o.n_absorbed = (int64_t)r[2];
+            o.n_injected = (int64_t)r[3];
+            o.pcg_iterations = (int32_t)r[4];
+            o.pcg_residual = r[5];
+        }
+    if (rc) return rc;
+    int32_t oi[2];
+    PG_CUDA(cudaMemcpy(oi, s->pcg_out_i, sizeof(oi), cudaMemcpyDeviceToHost));
+    if (oi[1] != 0) return fail(PG_ERR_NOT_CONVERGED, "pg_run_steps: the last PCG solve did not converge");
+    return PG_OK;
 }
 
 int pg_step(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_objects, pg_step_result *res) {

@@ -51,7 +51,8 @@ __global__ void k_inject_count(InjectParams ip, const double *__restrict__ flux_
     const double nf = flux_num[idx] * ip.sp[s].ndt;
     int64_t n = (int64_t)nf;
     double u, unused;
-    uniforms2(ip.seed, 0u, (uint32_t)j, (uint32_t)s, ip.step, u, unused);
+    const uint32_t step = ip.counts_dev ? (uint32_t)ip.counts_dev[2] : ip.step;
+    uniforms2(ip.seed, 0u, (uint32_t)j, (uint32_t)s, step, u, unused);
     if (u < nf - (double)n) n += 1;
     counts[idx] = n;
 }
@@ -63,6 +64,9 @@ __global__ void k_inject_generate(DevMesh m, DevParticles p, InjectParams ip, co
                                   double *__restrict__ rho_acc, DevState *__restrict__ st) {
     const int total_streams = ip.n_species * ip.n_facets;
     const int64_t total = offsets[total_streams];
+    const int64_t slot_base = ip.counts_dev ? ip.counts_dev[0] : ip.slot_base;
+    const int64_t pid_base = ip.counts_dev ? ip.counts_dev[1] : ip.pid_base;
+    const uint32_t step = ip.counts_dev ? (uint32_t)ip.counts_dev[2] : ip.step;
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -80,7 +84,7 @@ __global__ void k_inject_generate(DevMesh m, DevParticles p, InjectParams ip, co
         const InjectSpecies &S = ip.sp[s];
         const double *F = facets + 14 * (size_t)j;
         const double nx = F[10], ny = F[11], nz = F[12];
-        const uint32_t c1 = (uint32_t)j, c2 = (uint32_t)(s + 8 * (k + 1)), c3 = ip.step;
+        const uint32_t c1 = (uint32_t)j, c2 = (uint32_t)(s + 8 * (k + 1)), c3 = step;
         const double pmax = pdf_max[idx];
         // rejection sampling, 32 candidates per round; each candidate is
         // screened in FP32 and only undecided ones take the FP64 test
@@ -117,9 +121,9 @@ __global__ void k_inject_generate(DevMesh m, DevParticles p, InjectParams ip, co
             }
         }
         if (lane != 0) continue;
-        const int64_t i = ip.slot_base + t;
+        const int64_t i = slot_base + t;
         p.sp[i] = (uint8_t)s;
-        p.pid[i] = ip.pid_base + t;
+        p.pid[i] = pid_base + t;
         if (found < 0) { raise_device_error(st, PG_ERR_ARG, idx); p.cell[i] = kDead; continue; }
         double r1, r2, r, unused;
         uniforms2(ip.seed, 0u, c1, c2, c3, r1, r2);

@@ -40,7 +40,8 @@ __global__ void __launch_bounds__(kThreads) k_mixed(DevMesh m, DevParticles p, i
     double ke = 0.0;
     int retests = 0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_slots; i += stride) {
+    const int64_t n_use = slots_in_use(p, n_slots);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_use; i += stride) {
         int c = p.cell[i];
         if (c < 0) continue;
         const int s = p.sp[i];
@@ -136,7 +137,8 @@ __global__ void __launch_bounds__(kThreads) k_kinetic_mixed(DevParticles p, int6
                                                            double *__restrict__ partials) {
     double ke = 0.0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_slots; i += stride) {
+    const int64_t n_use = slots_in_use(p, n_slots);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_use; i += stride) {
         if (p.cell[i] < 0) continue;
         const float hm = mp.half_m[p.sp[i]];
         const float vx = p.vxf[i], vy = p.vyf[i], vz = p.vzf[i];

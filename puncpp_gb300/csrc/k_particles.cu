@@ -52,7 +52,8 @@ __global__ void __launch_bounds__(kThreads) k_particles(DevMesh m, DevParticles 
                                                        double *__restrict__ partials) {
     double ke = 0.0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_slots; i += stride) {
+    const int64_t n_use = slots_in_use(p, n_slots);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_use; i += stride) {
         int c = p.cell[i];
         if (c < 0) continue;
         const int s = p.sp[i];
@@ -171,7 +172,8 @@ __global__ void __launch_bounds__(kThreads) k_kinetic(DevParticles p, int64_t n_
                                                      double *__restrict__ partials) {
     double ke = 0.0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_slots; i += stride) {
+    const int64_t n_use = slots_in_use(p, n_slots);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_use; i += stride) {
         if (p.cell[i] < 0) continue;
         const double hm = pp.half_m[p.sp[i]];
         const double vx = p.vx[i], vy = p.vy[i], vz = p.vz[i];
@@ -203,6 +205,15 @@ __global__ void k_locate(DevMesh m, const double *__restrict__ xyz, int64_t n, i
         if (inside_fp64(m, x, y, z, c)) { found = c; break; }
     }
     out[i] = found;
+}
+
+// x <- 2 x - x_prev, x_prev <- old x (linear extrapolation of the last two solutions).
+__global__ void k_extrapolate(double *__restrict__ x, double *__restrict__ x_prev, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double xn = x[i];
+    x[i] = 2.0 * xn - x_prev[i];
+    x_prev[i] = xn;
 }
 
 __global__ void k_scale(const double *__restrict__ a, const double *__restrict__ b, double *__restrict__ o, int64_t n) {
@@ -288,7 +299,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int64_t *__re
 
 __global__ void k_sort_hist(DevParticles p, int64_t n_slots, int64_t *__restrict__ hist) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_slots; i += stride) {
+    const int64_t n_use = slots_in_use(p, n_slots);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_use; i += stride) {
         const int c = p.cell[i];
         if (c >= 0) atomicAdd(reinterpret_cast<unsigned long long *>(hist + c), 1ull);
     }
@@ -297,7 +309,8 @@ __global__ void k_sort_hist(DevParticles p, int64_t n_slots, int64_t *__restrict
 template <bool MIXED>
 __global__ void k_sort_scatter(DevParticles s, DevParticles d, int64_t n_slots, int64_t *__restrict__ cursor) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_slots; i += stride) {
+    const int64_t n_use = slots_in_use(s, n_slots);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_use; i += stride) {
         const int c = s.cell[i];
         if (c < 0) continue;
         const int64_t j = (int64_t)atomicAdd(reinterpret_cast<unsigned long long *>(cursor + c), 1ull);
@@ -418,6 +431,12 @@ void launch_scale(const double *a, const double *b, double *out, int64_t n, cuda
     if (n <= 0) return;
     count_launches(1);
     k_scale<<<(unsigned)((n + kThreads - 1) / kThreads), kThreads, 0, st>>>(a, b, out, n);
+}
+
+void launch_extrapolate(double *x, double *x_prev, int64_t n, cudaStream_t st) {
+    if (n <= 0) return;
+    count_launches(1);
+    k_extrapolate<<<(unsigned)((n + kThreads - 1) / kThreads), kThreads, 0, st>>>(x, x_prev, n);
 }
 
 int64_t scan_tmp_size(int64_t n) { return (n + kScanTile - 1) / kScanTile + 1; }

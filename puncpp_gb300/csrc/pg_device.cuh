@@ -52,7 +52,15 @@ struct DevParticles {
     uint8_t *sp = nullptr;
     int64_t *pid = nullptr;
     int64_t capacity = 0;
+    // when set, the number of slots in use is read from device memory (kernels
+    // of a captured step: the count changes between replays)
+    const int64_t *n_dev = nullptr;
 };
+
+// slots in use: the device count when present, else the launch argument
+__device__ __forceinline__ int64_t slots_in_use(const DevParticles &p, int64_t n_slots) {
+    return p.n_dev ? *p.n_dev : n_slots;
+}
 
 // Device-side counters and error word, read back with one copy.
 struct DevState {
@@ -101,6 +109,9 @@ struct InjectParams {
     double dt;
     int64_t slot_base;            // first free slot
     int64_t pid_base;
+    // when set: slot base, id base and step number read from
+    // counts_dev[0], [1], [2] (captured steps)
+    const int64_t *counts_dev;
     InjectSpecies sp[kMaxSpecies];
     // mixed form: fixed-point deposit target and q * 2^40 / q_max per species
     unsigned long long *rho_fixed;
@@ -237,6 +248,7 @@ void launch_kinetic(const DevParticles &p, int64_t n_slots, const double *half_m
                     int nblocks, double *ke_out, cudaStream_t st);
 void launch_locate(const DevMesh &m, const double *xyz, int64_t n, int32_t *cells, cudaStream_t st);
 void launch_scale(const double *a, const double *b, double *out, int64_t n, cudaStream_t st);
+void launch_extrapolate(double *x, double *x_prev, int64_t n, cudaStream_t st);
 
 void launch_inject_count(const DevMesh &m, const InjectParams &ip, const double *flux_num,
                          int64_t *counts, cudaStream_t st);
@@ -280,6 +292,29 @@ struct Pots {
 };
 void launch_superpose(const double *phi0, const double *lap, const Pots &pots, int32_t n, double *out,
                       cudaStream_t st);
+
+// CircuitCM matrices and groups on the device (k_step.cu)
+struct CircuitDev {
+    int32_t n = 0;                       // objects
+    int32_t n_groups = 0, n_fv = 0;
+    const int32_t *g_ptr = nullptr, *g_mem = nullptr;   // charge-sharing groups
+    const int32_t *f_ptr = nullptr, *f_mem = nullptr;   // fixed-voltage sets
+    const double *inv_cap = nullptr;     // [n][n]
+    const double *inv_circ = nullptr;    // [2n][2n]
+    double *cv = nullptr;                // [2n] circuit vector
+};
+void launch_inject_commit(int64_t *counts, const DevState *st, cudaStream_t s);
+void launch_objects_update(const DevState *st, const double *q, int n_species, const int64_t *tags, int n_obj,
+                           double *obj, double dt, cudaStream_t s);
+void launch_circuit_pre(const double *isrc, int n_isrc, double circ_dt, int n_obj, double *obj, double *obj_pot,
+                        cudaStream_t s);
+void launch_circuit_post(const CircuitDev &c, const double *img, double *obj, double *obj_pot, cudaStream_t s);
+void launch_superpose_dev(const double *phi0, const double *lap, const double *pot, int n_obj, int32_t n, double *out,
+                          cudaStream_t s);
+void launch_step_record(double *rows, int row_len, int64_t *counts, const double *ke, const DevState *st,
+                        int n_species, const int32_t *pcg_i, const double *pcg_d, const double *obj, int n_obj,
+                        cudaStream_t s);
+void launch_set_count(int64_t *counts, const int64_t *cursor, int32_t nc, cudaStream_t s);
 
 // mixed-precision form
 void launch_mixed_pass(const DevMesh &m, const DevParticles &p, int64_t n_slots, const MixedParams &mp, bool push,

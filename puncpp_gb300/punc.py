@@ -120,12 +120,12 @@ class Population:
 
     def __init__(self, mesh: Mesh, precision: int = L.PG_FP64, periodic: bool = False, capacity: int = 0,
                  max_walk_steps: int = 0, sort_interval: int = 0, pcg_rtol: float = 0.0, pcg_atol: float = 0.0,
-                 pcg_max_iter: int = 0, warm_start: bool = True, ext_E=(0.0, 0.0, 0.0),
+                 pcg_max_iter: int = 0, warm_start: int = 1, ext_E=(0.0, 0.0, 0.0),
                  circuit_resolve: bool = False, pcg_precision: int = 0, pcg_precond: int = 0):
         lib = L.load()
         self.mesh = mesh
         cfg = L.Config(precision, 1 if periodic else 0, mesh.eps0, capacity, max_walk_steps, sort_interval,
-                       pcg_rtol, pcg_atol, pcg_max_iter, 1 if warm_start else 0, (C.c_double * 3)(*ext_E),
+                       pcg_rtol, pcg_atol, pcg_max_iter, int(warm_start), (C.c_double * 3)(*ext_E),
                        1 if circuit_resolve else 0, pcg_precision, pcg_precond)
         h = C.c_void_p()
         L.check(lib.pg_create(mesh.handle, C.byref(cfg), C.byref(h)))
@@ -487,6 +487,22 @@ def step(pop: Population, objects, dt: float, B=(0.0, 0.0, 0.0), first_step=Fals
     L.check(L.load().pg_step(pop.handle, C.byref(a), arr, len(objects), C.byref(res)))
     _objects_out(arr, objects)
     return res
+
+
+def run_steps(pop: Population, objects, dt: float, n_steps: int, B=(0.0, 0.0, 0.0), first_step=False,
+              use_accel=False, Ld=None, inject=False, seed=0, step_no=0, E0=(0.0, 0.0, 0.0), efield_cg1=False,
+              use_graph=True):
+    """n_steps fused timesteps with the bookkeeping on the device (one host
+    synchronisation at the end), optionally replaying a captured CUDA graph;
+    returns the per-step results."""
+    a = L.StepArgs(dt, (C.c_double * 3)(*B), 1 if first_step else 0, 1 if use_accel else 0,
+                   0 if Ld is None else 1, (C.c_double * 3)(*(Ld if Ld is not None else (0.0, 0.0, 0.0))),
+                   1 if inject else 0, seed, step_no, (C.c_double * 3)(*E0), 1 if efield_cg1 else 0)
+    arr = _objects_in(objects)
+    res = (L.StepResult * max(1, n_steps))()
+    L.check(L.load().pg_run_steps(pop.handle, C.byref(a), arr, len(objects), n_steps, 1 if use_graph else 0, res))
+    _objects_out(arr, objects)
+    return list(res)[:n_steps]
 
 
 def stage_times(pop: Population) -> dict:

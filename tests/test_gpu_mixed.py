@@ -178,3 +178,41 @@ def test_mixed_diagnostics_close_to_the_oracle(lib, oracle_mod):
     re, ri = o.density_dg0(1.0, 1.0)
     assert rel(ne, re) < 1e-12 and rel(ni, ri) < 1e-12
     assert np.allclose(pop.statistics(), o.statistics(), rtol=1e-6, atol=0)
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_run_steps_equals_step_by_step(use_graph, lib, oracle_mod):
+    """pg_run_steps (device-side bookkeeping, optionally a captured CUDA graph)
+    against pg_step called step by step: the mixed form is deterministic (fixed-
+    point deposit, fixed-order reductions), so particles, objects and per-step
+    results agree bit for bit, across a cell sort."""
+    ma = meshgen.probe_box(8, 3.0, 0.8)
+    mesh = punc.Mesh(ma)
+    rng = np.random.default_rng(31)
+    xe, ve = uniform_points(ma, 20000, rng), maxwellian_velocities(20000, 1.0, rng)
+    xi, vi = uniform_points(ma, 20000, rng), maxwellian_velocities(20000, 0.1, rng)
+    sp = [punc.Species(-1.0, 1.0, n=20.0, vth=1.0), punc.Species(1.0, 100.0, n=20.0, vth=0.1)]
+    runs = []
+    for k in range(2):
+        pop = punc.Population(mesh, precision=L.PG_MIXED, pcg_rtol=1e-10, sort_interval=5)
+        pop.add_particles(f32(xe), f32(ve), -1.0, 1.0)
+        pop.add_particles(f32(xi), f32(vi), 1.0, 100.0)
+        punc.create_flux(pop, sp)
+        objs = [punc.Object(2)]
+        punc.CircuitCM(pop, objs, [(-1, 0, -1.5)], [], 0.1)
+        runs.append((pop, objs))
+    (p1, o1), (p2, o2) = runs
+    ref = [punc.step(p1, o1, 0.1, first_step=(n == 0), inject=True, seed=3, step_no=n) for n in range(8)]
+    got = punc.run_steps(p2, o2, 0.1, 8, first_step=True, inject=True, seed=3, step_no=0, use_graph=use_graph)
+    for a, b in zip(ref, got):
+        assert (a.KE, a.n_particles, a.n_absorbed, a.n_injected, a.pcg_iterations) == \
+               (b.KE, b.n_particles, b.n_absorbed, b.n_injected, b.pcg_iterations)
+    assert (o1[0].charge, o1[0].current, o1[0].potential) == (o2[0].charge, o2[0].current, o2[0].potential)
+    a, b = p1.particles(), p2.particles()
+    for k in ("id", "cell", "x", "v"):
+        assert np.array_equal(a[k], b[k]), k
+    # a second call continues from where the first stopped
+    ref2 = [punc.step(p1, o1, 0.1, inject=True, seed=3, step_no=n) for n in range(8, 12)]
+    got2 = punc.run_steps(p2, o2, 0.1, 4, inject=True, seed=3, step_no=8, use_graph=use_graph)
+    assert [r.n_particles for r in ref2] == [r.n_particles for r in got2]
+    assert np.array_equal(p1.particles()["x"], p2.particles()["x"])
