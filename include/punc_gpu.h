@@ -188,6 +188,16 @@ int pg_status_detail(pg_sim *sim, int32_t *code, int64_t *index);
  * locate each point and keep those inside the mesh. */
 int pg_add_particles(pg_sim *sim, const double *xs, const double *vs, int64_t n,
                      double q, double m, int64_t *n_added);
+/* pg_add_particles locating only in cells [cell_lo, cell_hi): batched runs keep
+ * each run's mesh at its own coordinates (the runs overlap in space) and load
+ * each run's particles into its own cell range. */
+int pg_add_particles_range(pg_sim *sim, const double *xs, const double *vs, int64_t n, double q, double m,
+                           int32_t cell_lo, int32_t cell_hi, int64_t *n_added);
+/* Batched runs: per exterior facet (engine order, PG_T_EXT_FACETS rows) the
+ * injection RNG stream id and seed offset, so that each run draws the streams
+ * of its standalone mesh (facet j of run r: stream = j - first facet of r,
+ * key = seed + offset of r).  Either array may be NULL (keep j / 0). */
+int pg_set_injection_streams(pg_sim *sim, const uint32_t *facet_stream, const uint64_t *facet_seed);
 /* num_of_particles / num_of_negatives / num_of_positives
  * (punc/include/punc/population.h:701-744). */
 int pg_num_particles(pg_sim *sim, int64_t *total, int64_t *negatives, int64_t *positives);

@@ -110,6 +110,8 @@ SIGNATURES = {
     "pg_status_detail": ([_P, _I32, _I64], C.c_int),
     "pg_add_particles": ([_P, _D, _D, C.c_int64, C.c_double, C.c_double, _I64], C.c_int),
     "pg_num_particles": ([_P, _I64, _I64, _I64], C.c_int),
+    "pg_add_particles_range": ([_P, _D, _D, C.c_int64, C.c_double, C.c_double, C.c_int32, C.c_int32, _I64], C.c_int),
+    "pg_set_injection_streams": ([_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint64)], C.c_int),
     "pg_get_particles": ([_P, C.c_int64, _D, _D, _D, _D, _I64, _I64, _I64], C.c_int),
     "pg_locate": ([_P, _D, C.c_int64, _I64], C.c_int),
     "pg_efield_dg0": ([_P, _D], C.c_int),

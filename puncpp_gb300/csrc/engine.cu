@@ -108,6 +108,8 @@ struct pg_sim {
     double *flux_num = nullptr, *pdf_max = nullptr;
     std::vector<double> flux_num_h;
     std::vector<double> flux_sum_h;            // per injected species: sum over facets of flux_num
+    uint32_t *d_inj_c1 = nullptr;              // per exterior facet RNG stream ids (batched runs)
+    uint64_t *d_inj_seed = nullptr;            // per exterior facet seed offsets (batched runs)
     int64_t *inj_counts = nullptr, *inj_offsets = nullptr, *scan_tmp = nullptr;
     int64_t scan_tmp_n = 0;
 
@@ -784,6 +786,8 @@ static int inject_internal(pg_sim *s, double dt, uint64_t seed, uint64_t step, b
     for (int k = 0; k < ip.n_species; ++k) ipd.sp[k] = ip.sp[k];
     ipd.slot_base = s->n_slots;
     ipd.pid_base = s->next_pid;
+    ipd.facet_c1 = s->d_inj_c1;
+    ipd.facet_seed = s->d_inj_seed;
     ipd.rho_fixed = s->rho_fixed;
     {
         const double unit = fixed_unit(s);
@@ -1089,7 +1093,37 @@ int pg_status_detail(pg_sim *s, int32_t *code, int64_t *index) {
     return PG_OK;
 }
 
+static int add_particles_internal(pg_sim *s, const double *xs, const double *vs, int64_t n, double q, double m,
+                                  int32_t cell_lo, int32_t cell_hi, int64_t *n_added);
+
 int pg_add_particles(pg_sim *s, const double *xs, const double *vs, int64_t n, double q, double m, int64_t *n_added) {
+    return add_particles_internal(s, xs, vs, n, q, m, 0, 0x7fffffff, n_added);
+}
+
+int pg_add_particles_range(pg_sim *s, const double *xs, const double *vs, int64_t n, double q, double m,
+                           int32_t cell_lo, int32_t cell_hi, int64_t *n_added) {
+    if (s && (cell_lo < 0 || cell_hi <= cell_lo)) return fail(PG_ERR_ARG, "pg_add_particles_range: empty cell range");
+    return add_particles_internal(s, xs, vs, n, q, m, cell_lo, cell_hi, n_added);
+}
+
+int pg_set_injection_streams(pg_sim *s, const uint32_t *facet_stream, const uint64_t *facet_seed) {
+    if (!s) return fail(PG_ERR_ARG, "NULL handle");
+    int rc;
+    if (facet_stream) {
+        std::vector<uint32_t> v(facet_stream, facet_stream + s->n_ext);
+        if (!s->d_inj_c1 && (rc = dalloc(s, &s->d_inj_c1, std::max(1, s->n_ext)))) return rc;
+        PG_CUDA(cudaMemcpy(s->d_inj_c1, v.data(), sizeof(uint32_t) * v.size(), cudaMemcpyHostToDevice));
+    }
+    if (facet_seed) {
+        std::vector<uint64_t> v(facet_seed, facet_seed + s->n_ext);
+        if (!s->d_inj_seed && (rc = dalloc(s, &s->d_inj_seed, std::max(1, s->n_ext)))) return rc;
+        PG_CUDA(cudaMemcpy(s->d_inj_seed, v.data(), sizeof(uint64_t) * v.size(), cudaMemcpyHostToDevice));
+    }
+    return PG_OK;
+}
+
+static int add_particles_internal(pg_sim *s, const double *xs, const double *vs, int64_t n, double q, double m,
+                                  int32_t cell_lo, int32_t cell_hi, int64_t *n_added) {
     if (!s || (n > 0 && (!xs || !vs)) || n < 0) return fail(PG_ERR_ARG, "pg_add_particles: bad arguments");
     if (n_added) *n_added = 0;
     if (n == 0) return PG_OK;
@@ -1109,7 +1143,10 @@ int pg_add_particles(pg_sim *s, const double *xs, const double *vs, int64_t n, d
     PG_CUDA(cudaMalloc(&d_cells, sizeof(int32_t) * n));
     std::vector<int32_t> cells(n);
     cudaMemcpyAsync(d_xyz, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->stream);
-    launch_locate(s->dm, d_xyz, n, d_cells, s->stream);
+    DevMesh dm = s->dm;
+    dm.loc_lo = cell_lo;
+    dm.loc_hi = cell_hi;
+    launch_locate(dm, d_xyz, n, d_cells, s->stream);
     cudaMemcpyAsync(cells.data(), d_cells, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s->stream);
     cudaError_t e = cudaStreamSynchronize(s->stream);
     cudaFree(d_xyz);
@@ -1806,6 +1843,8 @@ static void inject_enqueue(pg_sim *s, const DevParticles &Pd, double dt, uint64_
         I.q = S.q;
     }
     ip.counts_dev = s->run_counts;
+    ip.facet_c1 = s->d_inj_c1;
+    ip.facet_seed = s->d_inj_seed;
     ip.rho_fixed = s->rho_fixed;
     const double unit = fixed_unit(s);
     for (int k = 0; k < s->n_species; ++k) ip.q_scaled[k] = (float)(s->q[k] / unit);
@@ -2016,7 +2055,8 @@ int pg_run_steps(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n
     ak.step = 0;            // read from the device counters
     ak.first_step = 0;
     std::string key(reinterpret_cast<const char *>(&ak), sizeof(pg_step_args));
-    const void *bufs[] = {s->scan_tmp, s->inj_counts, s->inj_offsets, s->flux_num, s->pdf_max, s->run_rows};
+    const void *bufs[] = {s->scan_tmp, s->inj_counts, s->inj_offsets, s->flux_num, s->pdf_max, s->run_rows,
+                          s->d_inj_c1, s->d_inj_seed};
     key.append(reinterpret_cast<const char *>(bufs), sizeof(bufs));
     const int32_t flags[] = {s->n_inj_species, s->flux_ready ? 1 : 0, s->circuit_ready ? 1 : 0, s->n_species};
     key.append(reinterpret_cast<const char *>(flags), sizeof(flags));

@@ -52,7 +52,9 @@ __global__ void k_inject_count(InjectParams ip, const double *__restrict__ flux_
     int64_t n = (int64_t)nf;
     double u, unused;
     const uint32_t step = ip.counts_dev ? (uint32_t)ip.counts_dev[2] : ip.step;
-    uniforms2(ip.seed, 0u, (uint32_t)j, (uint32_t)s, step, u, unused);
+    const uint64_t seed = ip.facet_seed ? ip.seed + ip.facet_seed[j] : ip.seed;
+    const uint32_t c1 = ip.facet_c1 ? ip.facet_c1[j] : (uint32_t)j;
+    uniforms2(seed, 0u, c1, (uint32_t)s, step, u, unused);
     if (u < nf - (double)n) n += 1;
     counts[idx] = n;
 }
@@ -84,7 +86,8 @@ __global__ void k_inject_generate(DevMesh m, DevParticles p, InjectParams ip, co
         const InjectSpecies &S = ip.sp[s];
         const double *F = facets + 14 * (size_t)j;
         const double nx = F[10], ny = F[11], nz = F[12];
-        const uint32_t c1 = (uint32_t)j, c2 = (uint32_t)(s + 8 * (k + 1)), c3 = step;
+        const uint32_t c1 = ip.facet_c1 ? ip.facet_c1[j] : (uint32_t)j, c2 = (uint32_t)(s + 8 * (k + 1)), c3 = step;
+        const uint64_t seed = ip.facet_seed ? ip.seed + ip.facet_seed[j] : ip.seed;
         const double pmax = pdf_max[idx];
         // rejection sampling, 32 candidates per round; each candidate is
         // screened in FP32 and only undecided ones take the FP64 test
@@ -94,7 +97,7 @@ __global__ void k_inject_generate(DevMesh m, DevParticles p, InjectParams ip, co
         B.factor = S.factor;
         const FluxBox32 B32 = flux_box32(B);
         const float nx32 = (float)nx, ny32 = (float)ny, nz32 = (float)nz, pmax32 = (float)pmax;
-        const uint32_t k0 = uint32_t(ip.seed), k1 = uint32_t(ip.seed >> 32);
+        const uint32_t k0 = uint32_t(seed), k1 = uint32_t(seed >> 32);
         double vx = 0, vy = 0, vz = 0;
         int found = -1;
         for (int round = 0; round < kMaxRounds && found < 0; ++round) {
@@ -126,8 +129,8 @@ __global__ void k_inject_generate(DevMesh m, DevParticles p, InjectParams ip, co
         p.pid[i] = pid_base + t;
         if (found < 0) { raise_device_error(st, PG_ERR_ARG, idx); p.cell[i] = kDead; continue; }
         double r1, r2, r, unused;
-        uniforms2(ip.seed, 0u, c1, c2, c3, r1, r2);
-        uniforms2(ip.seed, 1u, c1, c2, c3, r, unused);
+        uniforms2(seed, 0u, c1, c2, c3, r1, r2);
+        uniforms2(seed, 1u, c1, c2, c3, r, unused);
         double x = (1.0 - r1) * F[1] + r1 * F[4];
         double y = (1.0 - r1) * F[2] + r1 * F[5];
         double z = (1.0 - r1) * F[3] + r1 * F[6];

@@ -202,6 +202,7 @@ __global__ void k_locate(DevMesh m, const double *__restrict__ xyz, int64_t n, i
     int found = -1;
     for (int64_t k = m.bin_ptr[bin]; k < m.bin_ptr[bin + 1]; ++k) {
         const int c = m.bin_cells[k];
+        if (c < m.loc_lo || c >= m.loc_hi) continue;
         if (inside_fp64(m, x, y, z, c)) { found = c; break; }
     }
     out[i] = found;

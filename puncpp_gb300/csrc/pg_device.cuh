@@ -41,6 +41,9 @@ struct DevMesh {
     int32_t nbin[3] = {1, 1, 1};
     const int64_t *bin_ptr = nullptr;
     const int32_t *bin_cells = nullptr;
+    // point location considers cells in [loc_lo, loc_hi) only (batched runs
+    // whose meshes overlap in space)
+    int32_t loc_lo = 0, loc_hi = 0x7fffffff;
 };
 
 struct DevParticles {
@@ -112,6 +115,10 @@ struct InjectParams {
     // when set: slot base, id base and step number read from
     // counts_dev[0], [1], [2] (captured steps)
     const int64_t *counts_dev;
+    // when set (batched runs): the stream of facet j is keyed by
+    // (seed + facet_seed[j], facet_c1[j]) instead of (seed, j)
+    const uint32_t *facet_c1;
+    const uint64_t *facet_seed;
     InjectSpecies sp[kMaxSpecies];
     // mixed form: fixed-point deposit target and q * 2^40 / q_max per species
     unsigned long long *rho_fixed;
