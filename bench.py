@@ -161,6 +161,13 @@ def run_ours(args):
         one(first=(k == 0))
     cg1 = args.efield == "cg1"
     graph = args.step_mode == "graph"
+    tuning = None
+    if args.autotune:
+        # the autotuner's steps are part of the warm-up
+        tuning = punc.autotune(pop, objs, DT, steps_per_trial=2, inject=True, seed=0x5EED0002, step_no=step_no,
+                               efield_cg1=cg1)
+        step_no += (24 if prec == L.PG_MIXED else 12) * 2 + 41
+        n_now = pop.num_of_particles()
     if args.step_mode != "staged":
         # capture the step graph (and run one more warm-up step) outside the timed region
         rs = punc.run_steps(pop, objs, DT, 1, inject=True, seed=0x5EED0002, step_no=step_no, efield_cg1=cg1,
@@ -289,7 +296,7 @@ def run_ours(args):
         "data": "synthetic: seeded uniform/Maxwellian particles on a generated Kuhn probe mesh (no dataset)",
         "config": {"workload": workload_name(args.n_side, args.n_per), "precision": args.precision,
                    "pcg_precond": args.pcg_precond, "warm_start": args.warm_start, "efield": args.efield,
-                   "step_mode": args.step_mode, "cells": nc, "dofs": nv, "nnz": nnz,
+                   "step_mode": args.step_mode, "tuning": tuning, "cells": nc, "dofs": nv, "nnz": nnz,
                    "amg_levels": [[v["rows"], v["nnz"]] for v in lay["levels"]], "particles_initial": n0,
                    "particles_mean_pushed": round(n_avg), "pcg_iterations_per_step": round(iters / args.steps, 1),
                    "l2": "inputs larger than L2 (particle SoA ~250 MB, mesh tables ~0.9 GB)"},
@@ -440,6 +447,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="probe-80", help="probe-N: N^3 sub-cubes, particles scaled by (N/80)^3")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="skip the engine's autotuner (launch configuration, sort interval) in the warm-up")
     ap.add_argument("--step-mode", default="graph", choices=["graph", "stream", "staged"],
                     help="graph: pg_run_steps replaying a captured CUDA graph; stream: pg_run_steps without the "
                          "graph; staged: pg_step per step with stage timing")

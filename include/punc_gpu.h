@@ -274,6 +274,26 @@ int pg_step(pg_sim *sim, const pg_step_args *args, pg_object *objects, int32_t n
  * results (optional): [n_steps]. */
 int pg_run_steps(pg_sim *sim, const pg_step_args *args, pg_object *objects, int32_t n_objects,
                  int32_t n_steps, int32_t use_graph, pg_step_result *results);
+/* Launch configuration of the particle pass and the cell-sort interval. */
+typedef struct pg_tuning {
+    int32_t threads;          /* block size of the fused particle pass (0: 256; 32..512) */
+    int32_t blocks_per_sm;    /* blocks of the particle pass per SM (0: keep; at most 32) */
+    int32_t dep_agg;          /* 1: warp-aggregated fixed-point deposit (mixed form) */
+    int32_t sort_interval;    /* steps between cell sorts (0: keep) */
+    double pass_ms;           /* autotune: device time of the chosen particle pass */
+    double sort_ms;           /* autotune: device time of one cell sort */
+} pg_tuning;
+int pg_set_tuning(pg_sim *sim, const pg_tuning *tuning);
+int pg_get_tuning(pg_sim *sim, pg_tuning *tuning);
+/* Autotuner: runs real steps of this simulation (pg_step with args, the RNG
+ * step advancing), steps_per_trial for each block size in {128, 256, 512},
+ * blocks per SM in {2, 4, 8, 16} and (mixed form) deposit aggregation off/on,
+ * keeps the fastest particle pass, then measures one cell sort and the growth
+ * of the pass time over 40 steps without sorting and picks the sort interval in
+ * {5, 10, 20, 40} of least modelled cost (sort / I + mean growth over I).
+ * Applies and returns the choice; about 24 steps_per_trial + 41 steps. */
+int pg_autotune(pg_sim *sim, const pg_step_args *args, pg_object *objects, int32_t n_objects,
+                int32_t steps_per_trial, pg_tuning *out);
 /* Sort particles by cell and drop absorbed slots. */
 int pg_sort(pg_sim *sim);
 

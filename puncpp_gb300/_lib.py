@@ -82,6 +82,11 @@ class StepResult(C.Structure):
                 ("n_injected", C.c_int64), ("pcg_iterations", C.c_int32), ("pcg_residual", C.c_double)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("threads", C.c_int32), ("blocks_per_sm", C.c_int32), ("dep_agg", C.c_int32),
+                ("sort_interval", C.c_int32), ("pass_ms", C.c_double), ("sort_ms", C.c_double)]
+
+
 MAX_AMG_LEVELS = 12
 
 
@@ -135,6 +140,9 @@ SIGNATURES = {
     "pg_inject": ([_P, C.c_double, C.c_uint64, C.c_uint64, _I64], C.c_int),
     "pg_step": ([_P, C.POINTER(StepArgs), C.POINTER(Object), C.c_int32, C.POINTER(StepResult)], C.c_int),
     "pg_sort": ([_P], C.c_int),
+    "pg_set_tuning": ([_P, C.POINTER(Tuning)], C.c_int),
+    "pg_get_tuning": ([_P, C.POINTER(Tuning)], C.c_int),
+    "pg_autotune": ([_P, C.POINTER(StepArgs), C.POINTER(Object), C.c_int32, C.c_int32, C.POINTER(Tuning)], C.c_int),
     "pg_run_steps": ([_P, C.POINTER(StepArgs), C.POINTER(Object), C.c_int32, C.c_int32, C.c_int32,
                       C.POINTER(StepResult)], C.c_int),
     "pg_stage_times": ([_P, _D, C.c_int32, _I32], C.c_int),

@@ -117,7 +117,10 @@ struct pg_sim {
     DevState *state = nullptr;
     DevState *state_h = nullptr;   // pinned
     double *partials = nullptr, *ke_dev = nullptr;
-    int n_part = 0;
+    int n_part = 0;                           // blocks of a particle pass (partial sums in use)
+    int part_cap = 0;                         // partial-sum slots allocated
+    int32_t tune_threads = 0;                 // particle-pass block size (0: 256)
+    int32_t tune_dep_agg = 0;                 // warp-aggregated fixed-point deposit
 
     // sort scratch
     int64_t *sort_hist = nullptr, *sort_cursor = nullptr;
@@ -599,6 +602,8 @@ static void fill_mixed(const pg_sim *s, MixedParams &mp, double dt_push, const d
     }
     mp.dt = (float)dt_move;
     mp.periodic = periodic ? 1 : 0;
+    mp.threads = s->tune_threads;
+    mp.dep_agg = s->tune_dep_agg;
     for (int j = 0; j < 3; ++j) mp.Ld[j] = Ld ? (float)Ld[j] : 1.0f;
 }
 
@@ -812,6 +817,7 @@ static int inject_internal(pg_sim *s, double dt, uint64_t seed, uint64_t step, b
 
 static void fill_push(const pg_sim *s, PushParams &pp, double dt, const double *B, bool accel) {
     pp = PushParams{};
+    pp.threads = s->tune_threads;
     pp.accel = accel ? 1 : 0;
     pp.has_B = (!accel && B && (B[0] != 0.0 || B[1] != 0.0 || B[2] != 0.0)) ? 1 : 0;
     for (int k = 0; k < s->n_species; ++k) {
@@ -1048,7 +1054,8 @@ int pg_create(const pg_mesh *mesh, const pg_config *cfg_in, pg_sim **out) {
     if (cudaMallocHost(&s->state_h, sizeof(DevState)) != cudaSuccess) return bail(fail(PG_ERR_CUDA, "cudaMallocHost failed"));
     std::memset(s->state_h, 0, sizeof(DevState));
     s->n_part = sm_count() * 8;
-    if ((rc = dalloc(s, &s->partials, s->n_part)) || (rc = dalloc(s, &s->ke_dev, 1)) || (rc = dalloc(s, &s->d_q, kMaxSpecies)))
+    s->part_cap = sm_count() * 32;
+    if ((rc = dalloc(s, &s->partials, s->part_cap)) || (rc = dalloc(s, &s->ke_dev, 1)) || (rc = dalloc(s, &s->d_q, kMaxSpecies)))
         return bail(rc);
     cudaMemset(s->d_q, 0, sizeof(double) * kMaxSpecies);
     if ((rc = dalloc(s, &s->sort_hist, h.nc + 1)) || (rc = dalloc(s, &s->sort_cursor, h.nc + 1))) return bail(rc);
@@ -2132,6 +2139,118 @@ int pg_run_steps(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n
     PG_CUDA(cudaMemcpy(oi, s->pcg_out_i, sizeof(oi), cudaMemcpyDeviceToHost));
     if (oi[1] != 0) return fail(PG_ERR_NOT_CONVERGED, "pg_run_steps: the last PCG solve did not converge");
     return PG_OK;
+}
+
+int pg_set_tuning(pg_sim *s, const pg_tuning *t) {
+    if (!s || !t) return fail(PG_ERR_ARG, "pg_set_tuning: NULL argument");
+    if (t->threads != 0 && (t->threads < 32 || t->threads > 512 || (t->threads & 31)))
+        return fail(PG_ERR_ARG, "pg_set_tuning: threads must be 0 or a multiple of 32 in [32, 512]");
+    if (t->blocks_per_sm < 0 || sm_count() * t->blocks_per_sm > s->part_cap)
+        return fail(PG_ERR_ARG, "pg_set_tuning: blocks_per_sm out of range (at most 32)");
+    if (t->sort_interval < 0) return fail(PG_ERR_ARG, "pg_set_tuning: negative sort_interval");
+    s->tune_threads = t->threads;
+    if (t->blocks_per_sm > 0) s->n_part = sm_count() * t->blocks_per_sm;
+    s->tune_dep_agg = t->dep_agg ? 1 : 0;
+    if (t->sort_interval > 0) s->cfg.sort_interval = t->sort_interval;
+    drop_graphs(s);
+    return PG_OK;
+}
+
+int pg_get_tuning(pg_sim *s, pg_tuning *t) {
+    if (!s || !t) return fail(PG_ERR_ARG, "pg_get_tuning: NULL argument");
+    *t = pg_tuning{};
+    t->threads = s->tune_threads ? s->tune_threads : 256;
+    t->blocks_per_sm = s->n_part / sm_count();
+    t->dep_agg = s->tune_dep_agg;
+    t->sort_interval = s->cfg.sort_interval;
+    return PG_OK;
+}
+
+// Device time of the fused particle pass of one pg_step, from the stage timer.
+static double pass_ms(pg_sim *s) {
+    for (size_t k = 0; k < s->stage_names.size(); ++k)
+        if (s->stage_names[k] == "push_move_update_deposit") return s->stage_ms[k];
+    return 0.0;
+}
+
+int pg_autotune(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_objects, int32_t steps_per_trial,
+                pg_tuning *out) {
+    if (!s || !a) return fail(PG_ERR_ARG, "pg_autotune: NULL argument");
+    const int k = std::max(1, steps_per_trial);
+    const bool profiling = s->profiling;
+    s->profiling = true;
+    pg_step_args st = *a;
+    int rc = PG_OK;
+    auto run = [&](int n, double *ms) -> int {
+        collect_stages(s);
+        for (auto &v : s->stage_ms) v = 0.0;
+        for (int i = 0; i < n; ++i) {
+            int r = pg_step(s, &st, objects, n_objects, nullptr);
+            if (r) return r;
+            st.first_step = 0;
+            st.step += 1;
+        }
+        collect_stages(s);
+        if (ms) *ms = pass_ms(s) / n;
+        return PG_OK;
+    };
+    // block size x blocks per SM x deposit aggregation (mixed form)
+    pg_tuning best{};
+    double best_ms = 1e300;
+    const int threads[] = {128, 256, 512};
+    const int bps[] = {2, 4, 8, 16};
+    const int saved_interval = s->cfg.sort_interval;
+    s->cfg.sort_interval = 1 << 30;   // no sorts while timing the launch configurations
+    if ((rc = do_sort(s))) goto done;
+    if ((rc = run(1, nullptr))) goto done;
+    for (int th : threads)
+        for (int b : bps)
+            for (int agg = 0; agg <= (is_mixed(s) ? 1 : 0); ++agg) {
+                pg_tuning t{th, b, agg, 0};
+                if ((rc = pg_set_tuning(s, &t))) goto done;
+                if ((rc = do_sort(s))) goto done;
+                double ms = 0;
+                if ((rc = run(k, &ms))) goto done;
+                if (ms < best_ms) { best_ms = ms; best = t; }
+            }
+    if ((rc = pg_set_tuning(s, &best))) goto done;
+    {
+        // sort interval: the sort's cost against the growth of the pass time
+        // with the steps since the last sort
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, s->stream);
+        rc = do_sort(s);
+        cudaEventRecord(e1, s->stream);
+        cudaEventSynchronize(e1);
+        float sort_ms = 0;
+        cudaEventElapsedTime(&sort_ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (rc) goto done;
+        const int horizon = 40;
+        std::vector<double> t(horizon, 0.0);
+        for (int i = 0; i < horizon; ++i)
+            if ((rc = run(1, &t[i]))) goto done;
+        double best_cost = 1e300;
+        int best_i = saved_interval;
+        for (int I : {5, 10, 20, 40}) {
+            double mean = 0.0;
+            for (int i = 0; i < I; ++i) mean += t[i] - t[0];
+            const double cost = sort_ms / I + mean / I;
+            if (cost < best_cost) { best_cost = cost; best_i = I; }
+        }
+        best.sort_interval = best_i;
+        best.pass_ms = best_ms;
+        best.sort_ms = sort_ms;
+    }
+done:
+    s->cfg.sort_interval = best.sort_interval > 0 ? best.sort_interval : saved_interval;
+    s->profiling = profiling;
+    if (rc) return rc;
+    if (out) *out = best;
+    return do_sort(s);
 }
 
 int pg_step(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_objects, pg_step_result *res) {

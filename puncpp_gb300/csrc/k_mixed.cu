@@ -33,8 +33,37 @@ __device__ __forceinline__ double block_sum_d(double v) {
     return s;
 }
 
+// Deposit of one particle with the lanes of the warp in the same cell adding
+// their fixed-point contributions first (integer sums: the same bits as
+// separate atomics); the group's first lane issues the four atomics.
+__device__ __forceinline__ void deposit_fixed_agg(const DevMesh &m, int c, float x, float y, float z, float q_scaled,
+                                                  unsigned long long *rho_fixed) {
+    const float4 *A = reinterpret_cast<const float4 *>(m.bary_f) + 3 * (size_t)c;
+    const float4 a0 = __ldg(A), a1 = __ldg(A + 1), a2 = __ldg(A + 2);
+    const float l0 = fmaf(a0.w, z, fmaf(a0.z, y, fmaf(a0.y, x, a0.x)));
+    const float l1 = fmaf(a1.w, z, fmaf(a1.z, y, fmaf(a1.y, x, a1.x)));
+    const float l2 = fmaf(a2.w, z, fmaf(a2.z, y, fmaf(a2.y, x, a2.x)));
+    const float l3 = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, l0), l1), l2);
+    long long v0 = __float2ll_rn(__fmul_rn(l0, q_scaled)), v1 = __float2ll_rn(__fmul_rn(l1, q_scaled));
+    long long v2 = __float2ll_rn(__fmul_rn(l2, q_scaled)), v3 = __float2ll_rn(__fmul_rn(l3, q_scaled));
+    const unsigned peers = __match_any_sync(__activemask(), c);
+    const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+    for (unsigned rest = peers & ~(1u << leader); rest; rest &= rest - 1) {
+        const int src = __ffs(rest) - 1;
+        const long long w0 = __shfl_sync(peers, v0, src), w1 = __shfl_sync(peers, v1, src);
+        const long long w2 = __shfl_sync(peers, v2, src), w3 = __shfl_sync(peers, v3, src);
+        if (lane == leader) { v0 += w0; v1 += w1; v2 += w2; v3 += w3; }
+    }
+    if (lane != leader) return;
+    const int4 d = __ldg(m.dofs + c);
+    atomicAdd(rho_fixed + d.x, (unsigned long long)v0);
+    atomicAdd(rho_fixed + d.y, (unsigned long long)v1);
+    atomicAdd(rho_fixed + d.z, (unsigned long long)v2);
+    atomicAdd(rho_fixed + d.w, (unsigned long long)v3);
+}
+
 template <bool PUSH, bool HAS_B, bool ACCEL, bool MOVE, bool PERIODIC, bool WALK, bool DEPOSIT>
-__global__ void __launch_bounds__(kThreads) k_mixed(DevMesh m, DevParticles p, int64_t n_slots, MixedParams mp,
+__global__ void __launch_bounds__(512) k_mixed(DevMesh m, DevParticles p, int64_t n_slots, MixedParams mp,
                                                    int max_steps, unsigned long long *__restrict__ rho_fixed,
                                                    DevState *__restrict__ st, double *__restrict__ partials) {
     double ke = 0.0;
@@ -117,7 +146,10 @@ __global__ void __launch_bounds__(kThreads) k_mixed(DevMesh m, DevParticles p, i
             }
             if (nc != c) { p.cell[i] = nc; c = nc; }
         }
-        if (DEPOSIT) deposit_fixed(m, c, x, y, z, mp.q_scaled[s], rho_fixed);
+        if (DEPOSIT) {
+            if (mp.dep_agg) deposit_fixed_agg(m, c, x, y, z, mp.q_scaled[s], rho_fixed);
+            else deposit_fixed(m, c, x, y, z, mp.q_scaled[s], rho_fixed);
+        }
     }
     if (PUSH) {
         const double t = block_sum_d(ke);
@@ -179,10 +211,13 @@ void launch_mixed_pass(const DevMesh &m, const DevParticles &p, int64_t n_slots,
                        bool move, bool walk, bool deposit, int max_steps, unsigned long long *rho_fixed,
                        DevState *state, double *partials, int nblocks, double *ke_out, cudaStream_t st) {
     if (n_slots <= 0) return;
-    const int g = grid_for(n_slots, push ? nblocks : (1 << 20));
+    const int threads = mp.threads > 0 ? mp.threads : kThreads;
+    int64_t gg = (n_slots + threads - 1) / threads;
+    const int64_t cap = push ? nblocks : (1 << 20);
+    const int g = (int)(gg < 1 ? 1 : (gg > cap ? cap : gg));
     count_launches(push ? 2 : 1);
 #define PG_MIX(PU, HB, AC, MO, PE, WA, DE) \
-    k_mixed<PU, HB, AC, MO, PE, WA, DE><<<g, kThreads, 0, st>>>(m, p, n_slots, mp, max_steps, rho_fixed, state, partials)
+    k_mixed<PU, HB, AC, MO, PE, WA, DE><<<g, threads, 0, st>>>(m, p, n_slots, mp, max_steps, rho_fixed, state, partials)
     if (push && move && walk && deposit) {
         if (mp.accel) { if (mp.periodic) PG_MIX(true, false, true, true, true, true, true); else PG_MIX(true, false, true, true, false, true, true); }
         else if (mp.has_B) { if (mp.periodic) PG_MIX(true, true, false, true, true, true, true); else PG_MIX(true, true, false, true, false, true, true); }

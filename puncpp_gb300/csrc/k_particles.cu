@@ -46,7 +46,7 @@ __device__ __forceinline__ bool inside_fp64(const DevMesh &m, double x, double y
 
 // One pass over the particle slots doing any of push, move, walk and deposit.
 template <bool PUSH, bool HAS_B, bool ACCEL, bool MOVE, bool PERIODIC, bool WALK, bool DEPOSIT>
-__global__ void __launch_bounds__(kThreads) k_particles(DevMesh m, DevParticles p, int64_t n_slots, PushParams pp,
+__global__ void __launch_bounds__(512) k_particles(DevMesh m, DevParticles p, int64_t n_slots, PushParams pp,
                                                        MoveParams mp, int max_steps, const double *__restrict__ qsp,
                                                        double *__restrict__ rho_acc, DevState *__restrict__ st,
                                                        double *__restrict__ partials) {
@@ -396,10 +396,12 @@ void launch_deposit(const DevMesh &m, const DevParticles &p, int64_t n_slots, co
 void launch_fused_step(const DevMesh &m, const DevParticles &p, int64_t n_slots, const PushParams &pp,
                        const MoveParams &mp, int max_steps, const double *q_species, double *rho_acc,
                        DevState *state, double *partials, int nblocks, double *ke_out, cudaStream_t st) {
-    const int g = grid_for(n_slots, nblocks);
+    const int threads = pp.threads > 0 ? pp.threads : kThreads;
+    int64_t gg = (n_slots + threads - 1) / threads;
+    const int g = (int)(gg < 1 ? 1 : (gg > nblocks ? nblocks : gg));
     count_launches(2);
 #define PG_FUSED(HB, AC, PER)                                                                            \
-    k_particles<true, HB, AC, true, PER, true, true><<<g, kThreads, 0, st>>>(m, p, n_slots, pp, mp, max_steps, \
+    k_particles<true, HB, AC, true, PER, true, true><<<g, threads, 0, st>>>(m, p, n_slots, pp, mp, max_steps, \
                                                                            q_species, rho_acc, state, partials)
     if (pp.accel) {
         if (mp.periodic) PG_FUSED(false, true, true); else PG_FUSED(false, true, false);

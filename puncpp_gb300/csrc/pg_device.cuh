@@ -88,6 +88,7 @@ struct PushParams {
     int32_t has_B;
     int32_t accel;                // 1: accel() update rule
     int32_t cg1;                  // 1: field interpolated from the CG1 vertex field (accel_cg1 / boris_cg1)
+    int32_t threads;              // block size of the particle pass (0: 256; at most 512)
 };
 
 struct MoveParams {
@@ -138,6 +139,8 @@ struct MixedParams {
     int32_t periodic;
     float Ld[3];
     int32_t cg1;                  // 1: field interpolated from the CG1 vertex field
+    int32_t threads;              // block size of the particle pass (0: 256; at most 512)
+    int32_t dep_agg;              // 1: lanes of a warp in the same cell add their deposits before the atomics
 };
 
 // ESolver: rhs gather, three-component Jacobi-CG on the mass matrix, packing

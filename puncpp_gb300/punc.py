@@ -505,6 +505,34 @@ def run_steps(pop: Population, objects, dt: float, n_steps: int, B=(0.0, 0.0, 0.
     return list(res)[:n_steps]
 
 
+def _tuning_dict(t) -> dict:
+    return {"threads": t.threads, "blocks_per_sm": t.blocks_per_sm, "dep_agg": t.dep_agg,
+            "sort_interval": t.sort_interval, "pass_ms": t.pass_ms, "sort_ms": t.sort_ms}
+
+
+def set_tuning(pop: Population, threads=0, blocks_per_sm=0, dep_agg=0, sort_interval=0):
+    L.check(L.load().pg_set_tuning(pop.handle, C.byref(L.Tuning(threads, blocks_per_sm, dep_agg, sort_interval))))
+
+
+def get_tuning(pop: Population) -> dict:
+    t = L.Tuning()
+    L.check(L.load().pg_get_tuning(pop.handle, C.byref(t)))
+    return _tuning_dict(t)
+
+
+def autotune(pop: Population, objects, dt: float, steps_per_trial: int = 2, B=(0.0, 0.0, 0.0), first_step=False,
+             inject=False, seed=0, step_no=0, E0=(0.0, 0.0, 0.0), efield_cg1=False) -> dict:
+    """Autotuner of the particle pass launch and the sort interval; runs real
+    steps of the simulation (see pg_autotune) and applies its choice."""
+    a = L.StepArgs(dt, (C.c_double * 3)(*B), 1 if first_step else 0, 0, 0, (C.c_double * 3)(0.0, 0.0, 0.0),
+                   1 if inject else 0, seed, step_no, (C.c_double * 3)(*E0), 1 if efield_cg1 else 0)
+    arr = _objects_in(objects)
+    t = L.Tuning()
+    L.check(L.load().pg_autotune(pop.handle, C.byref(a), arr, len(objects), steps_per_trial, C.byref(t)))
+    _objects_out(arr, objects)
+    return _tuning_dict(t)
+
+
 def stage_times(pop: Population) -> dict:
     lib = L.load()
     n = C.c_int32()

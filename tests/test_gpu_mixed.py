@@ -216,3 +216,38 @@ def test_run_steps_equals_step_by_step(use_graph, lib, oracle_mod):
     got2 = punc.run_steps(p2, o2, 0.1, 4, inject=True, seed=3, step_no=8, use_graph=use_graph)
     assert [r.n_particles for r in ref2] == [r.n_particles for r in got2]
     assert np.array_equal(p1.particles()["x"], p2.particles()["x"])
+
+
+def test_launch_tuning_does_not_change_the_mixed_results(lib, oracle_mod):
+    """The mixed form is deterministic: block size, grid size and the
+    warp-aggregated deposit give the same particles and charge bit for bit;
+    the autotuner returns a configuration from its search space and applies it."""
+    ma = meshgen.probe_box(8, 3.0, 0.8)
+    mesh = punc.Mesh(ma)
+    rng = np.random.default_rng(41)
+    xe, ve = f32(uniform_points(ma, 30000, rng)), f32(maxwellian_velocities(30000, 1.0, rng))
+    pops = []
+    for tune in ({}, dict(threads=512, blocks_per_sm=2, dep_agg=1), dict(threads=128, blocks_per_sm=16, dep_agg=0)):
+        pop = punc.Population(mesh, precision=L.PG_MIXED, pcg_rtol=1e-10)
+        pop.add_particles(xe, ve, -1.0, 1.0)
+        pop.add_particles(xe[::-1].copy(), ve * 0.1, 1.0, 100.0)
+        punc.create_flux(pop, [punc.Species(-1.0, 1.0, n=20.0, vth=1.0)])
+        if tune:
+            punc.set_tuning(pop, **tune)
+        pops.append(pop)
+    objs = [[punc.Object(2, potential=-1.0)] for _ in pops]
+    for n in range(3):
+        for pop, o in zip(pops, objs):
+            punc.step(pop, o, 0.1, first_step=(n == 0), inject=True, seed=1, step_no=n)
+        rho = [punc.Function(p, "rho").vector() for p in pops]
+        assert np.array_equal(rho[0], rho[1]) and np.array_equal(rho[0], rho[2])
+    a = pops[0].particles()
+    for p in pops[1:]:
+        b = p.particles()
+        assert np.array_equal(a["x"], b["x"]) and np.array_equal(a["v"], b["v"])
+    t = punc.autotune(pops[0], objs[0], 0.1, steps_per_trial=1, inject=True, seed=1, step_no=3)
+    assert t["threads"] in (128, 256, 512) and t["blocks_per_sm"] in (2, 4, 8, 16)
+    assert t["sort_interval"] in (5, 10, 20, 40) and t["pass_ms"] > 0 and t["sort_ms"] > 0
+    g = punc.get_tuning(pops[0])
+    assert (g["threads"], g["blocks_per_sm"], g["dep_agg"], g["sort_interval"]) == \
+           (t["threads"], t["blocks_per_sm"], t["dep_agg"], t["sort_interval"])
