@@ -294,6 +294,23 @@ int pg_get_tuning(pg_sim *sim, pg_tuning *tuning);
  * Applies and returns the choice; about 24 steps_per_trial + 41 steps. */
 int pg_autotune(pg_sim *sim, const pg_step_args *args, pg_object *objects, int32_t n_objects,
                 int32_t steps_per_trial, pg_tuning *out);
+/* Adjoint of n_steps fused steps (FP64 form; DG0 field with B = 0, no
+ * injection, no absorption, objects at fixed potentials): the forward runs the
+ * steps from the current state (args as pg_step; args->step the first step's
+ * RNG counter) keeping the particle state every ckpt_every steps, and returns
+ * loss = ||rho_K - rho_target||^2 with rho_K the CG1 charge after the steps.
+ * Cell sorting is suspended until pg_adjoint_release. */
+int pg_adjoint_forward(pg_sim *sim, const pg_step_args *args, pg_object *objects, int32_t n_objects,
+                       int32_t n_steps, int32_t ckpt_every, const double *rho_target, double *loss);
+/* Gradients of that loss, with each particle's cells fixed from the forward
+ * pass (the map is smooth between cell crossings): grad_v [n_out][3] with
+ * respect to the initial velocities and grad_x0 [n_out][3] to the initial
+ * positions, both indexed by particle id, and grad_E0 [3] to the uniform
+ * external field.  Segments between checkpoints are recomputed; the Poisson
+ * adjoint is a second PCG on the same symmetric matrix.  Any output may be
+ * NULL.  The state returns to the one after the forward steps. */
+int pg_adjoint_backward(pg_sim *sim, double *grad_v, int64_t n_out, double *grad_E0, double *grad_x0);
+int pg_adjoint_release(pg_sim *sim);
 /* Sort particles by cell and drop absorbed slots. */
 int pg_sort(pg_sim *sim);
 

@@ -439,3 +439,102 @@ class CircuitCM:
             objects[i]["charge"] = float(self.inv_circuit[n + i] @ cv)
             pots[i] = objects[i]["potential"]
         return self.solve(rho, pots), img
+
+
+class PeriodicPoisson:
+    """y = A^+ P b for the periodic P1 stiffness A (constant null space, P the
+    mean removal): the oracle's Jacobi-PCG on P b to a relative residual of
+    1e-13, then the mean removed from the solution (poisson.cpp:343-362 with
+    the null space orthogonalised out)."""
+
+    def __init__(self, oracle: Oracle, nthreads=1):
+        self.o = oracle
+        self.kind = -np.ones(oracle.ndof, np.int64)
+        self.g = np.zeros(oracle.ndof)
+        self.nthreads = nthreads
+
+    def __call__(self, b):
+        b = np.ascontiguousarray(b, float)
+        x = np.zeros(self.o.ndof)
+        it = lib().or_pcg(self.o.h, _d(b), _l(self.kind), _d(self.g), _d(x), 1e-13, 0.0, 100000, 1, self.nthreads)
+        if it < 0:
+            raise RuntimeError("oracle PCG did not converge")
+        return x - x.mean()
+
+
+def langmuir_adjoint(mesh, x0, v0, q, m, E0, dt, n_steps, target, Ld, first_step=True, nthreads=1):
+    """Loss ||rho_K - target||^2 of K periodic steps (CG1 deposit, P1 Poisson,
+    DG0 field plus the uniform E0, Boris push with B = 0, periodic move) and its
+    gradients by a reverse sweep with the cells fixed from the forward pass.
+    Not a reference algorithm (the reference has no adjoint): the derivative of
+    the stages restated above (distribute_cg1: punc/src/distributor.cpp,
+    efield_DG0: punc/src/efield.cpp, boris: punc/include/punc/pusher.h,
+    move_periodic: pusher.h), checked against jump-free finite differences.
+    Reverse step n: vbar += dt xbar; Ebar_c = sum_{p in c} coef vbar_p;
+    E0bar += sum_p coef vbar_p; phibar_k -= Ebar_c . grad lambda_k(c);
+    rhobar = M A^+ P phibar; xbar_p += q sum_i dv_inv_i rhobar_i grad lambda_i.
+    Returns (loss, grad_v0 [n][3], grad_E0 [3], grad_x0 [n][3]), rows by
+    particle id (insertion order)."""
+    o = Oracle(mesh)
+    K, M = o.matrices()
+    solve = PeriodicPoisson(o, nthreads)
+    n = o.add_particles(x0, v0, q, m)
+    if n != len(x0):
+        raise ValueError("langmuir_adjoint: a particle lies outside the mesh")
+    bary = o.table(T_BARY).reshape(-1, 12)
+    dofs = o.table(T_DOFS).reshape(-1, 4)
+    dv_inv = o.table(T_DV_INV)
+    G = np.zeros((o.nc, 4, 3))
+    for i in range(3):
+        G[:, i, :] = bary[:, 4 * i + 1:4 * i + 4]
+    G[:, 3, :] = -G[:, :3, :].sum(axis=1)
+
+    def cells_by_id():
+        p = o.particles(sort=False)
+        out = np.empty(n, np.int64)
+        out[p["id"]] = p["cell"]
+        return out
+
+    cells = []
+    for k in range(n_steps):
+        cells.append(cells_by_id())
+        phi = solve(M @ o.distribute_cg1(nthreads))
+        E = o.efield(phi, E0)
+        o.boris(E, (0.0, 0.0, 0.0), 0.5 * dt if (first_step and k == 0) else dt, nthreads)
+        o.move(dt, Ld, nthreads)
+        o.update([], dt, nthreads)
+    cells.append(cells_by_id())
+    rho = o.distribute_cg1(nthreads)
+    loss = float(np.sum((rho - target) ** 2))
+
+    def deposit_adjoint(rhobar, c):
+        # per cell sum_i dv_inv_i rhobar_i grad lambda_i, gathered per particle
+        per_cell = np.einsum("ci,cij->cj", dv_inv[dofs] * rhobar[dofs], G)
+        return q * per_cell[c]
+
+    xb = deposit_adjoint(2.0 * (rho - target), cells[n_steps])
+    vb = np.zeros((n, 3))
+    e0b = np.zeros(3)
+    for k in range(n_steps - 1, -1, -1):
+        coef = (0.5 * dt if (first_step and k == 0) else dt) * (q / m)
+        vb += dt * xb
+        Eb = np.stack([np.bincount(cells[k], weights=coef * vb[:, j], minlength=o.nc) for j in range(3)], axis=1)
+        e0b += coef * vb.sum(axis=0)
+        phib = np.bincount(dofs.ravel(), weights=-np.einsum("cj,cij->ci", Eb, G).ravel(), minlength=o.ndof)
+        rhob = M @ solve(phib)
+        xb += deposit_adjoint(rhob, cells[k])
+    return loss, vb, e0b, xb
+
+
+def langmuir_loss(mesh, x0, v0, q, m, E0, dt, n_steps, target, Ld, first_step=True, nthreads=1):
+    """The forward of langmuir_adjoint alone (for finite differences)."""
+    o = Oracle(mesh)
+    _, M = o.matrices()
+    solve = PeriodicPoisson(o, nthreads)
+    o.add_particles(x0, v0, q, m)
+    for k in range(n_steps):
+        phi = solve(M @ o.distribute_cg1(nthreads))
+        o.boris(o.efield(phi, E0), (0.0, 0.0, 0.0), 0.5 * dt if (first_step and k == 0) else dt, nthreads)
+        o.move(dt, Ld, nthreads)
+        o.update([], dt, nthreads)
+    return float(np.sum((o.distribute_cg1(nthreads) - target) ** 2))

@@ -140,6 +140,10 @@ SIGNATURES = {
     "pg_inject": ([_P, C.c_double, C.c_uint64, C.c_uint64, _I64], C.c_int),
     "pg_step": ([_P, C.POINTER(StepArgs), C.POINTER(Object), C.c_int32, C.POINTER(StepResult)], C.c_int),
     "pg_sort": ([_P], C.c_int),
+    "pg_adjoint_forward": ([_P, C.POINTER(StepArgs), C.POINTER(Object), C.c_int32, C.c_int32, C.c_int32, _D, _D],
+                           C.c_int),
+    "pg_adjoint_backward": ([_P, _D, C.c_int64, _D, _D], C.c_int),
+    "pg_adjoint_release": ([_P], C.c_int),
     "pg_set_tuning": ([_P, C.POINTER(Tuning)], C.c_int),
     "pg_get_tuning": ([_P, C.POINTER(Tuning)], C.c_int),
     "pg_autotune": ([_P, C.POINTER(StepArgs), C.POINTER(Object), C.c_int32, C.c_int32, C.POINTER(Tuning)], C.c_int),

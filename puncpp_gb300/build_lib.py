@@ -37,6 +37,7 @@ CU_UNITS = {
     "k_esolve.cu": ["--fmad=true"],
     "k_diag.cu": [],
     "k_step.cu": [],
+    "k_adjoint.cu": [],
 }
 CPP_UNITS = ["mesh_tables.cpp", "amg.cpp", "checkpoint.cpp"]
 

@@ -87,6 +87,25 @@ struct pg_sim {
     int64_t graph_cap[2] = {0, 0};
     long long graph_launches = 0;                          // kernels per captured step
 
+    // adjoint of K fused steps (pg_adjoint_forward / pg_adjoint_backward)
+    struct Adjoint {
+        bool ready = false;
+        int K = 0, C = 0;
+        int64_t n = 0;                        // particle slots (fixed over the K steps)
+        pg_step_args args{};
+        std::vector<pg_object> objects;
+        int saved_sort_interval = 0;
+        std::vector<void *> mem;              // device allocations of this adjoint
+        std::vector<double *> ck_x;           // per checkpoint: x, y, z, vx, vy, vz ([6][n])
+        std::vector<int32_t *> ck_c;          // per checkpoint: cells
+        double *fin_x = nullptr;              // state after the K steps
+        int32_t *fin_c = nullptr;
+        int32_t *rec_c = nullptr;             // cells of the steps of one segment ([C][n])
+        double *bar = nullptr;                // xbar, ybar, zbar, vxbar, vybar, vzbar ([6][n])
+        double *Ebar = nullptr, *phibar = nullptr, *y = nullptr, *rhobar = nullptr, *target = nullptr;
+        double *small = nullptr;              // [0..2] E0bar, [3] loss, [8..15] push coefficients
+    } adj;
+
     // diagnostics scratch (allocated on first use)
     double *diag_a = nullptr, *diag_b = nullptr, *diag_acc = nullptr;
     unsigned long long *diag_cnt = nullptr;
@@ -1074,6 +1093,7 @@ int pg_destroy(pg_sim *s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     for (auto &g : s->graph_exec)
         if (g) cudaGraphExecDestroy(g);
+    for (void *p : s->adj.mem) cudaFree(p);
     for (void *p : s->allocs) cudaFree(p);
     free_particles(s->P[0]);
     free_particles(s->P[1]);
@@ -2251,6 +2271,224 @@ done:
     if (rc) return rc;
     if (out) *out = best;
     return do_sort(s);
+}
+
+// ---- adjoint of K fused steps (FP64 form) ---------------------------------
+
+static void adj_free(pg_sim *s) {
+    for (void *p : s->adj.mem) cudaFree(p);
+    s->adj = pg_sim::Adjoint{};
+}
+
+static int adj_alloc(pg_sim *s, void **p, size_t bytes) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(8, bytes));
+    if (e != cudaSuccess) return fail(PG_ERR_CUDA, std::string("adjoint cudaMalloc: ") + cudaGetErrorString(e));
+    s->adj.mem.push_back(q);
+    *p = q;
+    return PG_OK;
+}
+
+// copy the particle state (positions, velocities, cells) of the current buffer
+static int adj_save(pg_sim *s, double *x, int32_t *c) {
+    const DevParticles &P = s->P[s->cur];
+    const size_t n = (size_t)s->adj.n;
+    double *src[6] = {P.x, P.y, P.z, P.vx, P.vy, P.vz};
+    for (int k = 0; k < 6; ++k)
+        PG_CUDA(cudaMemcpyAsync(x + k * n, src[k], sizeof(double) * n, cudaMemcpyDeviceToDevice, s->stream));
+    PG_CUDA(cudaMemcpyAsync(c, P.cell, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, s->stream));
+    return PG_OK;
+}
+
+static int adj_restore(pg_sim *s, const double *x, const int32_t *c) {
+    const DevParticles &P = s->P[s->cur];
+    const size_t n = (size_t)s->adj.n;
+    double *dst[6] = {P.x, P.y, P.z, P.vx, P.vy, P.vz};
+    for (int k = 0; k < 6; ++k)
+        PG_CUDA(cudaMemcpyAsync(dst[k], x + k * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, s->stream));
+    PG_CUDA(cudaMemcpyAsync(P.cell, c, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, s->stream));
+    s->rho_valid = false;
+    return PG_OK;
+}
+
+static pg_step_args adj_step_args(const pg_sim *s, int step) {
+    pg_step_args a = s->adj.args;
+    a.first_step = (step == 0 && s->adj.args.first_step) ? 1 : 0;
+    a.step = s->adj.args.step + (uint64_t)step;
+    a.inject = 0;
+    return a;
+}
+
+int pg_adjoint_forward(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_objects, int32_t n_steps,
+                       int32_t ckpt_every, const double *rho_target, double *loss) {
+    if (!s || !a || !rho_target || n_steps < 1 || ckpt_every < 1 || (n_objects > 0 && !objects))
+        return fail(PG_ERR_ARG, "pg_adjoint_forward: bad arguments");
+    if (is_mixed(s)) return fail(PG_ERR_ARG, "pg_adjoint_forward: the adjoint runs in the FP64 form");
+    if (a->inject || a->efield_cg1 || a->B[0] != 0.0 || a->B[1] != 0.0 || a->B[2] != 0.0)
+        return fail(PG_ERR_ARG, "pg_adjoint_forward: push with the DG0 field and B = 0, no injection");
+    if (s->circuit_ready) return fail(PG_ERR_ARG, "pg_adjoint_forward: objects at fixed potentials only");
+    if (s->adj.ready) { s->cfg.sort_interval = s->adj.saved_sort_interval; }
+    adj_free(s);
+    auto &J = s->adj;
+    J.K = n_steps;
+    J.C = ckpt_every;
+    J.args = *a;
+    J.objects.assign(objects, objects + n_objects);
+    J.saved_sort_interval = s->cfg.sort_interval;
+    int rc = do_sort(s);            // compact the slots once; no sort during the K steps
+    if (rc) return rc;
+    s->cfg.sort_interval = 1 << 30;
+    J.n = s->n_slots;
+    const size_t n = (size_t)J.n, nd = (size_t)s->ndof;
+    const int nck = (n_steps + ckpt_every - 1) / ckpt_every;
+    J.ck_x.resize(nck);
+    J.ck_c.resize(nck);
+    for (int k = 0; k < nck; ++k)
+        if ((rc = adj_alloc(s, (void **)&J.ck_x[k], sizeof(double) * 6 * n)) ||
+            (rc = adj_alloc(s, (void **)&J.ck_c[k], sizeof(int32_t) * n)))
+            return rc;
+    if ((rc = adj_alloc(s, (void **)&J.fin_x, sizeof(double) * 6 * n)) ||
+        (rc = adj_alloc(s, (void **)&J.fin_c, sizeof(int32_t) * n)) ||
+        (rc = adj_alloc(s, (void **)&J.rec_c, sizeof(int32_t) * (size_t)ckpt_every * n)) ||
+        (rc = adj_alloc(s, (void **)&J.bar, sizeof(double) * 6 * n)) ||
+        (rc = adj_alloc(s, (void **)&J.Ebar, sizeof(double) * 3 * (size_t)s->nc)) ||
+        (rc = adj_alloc(s, (void **)&J.phibar, sizeof(double) * nd)) ||
+        (rc = adj_alloc(s, (void **)&J.y, sizeof(double) * nd)) ||
+        (rc = adj_alloc(s, (void **)&J.rhobar, sizeof(double) * nd)) ||
+        (rc = adj_alloc(s, (void **)&J.target, sizeof(double) * nd)) ||
+        (rc = adj_alloc(s, (void **)&J.small, sizeof(double) * 16)))
+        return rc;
+    PG_CUDA(cudaMemcpyAsync(J.target, rho_target, sizeof(double) * nd, cudaMemcpyHostToDevice, s->stream));
+    int64_t live0 = 0, neg = 0, pos = 0;
+    if ((rc = pg_num_particles(s, &live0, &neg, &pos))) return rc;
+    std::vector<pg_object> obj = J.objects;
+    for (int k = 0; k < n_steps; ++k) {
+        if (k % ckpt_every == 0 && (rc = adj_save(s, J.ck_x[k / ckpt_every], J.ck_c[k / ckpt_every]))) return rc;
+        const pg_step_args ak = adj_step_args(s, k);
+        if ((rc = pg_step(s, &ak, obj.data(), (int32_t)obj.size(), nullptr))) return rc;
+    }
+    int64_t live1 = 0;
+    if ((rc = pg_num_particles(s, &live1, &neg, &pos))) return rc;
+    if (live1 != live0 || s->n_slots != J.n)
+        return fail(PG_ERR_ARG, "pg_adjoint_forward: particles were absorbed or added during the steps");
+    // rho_K and the loss ||rho_K - target||^2
+    rho_from_acc(s);
+    PG_CUDA(cudaMemsetAsync(J.small, 0, sizeof(double) * 16, s->stream));
+    launch_loss_grad(s->ndof, s->rho, J.target, J.rhobar, J.small + 3, s->stream);
+    if ((rc = adj_save(s, J.fin_x, J.fin_c))) return rc;
+    double l = 0;
+    PG_CUDA(cudaMemcpyAsync(&l, J.small + 3, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    if (loss) *loss = l;
+    J.ready = true;
+    return PG_OK;
+}
+
+// rhobar = M P A^+ P phibar (Dirichlet rows of phibar zeroed)
+static int adj_poisson(pg_sim *s) {
+    auto &J = s->adj;
+    if (s->has_dirichlet) launch_zero_dirichlet(s->ndof, s->bc_kind, J.phibar, s->stream);
+    PG_CUDA(cudaMemsetAsync(J.y, 0, sizeof(double) * s->ndof, s->stream));
+    PcgArgs a{};
+    a.n = s->ndof;
+    a.slice_ptr = s->A_sptr; a.slice_width = s->A_swidth; a.col = s->A_col; a.val = s->A_val; a.dinv = s->A_dinv;
+    a.b = J.phibar; a.x = J.y; a.r = s->r; a.z = s->z; a.p0 = s->p0; a.p1 = s->p1; a.Ap = s->Ap;
+    a.partials = s->pcg_part;
+    a.rtol = 1e-13; a.atol = 0.0;
+    a.max_iter = std::max(s->cfg.pcg_max_iter, 4000);
+    a.remove_mean = s->cfg.periodic ? 1 : 0;
+    a.out_iter = s->pcg_out_i; a.out_status = s->pcg_out_i + 1;
+    a.out_rr = s->pcg_out_d; a.out_bb = s->pcg_out_d + 1;
+    a.val32 = s->A_val32; a.dinv32 = s->A_dinv32;
+    a.r32 = s->r32; a.z32 = s->z32; a.p32 = s->p32; a.Ap32 = s->Ap32;
+    const int e = s->use_amg ? launch_pcg_amg(a, s->amg, s->stream) : launch_pcg(a, s->stream);
+    if (e) return fail(PG_ERR_CUDA, std::string("adjoint PCG launch: ") + cudaGetErrorString((cudaError_t)e));
+    launch_csr_matvec(s->ndof, s->M_row, s->M_col, s->M_val, J.y, J.rhobar, s->stream);
+    return PG_OK;
+}
+
+int pg_adjoint_backward(pg_sim *s, double *grad_v, int64_t n_out, double *grad_E0, double *grad_x0) {
+    if (!s) return fail(PG_ERR_ARG, "NULL handle");
+    auto &J = s->adj;
+    if (!J.ready) return fail(PG_ERR_STATE, "pg_adjoint_backward: call pg_adjoint_forward first");
+    const size_t n = (size_t)J.n;
+    double *xb = J.bar, *yb = J.bar + n, *zb = J.bar + 2 * n, *vxb = J.bar + 3 * n, *vyb = J.bar + 4 * n,
+           *vzb = J.bar + 5 * n;
+    const DevParticles &P = s->P[s->cur];
+    PG_CUDA(cudaMemsetAsync(J.bar, 0, sizeof(double) * 6 * n, s->stream));
+    PG_CUDA(cudaMemsetAsync(J.small, 0, sizeof(double) * 3, s->stream));
+    // d loss / d x_K through rho_K (cells at step K); rhobar holds 2 (rho_K - target)
+    launch_adj_deposit(s->dm, J.n, J.fin_c, P.sp, s->d_q, J.rhobar, xb, yb, zb, s->stream);
+    std::vector<pg_object> obj = J.objects;
+    int rc = PG_OK;
+    const int nck = (int)J.ck_x.size();
+    for (int seg = nck - 1; seg >= 0 && rc == PG_OK; --seg) {
+        const int k0 = seg * J.C, k1 = std::min(J.K, k0 + J.C);
+        // recompute the segment, recording the cells at the start of each step
+        if ((rc = adj_restore(s, J.ck_x[seg], J.ck_c[seg]))) break;
+        for (int k = k0; k < k1 && rc == PG_OK; ++k) {
+            PG_CUDA(cudaMemcpyAsync(J.rec_c + (size_t)(k - k0) * n, s->P[s->cur].cell, sizeof(int32_t) * n,
+                                    cudaMemcpyDeviceToDevice, s->stream));
+            const pg_step_args ak = adj_step_args(s, k);
+            rc = pg_step(s, &ak, obj.data(), (int32_t)obj.size(), nullptr);
+        }
+        if (rc) break;
+        for (int k = k1 - 1; k >= k0 && rc == PG_OK; --k) {
+            const pg_step_args ak = adj_step_args(s, k);
+            const double dt_push = ak.first_step ? 0.5 * ak.dt : ak.dt;
+            double coef[kMaxSpecies] = {0};
+            for (int sp = 0; sp < s->n_species; ++sp) coef[sp] = dt_push * (s->q[sp] / s->m[sp]);
+            PG_CUDA(cudaMemcpyAsync(J.small + 8, coef, sizeof(coef), cudaMemcpyHostToDevice, s->stream));
+            const int32_t *cells = J.rec_c + (size_t)(k - k0) * n;
+            PG_CUDA(cudaMemsetAsync(J.Ebar, 0, sizeof(double) * 3 * (size_t)s->nc, s->stream));
+            PG_CUDA(cudaMemsetAsync(J.phibar, 0, sizeof(double) * s->ndof, s->stream));
+            launch_adj_move_push(J.n, cells, P.sp, J.small + 8, ak.dt, xb, yb, zb, vxb, vyb, vzb, J.Ebar, J.small,
+                                 s->stream);
+            launch_adj_field(s->dm, J.Ebar, J.phibar, s->stream);
+            if ((rc = adj_poisson(s))) break;
+            launch_adj_deposit(s->dm, J.n, cells, P.sp, s->d_q, J.rhobar, xb, yb, zb, s->stream);
+        }
+    }
+    if (rc == PG_OK) {
+        if (grad_v || grad_x0) {
+            double *out = nullptr;
+            PG_CUDA(cudaMalloc(&out, sizeof(double) * 3 * std::max<int64_t>(1, n_out)));
+            cudaError_t e = cudaSuccess;
+            if (grad_v) {
+                cudaMemsetAsync(out, 0, sizeof(double) * 3 * n_out, s->stream);
+                launch_scatter_by_id(J.n, J.ck_c[0], P.pid, 0, n_out, vxb, vyb, vzb, out, s->stream);
+                e = cudaMemcpyAsync(grad_v, out, sizeof(double) * 3 * n_out, cudaMemcpyDeviceToHost, s->stream);
+            }
+            if (grad_x0 && e == cudaSuccess) {
+                cudaStreamSynchronize(s->stream);
+                cudaMemsetAsync(out, 0, sizeof(double) * 3 * n_out, s->stream);
+                launch_scatter_by_id(J.n, J.ck_c[0], P.pid, 0, n_out, xb, yb, zb, out, s->stream);
+                e = cudaMemcpyAsync(grad_x0, out, sizeof(double) * 3 * n_out, cudaMemcpyDeviceToHost, s->stream);
+            }
+            cudaStreamSynchronize(s->stream);
+            cudaFree(out);
+            if (e != cudaSuccess) rc = fail(PG_ERR_CUDA, cudaGetErrorString(e));
+        }
+        if (grad_E0) {
+            double g[3];
+            cudaMemcpyAsync(g, J.small, sizeof(g), cudaMemcpyDeviceToHost, s->stream);
+            cudaStreamSynchronize(s->stream);
+            for (int j = 0; j < 3; ++j) grad_E0[j] = g[j];
+        }
+    }
+    // back to the state after the K steps
+    int rc2 = adj_restore(s, J.fin_x, J.fin_c);
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    if (rc == PG_OK) rc = rc2;
+    if (rc == PG_OK) rc = check_state(s);
+    return rc;
+}
+
+int pg_adjoint_release(pg_sim *s) {
+    if (!s) return fail(PG_ERR_ARG, "NULL handle");
+    if (s->adj.ready) s->cfg.sort_interval = s->adj.saved_sort_interval;
+    adj_free(s);
+    return PG_OK;
 }
 
 int pg_step(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_objects, pg_step_result *res) {

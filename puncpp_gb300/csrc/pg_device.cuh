@@ -326,6 +326,21 @@ void launch_step_record(double *rows, int row_len, int64_t *counts, const double
                         cudaStream_t s);
 void launch_set_count(int64_t *counts, const int64_t *cursor, int32_t nc, cudaStream_t s);
 
+// adjoint of the fused steps (k_adjoint.cu)
+void launch_adj_deposit(const DevMesh &m, int64_t n, const int32_t *cell, const uint8_t *sp, const double *q,
+                        const double *rhobar, double *xb, double *yb, double *zb, cudaStream_t st);
+void launch_adj_move_push(int64_t n, const int32_t *cell, const uint8_t *sp, const double *coef, double dt,
+                          const double *xb, const double *yb, const double *zb, double *vxb, double *vyb, double *vzb,
+                          double *Ebar, double *e0bar, cudaStream_t st);
+void launch_adj_field(const DevMesh &m, const double *Ebar, double *phibar, cudaStream_t st);
+void launch_csr_matvec(int32_t n, const int32_t *row, const int32_t *col, const double *val, const double *x,
+                       double *y, cudaStream_t st);
+void launch_zero_dirichlet(int32_t n, const int32_t *bc_kind, double *v, cudaStream_t st);
+void launch_loss_grad(int32_t n, const double *rho, const double *target, double *rhobar, double *loss,
+                      cudaStream_t st);
+void launch_scatter_by_id(int64_t n, const int32_t *cell, const int64_t *pid, int64_t pid_base, int64_t n_out,
+                          const double *a, const double *b, const double *c, double *out, cudaStream_t st);
+
 // mixed-precision form
 void launch_mixed_pass(const DevMesh &m, const DevParticles &p, int64_t n_slots, const MixedParams &mp, bool push,
                        bool move, bool walk, bool deposit, int max_steps, unsigned long long *rho_fixed,

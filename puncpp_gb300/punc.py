@@ -533,6 +533,27 @@ def autotune(pop: Population, objects, dt: float, steps_per_trial: int = 2, B=(0
     return _tuning_dict(t)
 
 
+def adjoint_forward(pop: Population, objects, dt: float, n_steps: int, ckpt_every: int, rho_target,
+                    first_step=True, use_accel=False, E0=(0.0, 0.0, 0.0), Ld=None, step_no=0) -> float:
+    """K fused steps keeping checkpoints; returns ||rho_K - rho_target||^2."""
+    a = L.StepArgs(dt, (C.c_double * 3)(0.0, 0.0, 0.0), 1 if first_step else 0, 1 if use_accel else 0,
+                   0 if Ld is None else 1, (C.c_double * 3)(*(Ld if Ld is not None else (0.0, 0.0, 0.0))),
+                   0, 0, step_no, (C.c_double * 3)(*E0), 0)
+    arr = _objects_in(objects)
+    tgt = np.ascontiguousarray(rho_target, np.float64)
+    loss = C.c_double()
+    L.check(L.load().pg_adjoint_forward(pop.handle, C.byref(a), arr, len(objects), n_steps, ckpt_every, L.dptr(tgt),
+                                        C.byref(loss)))
+    return loss.value
+
+
+def adjoint_backward(pop: Population, n_particles: int):
+    """(grad wrt initial velocities [n][3], wrt E0 [3], wrt initial positions [n][3]), by particle id."""
+    gv, gx, ge = np.zeros((n_particles, 3)), np.zeros((n_particles, 3)), np.zeros(3)
+    L.check(L.load().pg_adjoint_backward(pop.handle, L.dptr(gv), n_particles, L.dptr(ge), L.dptr(gx)))
+    return gv, ge, gx
+
+
 def stage_times(pop: Population) -> dict:
     lib = L.load()
     n = C.c_int32()
