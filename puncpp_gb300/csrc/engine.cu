@@ -1,5 +1,6 @@
 // The pg_sim handle: device-resident mesh, particles, fields and solver,
 // and the C ABI entry points of punc_gpu.h.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -391,50 +392,111 @@ static int lanes_per_row(const Csr &A) {
     return g;
 }
 
-// Upload a CSR operator in FP32: SELL-32 (padding: column 0, value 0) when
-// g == 1, else CSR.
-static int upload_op(pg_sim *s, const Csr &A, int g, SpOp &out) {
+// Upload a CSR operator: SELL-32 (padding: the slice's first column, value
+// 0) when g == 1, else CSR.  c16: 16-bit column offsets from the smallest
+// column of each slice (SELL) or row (CSR), when every span fits in 16 bits;
+// v16: IEEE binary16 values of v / vscale with vscale = max|v| / 1024 (the
+// preconditioner's operators; binary16 keeps 11 significant bits, and halving
+// the bytes keeps the hierarchy of large meshes resident in L2).
+static int upload_op(pg_sim *s, const Csr &A, int g, SpOp &out, bool want_c16 = false, bool want_v16 = false) {
     const int64_t n = A.n;
     int rc;
+    out = SpOp{};
     out.n = (int32_t)n;
     out.g = g;
+    std::vector<int64_t> ptr;     // slice or row offsets
+    std::vector<int32_t> swidth;
+    std::vector<int32_t> col;
+    std::vector<double> val;
+    std::vector<int32_t> base;    // smallest column per slice or row
     if (g > 1) {
-        std::vector<float> val(A.v.begin(), A.v.end());
-        if (val.empty()) val.push_back(0.0f);
-        std::vector<int32_t> col(A.ci);
-        if (col.empty()) col.push_back(0);
-        int64_t *d_ptr; int32_t *d_col; float *d_val;
-        if ((rc = upload(s, &d_ptr, A.rp)) || (rc = upload(s, &d_col, col)) || (rc = upload(s, &d_val, val))) return rc;
-        out.ptr = d_ptr; out.swidth = nullptr; out.col = d_col; out.val = d_val;
-        return PG_OK;
-    }
-    const int64_t nsl = (n + 31) / 32;
-    std::vector<int64_t> sptr(nsl + 1, 0);
-    std::vector<int32_t> swidth(nsl, 0);
-    for (int64_t sl = 0; sl < nsl; ++sl) {
-        int64_t w = 0;
-        for (int64_t r = 32 * sl; r < std::min(n, 32 * sl + 32); ++r) w = std::max(w, A.rp[r + 1] - A.rp[r]);
-        swidth[sl] = (int32_t)w;
-        sptr[sl + 1] = sptr[sl] + 32 * w;
-    }
-    std::vector<int32_t> col(std::max<int64_t>(1, sptr[nsl]), 0);
-    std::vector<float> val(std::max<int64_t>(1, sptr[nsl]), 0.0f);
-    for (int64_t sl = 0; sl < nsl; ++sl)
-        for (int lane = 0; lane < 32; ++lane) {
-            const int64_t r = 32 * sl + lane;
-            if (r >= n) continue;
-            const int64_t len = A.rp[r + 1] - A.rp[r];
-            for (int64_t k = 0; k < len; ++k) {
-                const int64_t o = sptr[sl] + 32 * k + lane;
-                col[o] = A.ci[A.rp[r] + k];
-                val[o] = (float)A.v[A.rp[r] + k];
+        ptr.assign(A.rp.begin(), A.rp.end());
+        col.assign(A.ci.begin(), A.ci.end());
+        val.assign(A.v.begin(), A.v.end());
+        base.assign(n, 0);
+        for (int64_t r = 0; r < n; ++r)
+            if (A.rp[r + 1] > A.rp[r]) base[r] = *std::min_element(A.ci.begin() + A.rp[r], A.ci.begin() + A.rp[r + 1]);
+    } else {
+        const int64_t nsl = (n + 31) / 32;
+        ptr.assign(nsl + 1, 0);
+        swidth.assign(nsl, 0);
+        base.assign(nsl, 0);
+        for (int64_t sl = 0; sl < nsl; ++sl) {
+            int64_t w = 0;
+            int32_t b = INT32_MAX;
+            for (int64_t r = 32 * sl; r < std::min(n, 32 * sl + 32); ++r) {
+                w = std::max(w, A.rp[r + 1] - A.rp[r]);
+                for (int64_t k = A.rp[r]; k < A.rp[r + 1]; ++k) b = std::min(b, A.ci[k]);
             }
+            swidth[sl] = (int32_t)w;
+            base[sl] = b == INT32_MAX ? 0 : b;
+            ptr[sl + 1] = ptr[sl] + 32 * w;
         }
-    int64_t *d_sptr; int32_t *d_sw, *d_col; float *d_val;
-    if ((rc = upload(s, &d_sptr, sptr)) || (rc = upload(s, &d_sw, swidth)) || (rc = upload(s, &d_col, col)) ||
-        (rc = upload(s, &d_val, val)))
-        return rc;
-    out.ptr = d_sptr; out.swidth = d_sw; out.col = d_col; out.val = d_val;
+        col.assign(std::max<int64_t>(1, ptr[nsl]), 0);
+        val.assign(std::max<int64_t>(1, ptr[nsl]), 0.0);
+        for (int64_t sl = 0; sl < nsl; ++sl)
+            for (int64_t o = ptr[sl]; o < ptr[sl + 1]; ++o) col[o] = base[sl];
+        for (int64_t sl = 0; sl < nsl; ++sl)
+            for (int lane = 0; lane < 32; ++lane) {
+                const int64_t r = 32 * sl + lane;
+                if (r >= n) continue;
+                const int64_t len = A.rp[r + 1] - A.rp[r];
+                for (int64_t k = 0; k < len; ++k) {
+                    const int64_t o = ptr[sl] + 32 * k + lane;
+                    col[o] = A.ci[A.rp[r] + k];
+                    val[o] = A.v[A.rp[r] + k];
+                }
+            }
+    }
+    if (ptr.back() > (int64_t)INT32_MAX) return fail(PG_ERR_ARG, "operator with 2^31 or more stored entries");
+    if (col.empty()) col.push_back(0);
+    if (val.empty()) val.push_back(0.0);
+    bool c16 = want_c16;
+    if (c16) {
+        const int64_t units = (int64_t)base.size();
+        for (int64_t u = 0; u < units && c16; ++u)
+            for (int64_t o = ptr[u]; o < ptr[u + 1]; ++o)
+                if ((int64_t)col[o] - base[u] > 65535) { c16 = false; break; }
+    }
+    int64_t *d_ptr;
+    if ((rc = upload(s, &d_ptr, ptr))) return rc;
+    out.ptr = d_ptr;
+    if (g == 1) {
+        int32_t *d_sw;
+        if ((rc = upload(s, &d_sw, swidth))) return rc;
+        out.swidth = d_sw;
+    }
+    if (c16) {
+        std::vector<uint16_t> c(col.size(), 0);
+        const int64_t units = (int64_t)base.size();
+        for (int64_t u = 0; u < units; ++u)
+            for (int64_t o = ptr[u]; o < ptr[u + 1]; ++o) c[o] = (uint16_t)(col[o] - base[u]);
+        uint16_t *d_c;
+        int32_t *d_b;
+        if ((rc = upload(s, &d_c, c)) || (rc = upload(s, &d_b, base))) return rc;
+        out.col16 = d_c;
+        out.cbase = d_b;
+    } else {
+        int32_t *d_col;
+        if ((rc = upload(s, &d_col, col))) return rc;
+        out.col = d_col;
+    }
+    if (want_v16) {
+        double vmax = 0.0;
+        for (double v : val) vmax = std::max(vmax, std::fabs(v));
+        const double sc = vmax > 0.0 ? vmax / 1024.0 : 1.0;
+        std::vector<uint16_t> h(val.size());
+        for (size_t k = 0; k < val.size(); ++k) h[k] = __half_as_ushort(__float2half_rn((float)(val[k] / sc)));
+        uint16_t *d_h;
+        if ((rc = upload(s, &d_h, h))) return rc;
+        out.val16 = d_h;
+        out.vscale = (float)sc;
+    } else {
+        std::vector<float> v32(val.begin(), val.end());
+        float *d_val;
+        if ((rc = upload(s, &d_val, v32))) return rc;
+        out.val = d_val;
+    }
     return PG_OK;
 }
 
@@ -466,6 +528,7 @@ static int setup_amg(pg_sim *s, const std::vector<int32_t> &arow, const std::vec
     s->amg_nnz_p.assign(M.nlev, 0);
     int rc;
     if (L >= 1 && (rc = dalloc(s, &M.stack, cyc.stack_len))) return rc;
+    if ((rc = dalloc(s, &M.r_alt, h.levels[0].A.n))) return rc;
     for (int l = 0; l < M.nlev; ++l) {
         const AmgLevel &Lv = h.levels[l];
         s->amg_rows[l] = Lv.A.n;
@@ -473,21 +536,21 @@ static int setup_amg(pg_sim *s, const std::vector<int32_t> &arow, const std::vec
         if (l < L) s->amg_nnz_p[l] = (int64_t)Lv.S.ci.size();
         AmgLevelDev &D = M.lev[l];
         if (l == 0) {
-            // the PCG's own product reads level 0's operator, also when L == 0
-            D.A.n = (int32_t)Lv.A.n; D.A.g = 1;
-            D.A.ptr = s->A_sptr; D.A.swidth = s->A_swidth; D.A.col = s->A_col; D.A.val = s->A_val32;
+            // the PCG's own product A p reads level 0's operator, also when
+            // L == 0: FP32 values (the Krylov recurrence), 16-bit columns
+            if ((rc = upload_op(s, Lv.A, 1, D.A, true, false))) return rc;
             D.dinv = s->A_dinv32;
         }
         if (l == L) break;   // the coarsest level lives in G (or cinv when L == 0)
         if (l > 0) {
-            if ((rc = upload_op(s, Lv.A, lanes_per_row(Lv.A), D.A))) return rc;
+            if ((rc = upload_op(s, Lv.A, lanes_per_row(Lv.A), D.A, true, true))) return rc;
             std::vector<float> dinv(Lv.dinv.begin(), Lv.dinv.end());
             float *d_dinv;
             if ((rc = upload(s, &d_dinv, dinv)) || (rc = dalloc(s, &D.b, Lv.A.n))) return rc;
             D.dinv = d_dinv;
         }
         D.omega = (float)Lv.omega;
-        if (l < L - 1 && (rc = upload_op(s, Lv.ST, lanes_per_row(Lv.ST), D.ST))) return rc;
+        if (l < L - 1 && (rc = upload_op(s, Lv.ST, lanes_per_row(Lv.ST), D.ST, true, true))) return rc;
         if (l >= 2) D.t = M.stack + cyc.stack_off[l];
         else if ((rc = dalloc(s, &D.t, Lv.A.n))) return rc;
     }
@@ -503,11 +566,11 @@ static int setup_amg(pg_sim *s, const std::vector<int32_t> &arow, const std::vec
         C.v = h.coarse_inv;
         if ((rc = upload_op(s, C, lanes_per_row(C), M.cinv))) return rc;
     } else {
-        if ((rc = upload_op(s, h.levels[0].S, lanes_per_row(h.levels[0].S), M.S0)) ||
+        if ((rc = upload_op(s, h.levels[0].S, lanes_per_row(h.levels[0].S), M.S0, true, true)) ||
             (rc = upload_op(s, cyc.G, lanes_per_row(cyc.G), M.G)))
             return rc;
         M.yL = L >= 2 ? M.stack + cyc.stack_off[L] : M.stack;
-        if (L >= 2 && ((rc = upload_op(s, cyc.U1, lanes_per_row(cyc.U1), M.U1)) ||
+        if (L >= 2 && ((rc = upload_op(s, cyc.U1, lanes_per_row(cyc.U1), M.U1, true, true)) ||
                        (rc = dalloc(s, &M.y1, h.levels[1].A.n))))
             return rc;
     }

@@ -14,9 +14,14 @@
 // (G = C^-1 S^T) and the up-sweep of levels >= 1 collapsed into one product
 // (U1 = [S_1 | S_1 S_2 | ...]): L + 1 grid-wide phases for L >= 2 levels
 // above the coarsest.  The product A z of the search direction update is
-// folded into the next matrix phase (A p = A z + beta A p_old) and r.z into
-// the last V-cycle phase: an iteration is L + 3 grid barriers.
+// folded into the next matrix phase (A p = A z + beta A p_old), r.z into the
+// last cycle phase, and the x and r update of a CG step into the cycle's
+// first phase (r - alpha Ap gathered on the fly, two residual buffers): an
+// iteration is L + 2 grid barriers.  The smoothing products W_l b_l, needed
+// only by the up-sweep, run in the down-sweep phases whose restrictions are
+// small.
 #include <cooperative_groups.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "pg_device.cuh"
@@ -32,119 +37,164 @@ namespace {
 // only after a grid barrier, whose acquire makes the other blocks' writes
 // visible; never through the read-only path (__ldg).
 //
-// epi(i, sum_j S_ij xv(j)) for every row i of S, spread over the whole grid.
-// SELL operators take one thread per row, two rows at a time; CSR operators g
-// lanes per row, reduced by warp shuffles (g <= 32) and through shared memory
-// (g = 64..512, the warps of one block).  The loads of four entries are
-// issued before their products so that a lane keeps several gathers in
-// flight (the kernel runs at 32 warps per SM and is latency-bound otherwise).
-// Every thread of the grid must call this (the CSR path runs the same number
+// epi(i, sum_j S_ij xv(j), pre(i)) for every row i of S, spread over the
+// whole grid.  pre(i) loads the epilogue's own operands of row i before the
+// row's gathers start.  A phase is a chain of dependent L2 round trips (row
+// offsets -> column indices -> gathered values), so each thread keeps eight
+// gathers in flight: SELL operators take one thread per row and four rows at
+// a time, two entries of each per step; CSR operators g lanes per row, four
+// rows per lane group at a time, reduced by warp shuffles (g <= 32), or the
+// warps of one block per row, reduced through shared memory (g = 64..512).
+// Every thread of the grid must call this (the CSR paths run the same number
 // of rounds in all lanes so the shuffles are full-warp).
+struct NoPre {
+    __device__ __forceinline__ int operator()(int) const { return 0; }
+};
+
+constexpr int kRows = 4;   // rows per thread (SELL) or per lane group (CSR) at a time
+
+// Column and value of stored entry o (b: the entry's slice or row base) in
+// the operator's storage form.
+template <bool C16, bool V16>
+struct Entry {
+    __device__ static __forceinline__ int col(const SpOp &S, int o, int b) {
+        return C16 ? b + (int)__ldg(S.col16 + o) : __ldg(S.col + o);
+    }
+    __device__ static __forceinline__ float val(const SpOp &S, int o) {
+        return V16 ? __half2float(__ushort_as_half(__ldg(S.val16 + o))) : __ldg(S.val + o);
+    }
+};
+
 // This lane's share (entries lane, lane + g, ...) of row i of a CSR operator,
 // four entries' loads issued before their products.
-template <class XV>
+template <bool C16, bool V16, class XV>
 __device__ __forceinline__ float csr_lane_sum(const SpOp &S, int i, int lane, int g, XV xv) {
-    const int64_t k0 = __ldg(S.ptr + i);
-    const int len = (int)(__ldg(S.ptr + i + 1) - k0);
-    const int32_t *cp = S.col + k0;
-    const float *vp = S.val + k0;
+    using E = Entry<C16, V16>;
+    const int k0 = (int)__ldg(S.ptr + i);
+    const int len = (int)__ldg(S.ptr + i + 1) - k0;
+    const int b = C16 ? __ldg(S.cbase + i) : 0;
     float s0 = 0.0f, s1 = 0.0f;
     int k = lane;
     for (; k + 3 * g < len; k += 4 * g) {
-        const int c0 = __ldg(cp + k), c1 = __ldg(cp + k + g);
-        const int c2 = __ldg(cp + k + 2 * g), c3 = __ldg(cp + k + 3 * g);
-        const float v0 = __ldg(vp + k), v1 = __ldg(vp + k + g);
-        const float v2 = __ldg(vp + k + 2 * g), v3 = __ldg(vp + k + 3 * g);
+        const int c0 = E::col(S, k0 + k, b), c1 = E::col(S, k0 + k + g, b);
+        const int c2 = E::col(S, k0 + k + 2 * g, b), c3 = E::col(S, k0 + k + 3 * g, b);
+        const float v0 = E::val(S, k0 + k), v1 = E::val(S, k0 + k + g);
+        const float v2 = E::val(S, k0 + k + 2 * g), v3 = E::val(S, k0 + k + 3 * g);
         const float x0 = xv(c0), x1 = xv(c1), x2 = xv(c2), x3 = xv(c3);
         s0 = fmaf(v0, x0, s0);
         s1 = fmaf(v1, x1, s1);
         s0 = fmaf(v2, x2, s0);
         s1 = fmaf(v3, x3, s1);
     }
-    for (; k < len; k += g) s0 = fmaf(__ldg(vp + k), xv(__ldg(cp + k)), s0);
+    for (; k < len; k += g) s0 = fmaf(E::val(S, k0 + k), xv(E::col(S, k0 + k, b)), s0);
     return s0 + s1;
 }
 
-// Two rows' lane shares at once (row ib may be absent: ib < 0), so that a
-// lane keeps four gathers in flight across the two rows.
-template <class XV>
-__device__ __forceinline__ void csr_lane_sum2(const SpOp &S, int ia, int ib, int lane, int g, XV xv, float &ra,
-                                              float &rb) {
-    const int64_t ka = __ldg(S.ptr + ia);
-    const int la = (int)(__ldg(S.ptr + ia + 1) - ka);
-    int64_t kb = 0;
-    int lb = 0;
-    if (ib >= 0) {
-        kb = __ldg(S.ptr + ib);
-        lb = (int)(__ldg(S.ptr + ib + 1) - kb);
-    }
-    const int32_t *ca = S.col + ka, *cb = S.col + kb;
-    const float *va = S.val + ka, *vb = S.val + kb;
-    const int len = la > lb ? la : lb;
-    float sa = 0.0f, sb = 0.0f;
-    for (int k = lane; k < len; k += 2 * g) {
-        const int k1 = k + g;
-        const int c0 = k < la ? __ldg(ca + k) : -1, c1 = k1 < la ? __ldg(ca + k1) : -1;
-        const int d0 = k < lb ? __ldg(cb + k) : -1, d1 = k1 < lb ? __ldg(cb + k1) : -1;
-        const float v0 = k < la ? __ldg(va + k) : 0.0f, v1 = k1 < la ? __ldg(va + k1) : 0.0f;
-        const float w0 = k < lb ? __ldg(vb + k) : 0.0f, w1 = k1 < lb ? __ldg(vb + k1) : 0.0f;
-        const float x0 = c0 >= 0 ? xv(c0) : 0.0f, x1 = c1 >= 0 ? xv(c1) : 0.0f;
-        const float y0 = d0 >= 0 ? xv(d0) : 0.0f, y1 = d1 >= 0 ? xv(d1) : 0.0f;
-        sa = fmaf(v0, x0, sa);
-        sb = fmaf(w0, y0, sb);
-        sa = fmaf(v1, x1, sa);
-        sb = fmaf(w1, y1, sb);
-    }
-    ra = sa;
-    rb = sb;
-}
-
-template <class XV, class EPI>
-__device__ __forceinline__ void apply(const SpOp &S, XV xv, EPI epi, int t0, int ts) {
+template <bool C16, bool V16, class XV, class PRE, class EPI>
+__device__ __forceinline__ void apply_t(const SpOp &S, XV xv, PRE pre, EPI epi, int t0, int ts) {
+    using P = decltype(pre(0));
+    using E = Entry<C16, V16>;
+    const float vs = V16 ? S.vscale : 1.0f;
     if (S.g == 1) {
-        for (int i = t0; i < S.n; i += 2 * ts) {
-            const int i2 = i + ts;
-            const int64_t ba = __ldg(S.ptr + (i >> 5)) + (i & 31);
-            const int wa = __ldg(S.swidth + (i >> 5));
-            const bool two = i2 < S.n;
-            const int64_t bb = two ? __ldg(S.ptr + (i2 >> 5)) + (i2 & 31) : 0;
-            const int wb = two ? __ldg(S.swidth + (i2 >> 5)) : 0;
-            float sa = 0.0f, sb = 0.0f;
-            const int w = wa > wb ? wa : wb;
-            for (int k = 0; k < w; k += 2) {
-                // entries k, k+1 of both rows (padding entries are zero)
-                const bool a0 = k < wa, a1 = k + 1 < wa, b0 = k < wb, b1 = k + 1 < wb;
-                const int64_t oa = ba + 32 * k, ob = bb + 32 * k;
-                const int ca0 = a0 ? __ldg(S.col + oa) : 0, ca1 = a1 ? __ldg(S.col + oa + 32) : 0;
-                const int cb0 = b0 ? __ldg(S.col + ob) : 0, cb1 = b1 ? __ldg(S.col + ob + 32) : 0;
-                const float va0 = a0 ? __ldg(S.val + oa) : 0.0f, va1 = a1 ? __ldg(S.val + oa + 32) : 0.0f;
-                const float vb0 = b0 ? __ldg(S.val + ob) : 0.0f, vb1 = b1 ? __ldg(S.val + ob + 32) : 0.0f;
-                const float xa0 = a0 ? xv(ca0) : 0.0f, xa1 = a1 ? xv(ca1) : 0.0f;
-                const float xb0 = b0 ? xv(cb0) : 0.0f, xb1 = b1 ? xv(cb1) : 0.0f;
-                sa = fmaf(va0, xa0, sa);
-                sb = fmaf(vb0, xb0, sb);
-                sa = fmaf(va1, xa1, sa);
-                sb = fmaf(vb1, xb1, sb);
+        for (int i = t0; i < S.n; i += kRows * ts) {
+            int off[kRows];   // operators hold fewer than 2^31 entries (checked at upload)
+            int wid[kRows], cb[kRows];
+            P pv[kRows];
+            int w = 0;
+#pragma unroll
+            for (int q = 0; q < kRows; ++q) {
+                const int r = i + q * ts;
+                const bool ok = r < S.n;
+                off[q] = ok ? (int)__ldg(S.ptr + (r >> 5)) + (r & 31) : 0;
+                wid[q] = ok ? __ldg(S.swidth + (r >> 5)) : 0;
+                cb[q] = (ok && C16) ? __ldg(S.cbase + (r >> 5)) : 0;
+                pv[q] = ok ? pre(r) : P{};
+                w = wid[q] > w ? wid[q] : w;
             }
-            epi(i, sa);
-            if (two) epi(i2, sb);
+            float sum[kRows];
+#pragma unroll
+            for (int q = 0; q < kRows; ++q) sum[q] = 0.0f;
+            for (int k = 0; k < w; k += 2) {
+                // entries k, k + 1 of the four rows (slice padding: value 0)
+                int c[kRows][2];
+                float v[kRows][2], x[kRows][2];
+#pragma unroll
+                for (int q = 0; q < kRows; ++q)
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) {
+                        const bool ok = k + e < wid[q];
+                        const int o = off[q] + 32 * (k + e);
+                        c[q][e] = ok ? E::col(S, o, cb[q]) : -1;
+                        v[q][e] = ok ? E::val(S, o) : 0.0f;
+                    }
+#pragma unroll
+                for (int q = 0; q < kRows; ++q)
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) x[q][e] = c[q][e] >= 0 ? xv(c[q][e]) : 0.0f;
+#pragma unroll
+                for (int q = 0; q < kRows; ++q)
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) sum[q] = fmaf(v[q][e], x[q][e], sum[q]);
+            }
+#pragma unroll
+            for (int q = 0; q < kRows; ++q)
+                if (i + q * ts < S.n) epi(i + q * ts, V16 ? sum[q] * vs : sum[q], pv[q]);
         }
     } else if (S.g <= 32) {
         const int g = S.g;
         const int lane = t0 & (g - 1);
         const int grp = t0 / g, ngrp = ts / g;
         const int rounds = (S.n + ngrp - 1) / ngrp;
-        for (int t = 0; t < rounds; t += 2) {
-            // rounds t and t + 1 together
-            const int i = grp + t * ngrp, i2 = i + ngrp;
-            float s = 0.0f, s2 = 0.0f;
-            if (i < S.n) csr_lane_sum2(S, i, i2 < S.n ? i2 : -1, lane, g, xv, s, s2);
-            for (int o = g >> 1; o > 0; o >>= 1) {
-                s += __shfl_xor_sync(0xffffffffu, s, o);
-                s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        for (int t = 0; t < rounds; t += kRows) {
+            // rounds t .. t + 3 together
+            int off[kRows];
+            int len[kRows], cb[kRows];
+            P pv[kRows];
+            int L = 0;
+#pragma unroll
+            for (int q = 0; q < kRows; ++q) {
+                const int r = grp + (t + q) * ngrp;
+                const bool ok = r < S.n;
+                off[q] = ok ? (int)__ldg(S.ptr + r) : 0;
+                len[q] = ok ? (int)__ldg(S.ptr + r + 1) - off[q] : 0;
+                cb[q] = (ok && C16) ? __ldg(S.cbase + r) : 0;
+                pv[q] = (ok && lane == 0) ? pre(r) : P{};
+                L = len[q] > L ? len[q] : L;
             }
-            if (lane == 0 && i < S.n) epi(i, s);
-            if (lane == 0 && i2 < S.n) epi(i2, s2);
+            float sum[kRows];
+#pragma unroll
+            for (int q = 0; q < kRows; ++q) sum[q] = 0.0f;
+            for (int k = lane; k < L; k += 2 * g) {
+                int c[kRows][2];
+                float v[kRows][2], x[kRows][2];
+#pragma unroll
+                for (int q = 0; q < kRows; ++q)
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) {
+                        const int kk = k + e * g;
+                        const bool ok = kk < len[q];
+                        c[q][e] = ok ? E::col(S, off[q] + kk, cb[q]) : -1;
+                        v[q][e] = ok ? E::val(S, off[q] + kk) : 0.0f;
+                    }
+#pragma unroll
+                for (int q = 0; q < kRows; ++q)
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) x[q][e] = c[q][e] >= 0 ? xv(c[q][e]) : 0.0f;
+#pragma unroll
+                for (int q = 0; q < kRows; ++q)
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) sum[q] = fmaf(v[q][e], x[q][e], sum[q]);
+            }
+#pragma unroll
+            for (int q = 0; q < kRows; ++q)
+                for (int o = g >> 1; o > 0; o >>= 1) sum[q] += __shfl_xor_sync(0xffffffffu, sum[q], o);
+            if (lane == 0) {
+#pragma unroll
+                for (int q = 0; q < kRows; ++q) {
+                    const int r = grp + (t + q) * ngrp;
+                    if (r < S.n) epi(r, V16 ? sum[q] * vs : sum[q], pv[q]);
+                }
+            }
         }
     } else {
         // g / 32 warps of one block per row; partial sums meet in shared memory
@@ -157,43 +207,127 @@ __device__ __forceinline__ void apply(const SpOp &S, XV xv, EPI epi, int t0, int
         const int rounds = (S.n + ngrp - 1) / ngrp;
         for (int t = 0; t < rounds; ++t) {
             const int i = grp + t * ngrp;
-            float s = i < S.n ? csr_lane_sum(S, i, lane, g, xv) : 0.0f;
+            float s = i < S.n ? csr_lane_sum<C16, V16>(S, i, lane, g, xv) : 0.0f;
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
             if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
             __syncthreads();
             if (lane == 0 && i < S.n) {
                 float tot = 0.0f;
                 for (int w = 0; w < g / 32; ++w) tot += red[(threadIdx.x >> 5) + w];
-                epi(i, tot);
+                epi(i, V16 ? tot * vs : tot, pre(i));
             }
             __syncthreads();
         }
     }
 }
 
-// z = B r over the whole grid, r complete on entry; returns this thread's
-// share of r.z.  Level 0's b is r.
-__device__ double vcycle(const AmgDev &M, const float *r, float *z, cg::grid_group &grid, int t0, int ts) {
+// epi(i, (S xv)_i, pre(i)) over the whole grid, in the operator's storage
+// form (uniform branch).
+template <class XV, class PRE, class EPI>
+__device__ __forceinline__ void apply(const SpOp &S, XV xv, PRE pre, EPI epi, int t0, int ts) {
+    if (S.col16) {
+        if (S.val16) apply_t<true, true>(S, xv, pre, epi, t0, ts);
+        else apply_t<true, false>(S, xv, pre, epi, t0, ts);
+    } else {
+        if (S.val16) apply_t<false, true>(S, xv, pre, epi, t0, ts);
+        else apply_t<false, false>(S, xv, pre, epi, t0, ts);
+    }
+}
+
+// The residual as phase 0 of a V-cycle reads it: right after a CG step the
+// step's update r - alpha Ap is formed on the fly from the previous residual
+// (the same FP32 expression the rows' owners store), so the update needs no
+// phase of its own.
+template <bool kMerge>
+struct ResGather {
+    const float *r, *Ap;
+    float alpha;
+    __device__ __forceinline__ float operator()(int j) const { return kMerge ? fmaf(-alpha, Ap[j], r[j]) : r[j]; }
+};
+
+// t = W x for level Lv: W = w D^-1 (2 I - A w D^-1), xg(j) the input vector.
+template <class XG>
+__device__ __forceinline__ void smooth(const AmgLevelDev &Lv, XG xg, float *t, int t0, int ts) {
+    const float om = Lv.omega;
+    const float *dinv = Lv.dinv;
+    apply(Lv.A, [=](int j) { return om * __ldg(dinv + j) * xg(j); },
+          [=](int i) { return make_float2(__ldg(dinv + i), xg(i)); },
+          [=](int i, float s, float2 dx) { t[i] = om * dx.x * (2.0f * dx.y - s); }, t0, ts);
+}
+
+// Phase 0 of z = B r: the first restriction b_1 = S_0^T r (L >= 2), or
+// y_L = G r and t_0 = W_0 r (L == 1), or z = C^-1 r (L == 0, returning this
+// thread's share of r.z).  With kMerge, the CG step's x += alpha p and
+// r_new = r - alpha Ap of this thread's rows (r_new into rn) and ||r_new||^2
+// (into rr) run in the same phase.
+template <bool kMerge>
+__device__ double vcycle_phase0(const AmgDev &M, const PcgArgs &a, const float *r, float *rn, double alpha,
+                                float *z, float &rr, int t0, int ts) {
+    const int n = a.n;
+    const float alpha32 = (float)alpha;
+    const ResGather<kMerge> gr{r, a.Ap32, alpha32};
+    if (kMerge) {
+        float acc = 0.0f;
+        for (int i = t0; i < n; i += 2 * ts) {
+            // two rows per pass, loads first
+            const int i2 = i + ts;
+            const bool two = i2 < n;
+            const double x1 = a.x[i];
+            const float p1 = a.p32[i], q1 = a.Ap32[i], r1 = r[i];
+            const double x2 = two ? a.x[i2] : 0.0;
+            const float p2 = two ? a.p32[i2] : 0.0f, q2 = two ? a.Ap32[i2] : 0.0f;
+            const float r2 = two ? r[i2] : 0.0f;
+            const float n1 = fmaf(-alpha32, q1, r1), n2 = fmaf(-alpha32, q2, r2);
+            a.x[i] = fma(alpha, (double)p1, x1);
+            rn[i] = n1;
+            acc = fmaf(n1, n1, acc);
+            if (two) {
+                a.x[i2] = fma(alpha, (double)p2, x2);
+                rn[i2] = n2;
+                acc = fmaf(n2, n2, acc);
+            }
+        }
+        rr = acc;
+    }
     const int L = M.nlev - 1;
     double rz = 0.0;
     if (L == 0) {
-        apply(M.cinv, [=](int j) { return r[j]; },
-              [&](int i, float s) { z[i] = s; rz = fma((double)s, (double)r[i], rz); }, t0, ts);
-        return rz;
+        apply(M.cinv, gr, [=](int i) { return gr(i); },
+              [&](int i, float s, float ri) { z[i] = s; rz = fma((double)s, (double)ri, rz); }, t0, ts);
+    } else if (L == 1) {
+        float *yL = M.yL;
+        apply(M.G, gr, NoPre{}, [=](int i, float s, int) { yL[i] = s; }, t0, ts);
+        smooth(M.lev[0], gr, M.lev[0].t, t0, ts);
+    } else {
+        float *b1 = M.lev[1].b;
+        apply(M.lev[0].ST, gr, NoPre{}, [=](int i, float s, int) { b1[i] = s; }, t0, ts);
     }
-    for (int l = 0; l < L; ++l) {
-        const float *b = l == 0 ? r : M.lev[l].b;
-        const float om = M.lev[l].omega;
-        const float *dinv = M.lev[l].dinv;
-        float *t = M.lev[l].t;
-        apply(M.lev[l].A, [=](int j) { return om * __ldg(dinv + j) * b[j]; },
-              [=](int i, float s) { t[i] = om * __ldg(dinv + i) * (2.0f * b[i] - s); }, t0, ts);
+    return rz;
+}
+
+// Phases 1 .. of z = B r after phase 0 (L >= 1, r the current residual,
+// complete): down-sweep phases l = 1 .. L-1 (restriction or, at l = L-1,
+// G; smoothing t_l of levels l >= 2 into the stack; t_0 = W_0 r in phase 1
+// and t_1 = W_1 b_1 in phase L-1, where the restrictions leave the grid
+// idle), the collapsed up-sweep y_1 = t_1 + U1 [t_2 .. t_{L-1}, y_L]
+// (L >= 2), then z = t_0 + S_0 y_1; returns this thread's share of r.z.
+__device__ double vcycle_rest(const AmgDev &M, const float *r, float *z, cg::grid_group &grid, int t0, int ts) {
+    const int L = M.nlev - 1;
+    for (int l = 1; l < L; ++l) {
+        const float *b = M.lev[l].b;
+        const auto gb = [=](int j) { return b[j]; };
         if (l < L - 1) {
             float *bn = M.lev[l + 1].b;
-            apply(M.lev[l].ST, [=](int j) { return b[j]; }, [=](int i, float s) { bn[i] = s; }, t0, ts);
+            apply(M.lev[l].ST, gb, NoPre{}, [=](int i, float s, int) { bn[i] = s; }, t0, ts);
         } else {
             float *yL = M.yL;
-            apply(M.G, [=](int j) { return b[j]; }, [=](int i, float s) { yL[i] = s; }, t0, ts);
+            apply(M.G, gb, NoPre{}, [=](int i, float s, int) { yL[i] = s; }, t0, ts);
+        }
+        if (l >= 2) smooth(M.lev[l], gb, M.lev[l].t, t0, ts);
+        if (l == 1) smooth(M.lev[0], [=](int j) { return r[j]; }, M.lev[0].t, t0, ts);
+        if (l == L - 1) {
+            const float *b1 = M.lev[1].b;
+            smooth(M.lev[1], [=](int j) { return b1[j]; }, M.lev[1].t, t0, ts);
         }
         grid.sync();
     }
@@ -201,26 +335,33 @@ __device__ double vcycle(const AmgDev &M, const float *r, float *z, cg::grid_gro
     if (L >= 2) {
         const float *t1 = M.lev[1].t, *st = M.stack;
         float *y1 = M.y1;
-        apply(M.U1, [=](int j) { return st[j]; }, [=](int i, float s) { y1[i] = t1[i] + s; }, t0, ts);
+        apply(M.U1, [=](int j) { return st[j]; }, [=](int i) { return t1[i]; },
+              [=](int i, float s, float ti) { y1[i] = ti + s; }, t0, ts);
         grid.sync();
         yup = M.y1;
     }
     const float *tz = M.lev[0].t;
-    apply(M.S0, [=](int j) { return yup[j]; },
-          [&](int i, float s) {
-              const float zi = tz[i] + s;
+    double rz = 0.0;
+    apply(M.S0, [=](int j) { return yup[j]; }, [=](int i) { return make_float2(tz[i], r[i]); },
+          [&](int i, float s, float2 tr) {
+              const float zi = tr.x + s;
               z[i] = zi;
-              rz = fma((double)zi, (double)r[i], rz);
+              rz = fma((double)zi, (double)tr.y, rz);
           }, t0, ts);
     return rz;
 }
 
+// Block partials of the grid reductions: p.Ap in A, ||r||^2 of the merged
+// update in B, r.z in C, the pass start's (||r||^2, ||b||^2) in (B, D).  A
+// buffer is written again only after at least one grid barrier has passed
+// since every block read it.
 __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M) {
     cg::grid_group grid = cg::this_grid();
     __shared__ double sh[2 * kPcgThreads + 16];
     __shared__ double scal[4];
     const int nb = gridDim.x;
     const int n = a.n;
+    const int L = M.nlev - 1;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gstride = nb * blockDim.x;
     double *partA = a.partials;
@@ -243,14 +384,6 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M)
         for (int i = gtid; i < n; i += gstride) a.b[i] = a.b[i] - mean;
         grid.sync();
     }
-    // r.z of the V-cycle just applied -> beta (thread 0 keeps rz)
-    auto finish_rz = [&](double rz_part) {
-        block_sum2(rz_part, 0.0, sh, ra, rb);
-        if (threadIdx.x == 0) partA[blockIdx.x] = ra;
-        grid.sync();
-        grid_sum2(partA, nullptr, nb, sh, ra, rb);
-        __syncthreads();
-    };
     // solver scalars, kept by thread 0 in shared memory (no registers held
     // across the loop by the other threads)
     __shared__ double t_rz, t_tol2, t_rr, t_bb, t_rmax;
@@ -259,6 +392,8 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M)
         t_rz = t_tol2 = t_rr = t_bb = t_rmax = 0.0;
         t_it = 0; t_status = 1; t_updates = 0;
     }
+    // the two residual buffers: r is the current one
+    float *r = a.r32, *rn = M.r_alt;
     for (int pass = 0;; ++pass) {
         // true residual in FP64 into the FP32 recurrence
         double rr = 0.0, bb = 0.0;
@@ -270,14 +405,14 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M)
             for (int k = 0; k < w; ++k) s = fma(__ldg(a.val + base + 32 * k), __ldcg(a.x + __ldg(a.col + base + 32 * k)), s);
             const double bi = a.b[i];
             const double ri = bi - s;
-            a.r32[i] = (float)ri;
+            r[i] = (float)ri;
             rr = fma(ri, ri, rr);
             if (pass == 0) bb = fma(bi, bi, bb);
         }
         block_sum2(rr, bb, sh, ra, rb);
-        if (threadIdx.x == 0) { partB[blockIdx.x] = ra; partC[blockIdx.x] = rb; }
+        if (threadIdx.x == 0) { partB[blockIdx.x] = ra; partD[blockIdx.x] = rb; }
         grid.sync();
-        grid_sum2(partB, partC, nb, sh, ra, rb);
+        grid_sum2(partB, partD, nb, sh, ra, rb);
         if (threadIdx.x == 0) {
             t_rr = ra;
             if (pass == 0) {
@@ -296,12 +431,27 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M)
         if (scal[1] == 0.0) break;
         // z = B r and r.z; beta = 0 on the first pass (p = z), else continue
         // the direction across the replacement
-        finish_rz(vcycle(M, a.r32, a.z32, grid, gtid, gstride));
-        if (threadIdx.x == 0) {
-            scal[0] = pass > 0 ? ra / t_rz : 0.0;
-            t_rz = ra;
+        {
+            float unused = 0.0f;
+            const double rz0 = vcycle_phase0<false>(M, a, r, rn, 0.0, a.z32, unused, gtid, gstride);
+            if (L == 0) {
+                block_sum2(rz0, 0.0, sh, ra, rb);
+                if (threadIdx.x == 0) partC[blockIdx.x] = ra;
+            }
+            grid.sync();
+            if (L >= 1) {
+                const double rzp = vcycle_rest(M, r, a.z32, grid, gtid, gstride);
+                block_sum2(rzp, 0.0, sh, ra, rb);
+                if (threadIdx.x == 0) partC[blockIdx.x] = ra;
+                grid.sync();
+            }
+            grid_sum2(partC, nullptr, nb, sh, ra, rb);
+            if (threadIdx.x == 0) {
+                scal[0] = pass > 0 ? ra / t_rz : 0.0;
+                t_rz = ra;
+            }
+            __syncthreads();
         }
-        __syncthreads();
         bool first = pass == 0;
         for (;;) {
             // A: p = z + beta p, Ap = A z + beta Ap, p.Ap
@@ -310,11 +460,10 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M)
             {
                 const float *z = a.z32;
                 float *p = a.p32, *Ap = a.Ap32;
-                apply(A0, [=](int j) { return z[j]; },
-                      [&](int i, float s) {
-                          const float zi = z[i];
-                          const float pi = first ? zi : fmaf(beta, p[i], zi);
-                          const float api = first ? s : fmaf(beta, Ap[i], s);
+                apply(A0, [=](int j) { return z[j]; }, [=](int i) { return make_float3(z[i], p[i], Ap[i]); },
+                      [&](int i, float s, float3 zpa) {
+                          const float pi = first ? zpa.x : fmaf(beta, zpa.y, zpa.x);
+                          const float api = first ? s : fmaf(beta, zpa.z, s);
                           p[i] = pi;
                           Ap[i] = api;
                           pap32 = fmaf(pi, api, pap32);
@@ -332,41 +481,34 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M)
             }
             __syncthreads();
             if (scal[1] == 0.0) break;
-            // B: x, r update and ||r||^2 (rows of this thread as written in A)
-            const double alpha = scal[0];
-            const float alpha32 = (float)alpha;
+            // B + phase 0 of the next cycle: x += alpha p, r_new = r - alpha Ap
+            // into rn with ||r_new||^2, and phase 0 on r_new
             float rr32 = 0.0f;
-            for (int i = gtid; i < n; i += 2 * gstride) {
-                // two rows per pass, loads first
-                const int i2 = i + gstride;
-                const bool two = i2 < n;
-                const double x1 = a.x[i];
-                const float p1 = a.p32[i], q1 = a.Ap32[i], r1 = a.r32[i];
-                const double x2 = two ? a.x[i2] : 0.0;
-                const float p2 = two ? a.p32[i2] : 0.0f, q2 = two ? a.Ap32[i2] : 0.0f;
-                const float r2 = two ? a.r32[i2] : 0.0f;
-                const float n1 = fmaf(-alpha32, q1, r1), n2 = fmaf(-alpha32, q2, r2);
-                a.x[i] = fma(alpha, (double)p1, x1);
-                a.r32[i] = n1;
-                rr32 = fmaf(n1, n1, rr32);
-                if (two) {
-                    a.x[i2] = fma(alpha, (double)p2, x2);
-                    a.r32[i2] = n2;
-                    rr32 = fmaf(n2, n2, rr32);
-                }
-            }
-            block_sum2((double)rr32, 0.0, sh, ra, rb);
-            if (threadIdx.x == 0) partC[blockIdx.x] = ra;
+            const double rz0 = vcycle_phase0<true>(M, a, r, rn, scal[0], a.z32, rr32, gtid, gstride);
+            block_sum2((double)rr32, rz0, sh, ra, rb);
+            if (threadIdx.x == 0) { partB[blockIdx.x] = ra; if (L == 0) partC[blockIdx.x] = rb; }
             grid.sync();
-            grid_sum2(partC, nullptr, nb, sh, ra, rb);
+            {
+                float *t = r; r = rn; rn = t;
+            }
+            grid_sum2(partB, L == 0 ? partC : nullptr, nb, sh, ra, rb);
             if (threadIdx.x == 0) {
                 const double rr_rec = ra;
                 scal[2] = (rr_rec <= 1e-6 * t_rmax || rr_rec <= t_tol2 || t_it >= a.max_iter) ? 1.0 : 0.0;
+                scal[3] = rb;
             }
             __syncthreads();
             if (scal[2] != 0.0) break;   // replace the residual (next pass)
-            finish_rz(vcycle(M, a.r32, a.z32, grid, gtid, gstride));
-            if (threadIdx.x == 0) { scal[0] = ra / t_rz; t_rz = ra; }
+            double rz = scal[3];
+            if (L >= 1) {
+                const double rzp = vcycle_rest(M, r, a.z32, grid, gtid, gstride);
+                block_sum2(rzp, 0.0, sh, ra, rb);
+                if (threadIdx.x == 0) partC[blockIdx.x] = ra;
+                grid.sync();
+                grid_sum2(partC, nullptr, nb, sh, ra, rb);
+                rz = ra;
+            }
+            if (threadIdx.x == 0) { scal[0] = rz / t_rz; t_rz = rz; }
             __syncthreads();
         }
         if (scal[1] == 0.0) break;

@@ -209,8 +209,14 @@ struct SpOp {
     int32_t g = 1;                       // lanes per row
     const int64_t *ptr = nullptr;        // SELL slice offsets [n_slices+1] or CSR row offsets [n+1]
     const int32_t *swidth = nullptr;     // SELL slice widths (g == 1 only)
-    const int32_t *col = nullptr;
-    const float *val = nullptr;
+    const int32_t *col = nullptr;        // column indices (when col16 is null)
+    const float *val = nullptr;          // FP32 values (when val16 is null)
+    // compressed forms: column = cbase[slice or row] + col16[k]; value =
+    // vscale * half(val16[k]) (IEEE binary16 bits)
+    const uint16_t *col16 = nullptr;
+    const int32_t *cbase = nullptr;
+    const uint16_t *val16 = nullptr;
+    float vscale = 1.0f;
 };
 
 constexpr int kAmgMaxLevels = 12;
@@ -235,6 +241,7 @@ struct AmgDev {
     float *stack = nullptr;              // [t_2 .. t_{L-1}, y_L] (L >= 2) or y_1 (L == 1)
     float *yL = nullptr;                 // y_L inside the stack
     float *y1 = nullptr;                 // level-1 result (L >= 2)
+    float *r_alt = nullptr;              // second FP32 residual buffer of the solver [n]
 };
 
 // ---- launch wrappers (all on `stream`) -----------------------------------
