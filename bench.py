@@ -58,7 +58,9 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    """nvidia-smi sampling (every 100 ms) of SM clocks and throttle reasons,
+    from the start of the warm-up to the end of the timed steps: the timed
+    steps alone last well under one sampling interval."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -66,13 +68,15 @@ class ClockSampler:
 
     def __init__(self, device_index: int = 0):
         self.rows = []
+        self.times = []
+        self.window = None       # (start, end) of the timed steps, perf_counter seconds
         self.proc = None
         self.dev = device_index
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -83,6 +87,7 @@ class ClockSampler:
     def _read(self):
         for line in self.proc.stdout:
             self.rows.append([x.strip() for x in line.split(",")])
+            self.times.append(time.perf_counter())
 
     def __exit__(self, *a):
         if self.proc:
@@ -99,8 +104,11 @@ class ClockSampler:
         mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for r in self.rows for k in range(4) if len(r) > 5 + k and r[5 + k] == "Active"})
+        n_timed = (sum(1 for t in self.times if self.window[0] - 0.1 <= t <= self.window[1] + 0.1)
+                   if self.window else None)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(self.rows), "samples_near_timed_steps": n_timed,
+                "window": "every 100 ms from the start of the warm-up to the end of the timed steps"}
 
 
 # ---------------------------------------------------------------------------
@@ -157,8 +165,11 @@ def run_ours(args):
         n_now = r.n_particles
         return r, pushed
 
+    clk = ClockSampler().__enter__()
     for k in range(max(3, args.warmup)):
         one(first=(k == 0))
+        if k == 0:
+            rho_first = punc.Function(pop, "rho").vector()
     cg1 = args.efield == "cg1"
     graph = args.step_mode == "graph"
     tuning = None
@@ -178,26 +189,28 @@ def run_ours(args):
     launches0 = launch_count()
     pushed_total = 0
     iters = 0
-    with ClockSampler() as clk:
-        L.check(lib.pg_event_record(pop.handle, 0))
-        t_wall = time.perf_counter()
-        if args.step_mode == "staged":
-            punc.set_profiling(pop, True)
-            punc.stage_times(pop)  # reset
-            for _ in range(args.steps):
-                r, pushed = one()
-                pushed_total += pushed
-                iters += r.pcg_iterations
-        else:
-            rs = punc.run_steps(pop, objs, DT, args.steps, inject=True, seed=0x5EED0002, step_no=step_no,
-                                efield_cg1=cg1, use_graph=graph)
-            step_no += args.steps
-            pushed_total = n_now + sum(r.n_particles for r in rs[:-1])
-            n_now = rs[-1].n_particles
-            iters = sum(r.pcg_iterations for r in rs)
-        L.check(lib.pg_event_record(pop.handle, 1))
-        ms = ctypes_ms(lib, pop, 0, 1)
-        t_wall = time.perf_counter() - t_wall
+    L.check(lib.pg_event_record(pop.handle, 0))
+    t_wall = time.perf_counter()
+    t_start = t_wall
+    if args.step_mode == "staged":
+        punc.set_profiling(pop, True)
+        punc.stage_times(pop)  # reset
+        for _ in range(args.steps):
+            r, pushed = one()
+            pushed_total += pushed
+            iters += r.pcg_iterations
+    else:
+        rs = punc.run_steps(pop, objs, DT, args.steps, inject=True, seed=0x5EED0002, step_no=step_no,
+                            efield_cg1=cg1, use_graph=graph)
+        step_no += args.steps
+        pushed_total = n_now + sum(r.n_particles for r in rs[:-1])
+        n_now = rs[-1].n_particles
+        iters = sum(r.pcg_iterations for r in rs)
+    L.check(lib.pg_event_record(pop.handle, 1))
+    ms = ctypes_ms(lib, pop, 0, 1)
+    t_wall = time.perf_counter() - t_wall
+    clk.window = (t_start, t_start + t_wall)
+    clk.__exit__(None, None, None)
     launches = launch_count() - launches0
     if args.step_mode == "staged":
         prof_steps = args.steps
@@ -313,28 +326,27 @@ def run_ours(args):
         "wall_s_timed": round(t_wall, 3),
     }
     pop.close()
-    return out
+    return out, rho_first
 
 
 def amg_iteration_bytes(lay):
-    """Algorithmic bytes of one AMG-preconditioned PCG iteration, each operator
-    read once per use (FP32 value + int32 column = 8 B an entry), vectors in
-    FP32 except the FP64 solution:
-      level 0: A twice (PCG product, smoother), S and S^T once, 88 B per row
-               (p, Ap, z, r, t, x, D^-1 streams of the five phases);
-      levels 1..L-1: A and S^T once, 16 B per row;
-      G (last restriction + coarse solve) and the collapsed up-sweep U1 once,
-      8 B per level-1 row."""
+    """Algorithmic bytes of one AMG-preconditioned PCG iteration: the operator
+    bytes the engine reports (stored entries, padding excluded, times their
+    stored size: f32 or binary16 value + 32- or 16-bit column; A_0 twice, for
+    the PCG product and the level-0 smoother; every other cycle operator once)
+    plus the vectors, f32 except the f64 solution: 88 B per level-0 row (p, Ap,
+    z, r, t, x, D^-1 streams of the iteration's phases), 16 B per row of levels
+    1..L-1, 8 B per level-1 row (the up-sweep result)."""
     lv = lay["levels"]
     if not lv:
         return 0, "no AMG levels"
     L = len(lv) - 1
-    b = 2 * lv[0]["nnz"] * 8 + 2 * lv[0]["nnz_p"] * 8 + 88 * lv[0]["rows"]
+    b = lay["cycle_bytes"] + 88 * lv[0]["rows"]
     for l in range(1, L):
-        b += lv[l]["nnz"] * 8 + lv[l]["nnz_p"] * 8 + 16 * lv[l]["rows"]
-    b += (lay["cycle_nnz_g"] + lay["cycle_nnz_u1"]) * 8 + (8 * lv[1]["rows"] if L >= 2 else 0)
-    return b, ("per iteration: level 0 2*nnz(A)*8 + 2*nnz(S)*8 + 88*rows; levels 1..L-1 (nnz(A)+nnz(S^T))*8 + "
-               "16*rows; (nnz(G)+nnz(U1))*8 + 8*rows(1); operators re-read from L2 count each time")
+        b += 16 * lv[l]["rows"]
+    b += 8 * lv[1]["rows"] if L >= 2 else 0
+    return b, ("per iteration: operator bytes as stored (cycle_bytes: entries x stored size, A_0 twice) + "
+               "88*rows(0) + 16*rows(1..L-1) + 8*rows(1); operators re-read from L2 count each time")
 
 
 def ctypes_ms(lib, pop, a, b):
@@ -446,7 +458,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="probe-80", help="probe-N: N^3 sub-cubes, particles scaled by (N/80)^3")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
+                    help="mixed (the headline form: FP32 particles, fixed-point deposit, mixed PCG) or fp64")
+    ap.add_argument("--no-fp64-form", dest="fp64_form", action="store_false",
+                    help="skip the FP64-form run that the mixed form is compared with")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="skip the engine's autotuner (launch configuration, sort interval) in the warm-up")
     ap.add_argument("--step-mode", default="graph", choices=["graph", "stream", "staged"],
@@ -477,7 +492,24 @@ def main():
         if rank == 0:
             print(json.dumps(run_reference(args)))
         return
-    res = run_ours(args)
+    res, rho_first = run_ours(args)
+    if args.precision == "mixed" and args.fp64_form:
+        # the same workload in the FP64 form: its throughput, and the charge
+        # density error of the mixed form after one step from identical particles
+        import copy
+
+        import numpy as np
+        a64 = copy.copy(args)
+        a64.precision = "fp64"
+        r64, rho64 = run_ours(a64)
+        d = np.asarray(rho_first) - np.asarray(rho64)
+        res["fp64_form"] = {"value": r64["value"], "unit": UNIT, "ms_per_step": r64["ms_per_step"],
+                            "pcg_iterations_per_step": r64["config"]["pcg_iterations_per_step"],
+                            "e2e": r64["e2e"]["value"], "roofline_particles_frac": r64["roofline_particles"]["frac"]}
+        res["mixed_vs_fp64"] = round(res["value"] / r64["value"], 3)
+        res["rho_rel_err"] = {"l2": float(np.linalg.norm(d) / np.linalg.norm(rho64)),
+                              "max": float(np.abs(d).max() / np.abs(rho64).max()),
+                              "bar": 1e-5, "after": "one step from identical particles and injection streams"}
     if world > 1:
         import torch
         import torch.distributed as dist

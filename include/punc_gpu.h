@@ -18,7 +18,8 @@
 extern "C" {
 #endif
 
-#define PG_ABI_VERSION 1
+/* 2: pg_poisson_layout gained cycle_bytes */
+#define PG_ABI_VERSION 2
 
 typedef enum pg_status {
     PG_OK = 0,
@@ -373,6 +374,9 @@ typedef struct pg_poisson_layout {
                                                 to the next level (0 on the coarsest level) */
     int64_t cycle_nnz_g;                     /* entries of G = C^-1 S^T (last restriction + coarse solve) */
     int64_t cycle_nnz_u1;                    /* entries of the collapsed up-sweep operator of levels >= 1 */
+    int64_t cycle_bytes;                     /* operator bytes one AMG-PCG iteration reads: stored entries
+                                                (padding excluded) times their stored size, each operator
+                                                counted once per use */
 } pg_poisson_layout;
 int pg_poisson_layout_get(pg_sim *sim, pg_poisson_layout *out);
 

@@ -13,6 +13,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libpunc_gpu.so")
+ABI_VERSION = 2   # include/punc_gpu.h PG_ABI_VERSION, which these structures follow
 
 PG_OK = 0
 STATUS_NAMES = {
@@ -95,7 +96,7 @@ class PoissonLayout(C.Structure):
                 ("precond", C.c_int32), ("levels", C.c_int32),
                 ("level_rows", C.c_int64 * MAX_AMG_LEVELS), ("level_nnz", C.c_int64 * MAX_AMG_LEVELS),
                 ("level_nnz_p", C.c_int64 * MAX_AMG_LEVELS), ("cycle_nnz_g", C.c_int64),
-                ("cycle_nnz_u1", C.c_int64)]
+                ("cycle_nnz_u1", C.c_int64), ("cycle_bytes", C.c_int64)]
 
 
 # Every entry point of include/punc_gpu.h with its argument types.
@@ -187,6 +188,9 @@ def load(path: str = LIB_PATH):
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = res
+    if lib.pg_abi_version() != ABI_VERSION:
+        raise ImportError(f"{path}: ABI version {lib.pg_abi_version()}, these bindings follow {ABI_VERSION} "
+                          "(rebuild the library)")
     _lib = lib
     return lib
 

@@ -64,6 +64,7 @@ struct pg_sim {
     std::vector<int64_t> amg_rows, amg_nnz, amg_nnz_p;   // per level (pg_poisson_layout_get)
     int64_t a_nnz = 0, a_sell = 0;                       // stored nonzeros and SELL-32 entries of A
     int64_t amg_nnz_g = 0, amg_nnz_u1 = 0;               // cycle operators G and U1
+    int64_t amg_cycle_bytes = 0;                        // operator bytes read per AMG-PCG iteration
 
     // ESolver (CG1 field): dof -> cell adjacency, cell volumes, mass-matrix
     // D^-1 (and FP32 values), CG work arrays, the packed vertex field
@@ -574,6 +575,25 @@ static int setup_amg(pg_sim *s, const std::vector<int32_t> &arow, const std::vec
                        (rc = dalloc(s, &M.y1, h.levels[1].A.n))))
             return rc;
     }
+    // operator bytes of one iteration: A_0 twice (A p and the level-0
+    // smoother), then each operator of the cycle once
+    auto opb = [](const SpOp &o, int64_t entries) {
+        return entries * ((o.col16 ? 2 : 4) + (o.val16 ? 2 : 4));
+    };
+    int64_t cb = 2 * opb(M.lev[0].A, (int64_t)h.levels[0].A.ci.size());
+    if (L == 0) {
+        cb += opb(M.cinv, h.levels[0].A.n * h.levels[0].A.n);
+    } else {
+        cb += opb(M.S0, (int64_t)h.levels[0].S.ci.size());
+        if (L >= 2) cb += opb(M.lev[0].ST, (int64_t)h.levels[0].ST.ci.size());
+        for (int l = 1; l < L; ++l) {
+            cb += opb(M.lev[l].A, (int64_t)h.levels[l].A.ci.size());
+            if (l < L - 1) cb += opb(M.lev[l].ST, (int64_t)h.levels[l].ST.ci.size());
+        }
+        cb += opb(M.G, (int64_t)cyc.G.ci.size());
+        if (L >= 2) cb += opb(M.U1, (int64_t)cyc.U1.ci.size());
+    }
+    s->amg_cycle_bytes = cb;
     s->use_amg = true;
     return PG_OK;
 }
@@ -2679,6 +2699,7 @@ int pg_poisson_layout_get(pg_sim *s, pg_poisson_layout *out) {
     }
     out->cycle_nnz_g = s->use_amg ? s->amg_nnz_g : 0;
     out->cycle_nnz_u1 = s->use_amg ? s->amg_nnz_u1 : 0;
+    out->cycle_bytes = s->use_amg ? s->amg_cycle_bytes : 0;
     return PG_OK;
 }
 

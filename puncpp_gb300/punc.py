@@ -571,7 +571,7 @@ def poisson_layout(pop: Population) -> dict:
     return {"n_rows": out.n_rows, "nnz": out.nnz, "sell_entries": out.sell_entries, "precond": out.precond,
             "levels": [{"rows": out.level_rows[l], "nnz": out.level_nnz[l], "nnz_p": out.level_nnz_p[l]}
                        for l in range(n)],
-            "cycle_nnz_g": out.cycle_nnz_g, "cycle_nnz_u1": out.cycle_nnz_u1}
+            "cycle_nnz_g": out.cycle_nnz_g, "cycle_nnz_u1": out.cycle_nnz_u1, "cycle_bytes": out.cycle_bytes}
 
 
 def set_profiling(pop: Population, on: bool):

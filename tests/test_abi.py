@@ -30,7 +30,8 @@ def test_bindings_cover_the_header():
 
 
 def test_abi_version(lib):
-    assert lib.pg_abi_version() == 1
+    from puncpp_gb300 import _lib
+    assert lib.pg_abi_version() == _lib.ABI_VERSION == 2
 
 
 def test_philox_known_answers(lib, oracle_mod):
