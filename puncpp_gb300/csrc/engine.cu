@@ -44,6 +44,9 @@ struct pg_sim {
     int64_t *A_sptr = nullptr;                 // SELL-32 slices of the reduced matrix
     int32_t *A_swidth = nullptr, *A_col = nullptr, *M_row = nullptr, *M_col = nullptr;
     double *A_val = nullptr, *A_dinv = nullptr, *M_val = nullptr;
+    int64_t *Ms_ptr = nullptr;                           // M in SELL-32 for b = M rho
+    int32_t *Ms_width = nullptr, *Ms_col = nullptr;
+    double *Ms_val = nullptr;
     double *phi0 = nullptr;                    // zero-potential solution (superposition mode)
     bool phi0_valid = false;
     double *x_prev = nullptr;                  // previous PCG solution (pcg_warm_start == 2)
@@ -65,6 +68,10 @@ struct pg_sim {
     int64_t a_nnz = 0, a_sell = 0;                       // stored nonzeros and SELL-32 entries of A
     int64_t amg_nnz_g = 0, amg_nnz_u1 = 0;               // cycle operators G and U1
     int64_t amg_cycle_bytes = 0;                        // operator bytes read per AMG-PCG iteration
+    // the mixed form's step forms only the FP32 DG0 field; the FP64 one is
+    // formed from phi and these E0 when it is asked for
+    bool E64_stale = false;
+    double E0_last[3] = {0, 0, 0};
 
     // ESolver (CG1 field): dof -> cell adjacency, cell volumes, mass-matrix
     // D^-1 (and FP32 values), CG work arrays, the packed vertex field
@@ -610,7 +617,7 @@ static int poisson_solve_internal(pg_sim *s, const double *pot_h, bool zero_rho,
                                   double atol, pg_solve_info *acc, double *x_target = nullptr, bool *warm = nullptr) {
     if (s->n_obj > 0) PG_CUDA(cudaMemcpyAsync(s->obj_pot, pot_h, sizeof(double) * s->n_obj, cudaMemcpyHostToDevice, s->stream));
     if (zero_rho) PG_CUDA(cudaMemsetAsync(s->rho_acc, 0, sizeof(double) * s->ndof, s->stream));
-    launch_rhs(s->dm, s->M_row, s->M_col, s->M_val, zero_rho ? s->rho_acc : s->rho, s->bc_kind, s->bc_value, s->w_ext,
+    launch_rhs(s->dm, s->Ms_ptr, s->Ms_width, s->Ms_col, s->Ms_val, zero_rho ? s->rho_acc : s->rho, s->bc_kind, s->bc_value, s->w_ext,
                s->w_obj, s->obj_pot, s->n_obj, use_ext ? 1 : 0, s->b, s->stream);
     if (zero_rho) s->rho_valid = false;
     double *x = x_target ? x_target : s->phi;
@@ -1056,6 +1063,34 @@ int pg_create(const pg_mesh *mesh, const pg_config *cfg_in, pg_sim **out) {
         }
         for (int64_t i = 0; i <= nd; ++i) mrow[i] = (int32_t)h.rowptr[i];
         for (size_t k = 0; k < h.col.size(); ++k) mcol[k] = (int32_t)h.col[k];
+        {
+            // M in SELL-32 (rows' entries in CSR order; padding: value 0, own column)
+            const int64_t msl = (nd + 31) / 32;
+            std::vector<int64_t> mp(msl + 1, 0);
+            std::vector<int32_t> mw(msl, 0);
+            for (int64_t sl = 0; sl < msl; ++sl) {
+                int32_t w = 0;
+                for (int64_t r = 32 * sl; r < std::min<int64_t>(nd, 32 * sl + 32); ++r)
+                    w = std::max<int32_t>(w, (int32_t)(h.rowptr[r + 1] - h.rowptr[r]));
+                mw[sl] = w;
+                mp[sl + 1] = mp[sl] + 32 * (int64_t)w;
+            }
+            std::vector<int32_t> mc(std::max<int64_t>(1, mp[msl]), 0);
+            std::vector<double> mv(std::max<int64_t>(1, mp[msl]), 0.0);
+            for (int64_t sl = 0; sl < msl; ++sl)
+                for (int lane = 0; lane < 32; ++lane) {
+                    const int64_t r = 32 * sl + lane;
+                    const int64_t len = r < nd ? h.rowptr[r + 1] - h.rowptr[r] : 0;
+                    for (int32_t k = 0; k < mw[sl]; ++k) {
+                        const int64_t o = mp[sl] + 32 * (int64_t)k + lane;
+                        if (k < len) { mc[o] = (int32_t)h.col[h.rowptr[r] + k]; mv[o] = h.M[h.rowptr[r] + k]; }
+                        else mc[o] = (int32_t)std::min<int64_t>(r, nd - 1);
+                    }
+                }
+            if ((rc = upload(s, &s->Ms_ptr, mp)) || (rc = upload(s, &s->Ms_width, mw)) ||
+                (rc = upload(s, &s->Ms_col, mc)) || (rc = upload(s, &s->Ms_val, mv)))
+                return bail(rc);
+        }
         // SELL-32: slice s holds rows 32s..32s+31 column-major, padded with (row, 0.0)
         const int64_t nsl = (nd + 31) / 32;
         std::vector<int64_t> sptr(nsl + 1, 0);
@@ -1547,6 +1582,18 @@ int pg_statistics(pg_sim *s, double *stats) {
     return PG_OK;
 }
 
+// The DG0 field a step's push reads: FP32 only in the mixed form.
+static void step_efield(pg_sim *s, const double E0[3]) {
+    if (is_mixed(s)) {
+        launch_efield_f32(s->dm, s->phi, E0, s->stream);
+        s->E64_stale = true;
+        for (int j = 0; j < 3; ++j) s->E0_last[j] = E0[j];
+    } else {
+        launch_efield(s->dm, s->phi, E0, s->stream);
+        s->E64_stale = false;
+    }
+}
+
 int pg_efield_dg0(pg_sim *s, const double *phi) {
     if (!s) return fail(PG_ERR_ARG, "NULL handle");
     if (phi) {
@@ -1555,6 +1602,7 @@ int pg_efield_dg0(pg_sim *s, const double *phi) {
     }
     const double E0[3] = {0, 0, 0};
     launch_efield(s->dm, s->phi, E0, s->stream);
+    s->E64_stale = false;
     PG_CUDA(cudaStreamSynchronize(s->stream));
     return PG_OK;
 }
@@ -1571,6 +1619,10 @@ int pg_set_efield(pg_sim *s, const double *E) {
 int pg_get_efield(pg_sim *s, double *E) {
     if (!s || !E) return fail(PG_ERR_ARG, "pg_get_efield: NULL argument");
     std::vector<double> e4(4 * (size_t)s->nc);
+    if (s->E64_stale) {
+        launch_efield(s->dm, s->phi, s->E0_last, s->stream);
+        s->E64_stale = false;
+    }
     PG_CUDA(cudaStreamSynchronize(s->stream));
     PG_CUDA(cudaMemcpy(e4.data(), s->dm.E, sizeof(double) * e4.size(), cudaMemcpyDeviceToHost));
     for (int64_t c = 0; c < s->nc; ++c)
@@ -1898,7 +1950,7 @@ int pg_sort(pg_sim *s) {
 // rhs, boundary values and one PCG launch into x; object potentials are read
 // from s->obj_pot on the device; no status read-back.
 static int pcg_enqueue(pg_sim *s, double *x) {
-    launch_rhs(s->dm, s->M_row, s->M_col, s->M_val, s->rho, s->bc_kind, s->bc_value, s->w_ext, s->w_obj, s->obj_pot,
+    launch_rhs(s->dm, s->Ms_ptr, s->Ms_width, s->Ms_col, s->Ms_val, s->rho, s->bc_kind, s->bc_value, s->w_ext, s->w_obj, s->obj_pot,
                s->n_obj, 1, s->b, s->stream);
     launch_set_bc(s->bc_kind, s->bc_value, s->obj_pot, s->ndof, x, s->stream);
     PcgArgs a{};
@@ -2017,7 +2069,7 @@ static int enqueue_step(pg_sim *s, const pg_step_args *a, bool first) {
         const int err = launch_esolve(e, s->stream);
         if (err) return fail(PG_ERR_CUDA, std::string("ESolver launch: ") + cudaGetErrorString((cudaError_t)err));
     } else {
-        launch_efield(s->dm, s->phi, a->E0, s->stream);
+        step_efield(s, a->E0);
     }
     const double dt_push = first ? 0.5 * a->dt : a->dt;
     cudaMemsetAsync(s->state->absorbed, 0, sizeof(s->state->absorbed), s->stream);
@@ -2610,7 +2662,7 @@ int pg_step(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_obje
         if (rc) return rc;
     } else {
         StageScope t(s, "efield");
-        launch_efield(s->dm, s->phi, a->E0, s->stream);
+        step_efield(s, a->E0);
     }
     // accelerator + move + update, depositing the next step's charge
     {

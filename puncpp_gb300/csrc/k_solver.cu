@@ -36,21 +36,42 @@ __global__ void k_efield(DevMesh m, const double *__restrict__ phi, double e0x, 
     if (m.E_f) reinterpret_cast<float4 *>(m.E_f)[c] = make_float4((float)ex, (float)ey, (float)ez, 0.0f);
 }
 
+// The DG0 field of the mixed form's step, FP32 only: E_c = -sum_k phi_k
+// grad lambda_k(c) + E0 from the FP32 barycentric rows (the FP64 field is
+// formed on demand).
+__global__ void k_efield_f32(DevMesh m, const double *__restrict__ phi, float e0x, float e0y, float e0z) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.nc) return;
+    const int4 d = __ldg(m.dofs + c);
+    const double p3 = phi[d.w];
+    const float a = (float)(phi[d.x] - p3), b = (float)(phi[d.y] - p3), e = (float)(phi[d.z] - p3);
+    const float4 *A = reinterpret_cast<const float4 *>(m.bary_f) + 3 * (size_t)c;
+    const float4 r0 = __ldg(A), r1 = __ldg(A + 1), r2 = __ldg(A + 2);
+    const float gx = a * r0.y + b * r1.y + e * r2.y;
+    const float gy = a * r0.z + b * r1.z + e * r2.z;
+    const float gz = a * r0.w + b * r1.w + e * r2.w;
+    reinterpret_cast<float4 *>(m.E_f)[c] = make_float4(-gx + e0x, -gy + e0y, -gz + e0z, 0.0f);
+}
+
 // b = M rho on free rows, minus the Dirichlet columns moved to the right-hand
 // side; b = g on Dirichlet rows (PoissonSolver::solve, punc/src/poisson.cpp:343-362,
-// with the BC rows eliminated symmetrically).
-__global__ void k_rhs(int32_t n, const int32_t *__restrict__ mrow, const int32_t *__restrict__ mcol,
-                      const double *__restrict__ mval, const double *__restrict__ rho,
-                      const int32_t *__restrict__ bc_kind, const double *__restrict__ bc_value,
-                      const double *__restrict__ w_ext, const double *__restrict__ w_obj,
-                      const double *__restrict__ obj_pot, int32_t n_obj, int32_t use_ext, double *__restrict__ b) {
+// with the BC rows eliminated symmetrically).  M in SELL-32 (one thread per
+// row, the row's entries in their CSR order; padding: value 0, own column).
+__global__ void k_rhs(int32_t n, const int64_t *__restrict__ sptr, const int32_t *__restrict__ swidth,
+                      const int32_t *__restrict__ scol, const double *__restrict__ sval,
+                      const double *__restrict__ rho, const int32_t *__restrict__ bc_kind,
+                      const double *__restrict__ bc_value, const double *__restrict__ w_ext,
+                      const double *__restrict__ w_obj, const double *__restrict__ obj_pot, int32_t n_obj,
+                      int32_t use_ext, double *__restrict__ b) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int k = bc_kind[i];
     if (k == 0) { b[i] = use_ext ? bc_value[i] : 0.0; return; }
     if (k > 0) { b[i] = obj_pot[k - 1]; return; }
+    const int64_t base = __ldg(sptr + (i >> 5)) + (i & 31);
+    const int w = __ldg(swidth + (i >> 5));
     double s = 0.0;
-    for (int j = mrow[i]; j < mrow[i + 1]; ++j) s += mval[j] * rho[mcol[j]];
+    for (int e = 0; e < w; ++e) s += __ldg(sval + base + 32 * e) * __ldg(rho + __ldg(scol + base + 32 * e));
     if (use_ext) s = s - w_ext[i];
     for (int o = 0; o < n_obj; ++o) s = s - obj_pot[o] * w_obj[(size_t)o * n + i];
     b[i] = s;
@@ -454,12 +475,20 @@ void launch_efield(const DevMesh &m, const double *phi, const double E0[3], cuda
     k_efield<<<(m.nc + kThreads - 1) / kThreads, kThreads, 0, st>>>(m, phi, E0[0], E0[1], E0[2]);
 }
 
-void launch_rhs(const DevMesh &m, const int32_t *mrow, const int32_t *mcol, const double *mval, const double *rho,
-                const int32_t *bc_kind, const double *bc_value, const double *w_ext, const double *w_obj,
-                const double *obj_pot, int32_t n_obj, int32_t use_ext, double *b, cudaStream_t st) {
+void launch_efield_f32(const DevMesh &m, const double *phi, const double E0[3], cudaStream_t st) {
+    if (m.nc <= 0) return;
     count_launches(1);
-    k_rhs<<<(m.ndof + kThreads - 1) / kThreads, kThreads, 0, st>>>(m.ndof, mrow, mcol, mval, rho, bc_kind, bc_value,
-                                                                    w_ext, w_obj, obj_pot, n_obj, use_ext, b);
+    k_efield_f32<<<(m.nc + kThreads - 1) / kThreads, kThreads, 0, st>>>(m, phi, (float)E0[0], (float)E0[1],
+                                                                          (float)E0[2]);
+}
+
+void launch_rhs(const DevMesh &m, const int64_t *msptr, const int32_t *mswidth, const int32_t *mscol,
+                const double *msval, const double *rho, const int32_t *bc_kind, const double *bc_value,
+                const double *w_ext, const double *w_obj, const double *obj_pot, int32_t n_obj, int32_t use_ext,
+                double *b, cudaStream_t st) {
+    count_launches(1);
+    k_rhs<<<(m.ndof + kThreads - 1) / kThreads, kThreads, 0, st>>>(m.ndof, msptr, mswidth, mscol, msval, rho, bc_kind,
+                                                                    bc_value, w_ext, w_obj, obj_pot, n_obj, use_ext, b);
 }
 
 void launch_set_bc(const int32_t *bc_kind, const double *bc_value, const double *obj_pot, int32_t n, double *x,

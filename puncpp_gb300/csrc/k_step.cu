@@ -102,14 +102,19 @@ __global__ void k_superpose_dev(const double *__restrict__ phi0, const double *_
 }
 
 // One result row: KE, live particles, absorbed, injected (kept), PCG
-// iterations, ||r||, then per object current, charge, potential.
+// iterations, ||r||, then per object current, charge, potential.  One warp:
+// lanes sum the per-tag absorbed counts, lane 0 writes the row.
 __global__ void k_step_record(double *rows, int row_len, int64_t *counts, const double *ke, const DevState *st,
                               int n_species, const int32_t *pcg_i, const double *pcg_d, const double *obj, int n_obj) {
-    double *r = rows + (size_t)counts[3] * row_len;
-    int64_t live = 0, absorbed = 0, injected = 0;
-    for (int k = 0; k < n_species; ++k) live += st->live[k];
-    for (int t = 0; t < kMaxTags; ++t)
+    const int lane = threadIdx.x;
+    int64_t absorbed = 0;
+    for (int t = lane; t < kMaxTags; t += 32)
         for (int k = 0; k < n_species; ++k) absorbed += st->absorbed[t][k];
+    for (int o = 16; o > 0; o >>= 1) absorbed += __shfl_down_sync(0xffffffffu, absorbed, o);
+    if (lane != 0) return;
+    double *r = rows + (size_t)counts[3] * row_len;
+    int64_t live = 0, injected = 0;
+    for (int k = 0; k < n_species; ++k) live += st->live[k];
     for (int k = 0; k < kMaxSpecies; ++k) injected += st->injected[k];
     r[0] = *ke;
     r[1] = (double)live;
@@ -158,7 +163,7 @@ void launch_step_record(double *rows, int row_len, int64_t *counts, const double
                         int n_species, const int32_t *pcg_i, const double *pcg_d, const double *obj, int n_obj,
                         cudaStream_t s) {
     count_launches(1);
-    k_step_record<<<1, 1, 0, s>>>(rows, row_len, counts, ke, st, n_species, pcg_i, pcg_d, obj, n_obj);
+    k_step_record<<<1, 32, 0, s>>>(rows, row_len, counts, ke, st, n_species, pcg_i, pcg_d, obj, n_obj);
 }
 void launch_set_count(int64_t *counts, const int64_t *cursor, int32_t nc, cudaStream_t s) {
     count_launches(1);

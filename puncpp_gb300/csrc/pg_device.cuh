@@ -251,6 +251,8 @@ void count_launches(int n);
 long long launches_so_far();
 
 void launch_efield(const DevMesh &m, const double *phi, const double E0[3], cudaStream_t st);
+// FP32 field only (mixed form), from the FP32 barycentric rows
+void launch_efield_f32(const DevMesh &m, const double *phi, const double E0[3], cudaStream_t st);
 void launch_push(const DevMesh &m, const DevParticles &p, int64_t n_slots, const PushParams &pp,
                  double *partials, int nblocks, double *ke_out, cudaStream_t st);
 void launch_move(const DevParticles &p, int64_t n_slots, const MoveParams &mp, cudaStream_t st);
@@ -280,10 +282,10 @@ void launch_sort_hist(const DevParticles &p, int64_t n_slots, int64_t *hist, cud
 void launch_sort_scatter(const DevParticles &src, const DevParticles &dst, int64_t n_slots,
                          int64_t *cursor, cudaStream_t st);
 
-void launch_rhs(const DevMesh &m, const int32_t *mrow, const int32_t *mcol, const double *mval,
-                const double *rho, const int32_t *bc_kind, const double *bc_value,
-                const double *w_ext, const double *w_obj, const double *obj_pot, int32_t n_obj,
-                int32_t use_ext, double *b, cudaStream_t st);
+void launch_rhs(const DevMesh &m, const int64_t *msptr, const int32_t *mswidth, const int32_t *mscol,
+                const double *msval, const double *rho, const int32_t *bc_kind, const double *bc_value,
+                const double *w_ext, const double *w_obj, const double *obj_pot, int32_t n_obj, int32_t use_ext,
+                double *b, cudaStream_t st);
 void launch_set_bc(const int32_t *bc_kind, const double *bc_value, const double *obj_pot,
                    int32_t n, double *x, cudaStream_t st);
 int launch_pcg(const PcgArgs &a, cudaStream_t st);
