@@ -269,7 +269,10 @@ def run_ours(args):
     # algorithmic bytes: particle pass per particle / occupied cell / dof,
     # PCG per iteration per nonzero / dof
     if mixed:
-        pb, cb, pmodel = n_avg * 57 + occ * 160 + nv * 8, None, "Np*57 + occupied cells*160 + Ndof*8"
+        pb, cb, pmodel = (n_avg * 57 + occ * 80 + nv * 16, None,
+                          "Np*57 (FP32 x, v read+write, cell read+write, species) + occupied cells*80 (64-byte "
+                          "cell record: FP32 barycentric rows + neighbours; dof ids 16) + Ndof*16 (phi read for "
+                          "the in-pass DG0 field, int64 charge)")
     else:
         pb, cb, pmodel = n_avg * 104 + occ * 288 + nv * 8, None, "Np*104 + occupied cells*288 + Ndof*8"
     if lay["levels"]:
@@ -286,7 +289,7 @@ def run_ours(args):
                 "frac": round(ach / hbm, 4), "peak_source": peak_src, "traffic": None,
                 "algorithmic_bytes": model}
 
-    r_part = roof_of("k_mixed (fused FP32 push+move+walk, fixed-point deposit)" if mixed
+    r_part = roof_of("k_mixed (fused FP32 DG0 field+push+move+walk, fixed-point deposit)" if mixed
                      else "k_particles (fused FP64 push+move+walk+deposit)", args.steps * pb, part_ms, pmodel)
     pcg_kernel = ("k_pcg_amg (AMG-preconditioned mixed PCG, one cooperative launch per solve)" if lay["levels"]
                   else "k_pcg_rel (mixed Jacobi PCG, one cooperative launch per solve)" if mixed

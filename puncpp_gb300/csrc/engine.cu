@@ -862,6 +862,18 @@ static int ensure_scan_tmp(pg_sim *s, int64_t n) {
     return PG_OK;
 }
 
+// The FP32 screening boxes of the injected species (the same bits as
+// flux_box32 on the device: IEEE conversions and one division).
+static void fill_flux32(InjectParams &ip) {
+    for (int k = 0; k < ip.n_species; ++k) {
+        FluxBox B;
+        for (int c = 0; c < 3; ++c) { B.lo[c] = ip.sp[k].domain_lo[c]; B.w[c] = ip.sp[k].domain_w[c]; B.vd[c] = ip.sp[k].vd[c]; }
+        B.vth2 = ip.sp[k].vth2;
+        B.factor = ip.sp[k].factor;
+        ip.sp32[k] = flux_box32(B);
+    }
+}
+
 // Injection with optional deposit into rho_acc (fused step).
 static int inject_internal(pg_sim *s, double dt, uint64_t seed, uint64_t step, bool deposit, int64_t *n_inj) {
     if (!s->flux_ready) return fail(PG_ERR_STATE, "pg_inject: call pg_create_flux first");
@@ -895,6 +907,7 @@ static int inject_internal(pg_sim *s, double dt, uint64_t seed, uint64_t step, b
     if (rc) return rc;
     rc = ensure_scan_tmp(s, total + 1);
     if (rc) return rc;
+    fill_flux32(ip);
     // the species slots of the injection table are engine species ids
     InjectParams ipd = ip;
     for (int k = 0; k < ip.n_species; ++k) ipd.sp[k] = ip.sp[k];
@@ -981,15 +994,14 @@ int pg_create(const pg_mesh *mesh, const pg_config *cfg_in, pg_sim **out) {
         return bail(rc);
     cudaMemset(d_E, 0, sizeof(double) * 4 * h.nc);
     if (cfg.precision == PG_MIXED) {
-        float *pf, *bf, *ef;
-        if ((rc = dalloc(s, &pf, 16 * h.nc)) || (rc = dalloc(s, &bf, 12 * h.nc)) || (rc = dalloc(s, &ef, 4 * h.nc)) ||
-            (rc = dalloc(s, &s->rho_fixed, h.ndof)))
+        float4 *cf;
+        float *ef;
+        if ((rc = dalloc(s, &cf, 4 * h.nc)) || (rc = dalloc(s, &ef, 4 * h.nc)) || (rc = dalloc(s, &s->rho_fixed, h.ndof)))
             return bail(rc);
         cudaMemset(ef, 0, sizeof(float) * 4 * h.nc);
         cudaMemset(s->rho_fixed, 0, sizeof(unsigned long long) * h.ndof);
-        launch_float_tables(d_planes, d_bary, (int32_t)h.nc, pf, bf, s->stream);
-        s->dm.planes_f = pf;
-        s->dm.bary_f = bf;
+        launch_float_tables(d_bary, reinterpret_cast<const int4 *>(d_nbr), (int32_t)h.nc, cf, s->stream);
+        s->dm.cell_f = cf;
         s->dm.E_f = ef;
     } else if (cfg.precision != PG_FP64) {
         return bail(fail(PG_ERR_ARG, "pg_create: unknown precision"));
@@ -1582,7 +1594,17 @@ int pg_statistics(pg_sim *s, double *stats) {
     return PG_OK;
 }
 
-// The DG0 field a step's push reads: FP32 only in the mixed form.
+// The mixed form's step forms the DG0 field inside the particle pass, from
+// the potential at each particle's cell; the FP64 field (and the FP32 array
+// of pg_efield_dg0) are formed from phi and these E0 when asked for.
+static void pass_field(pg_sim *s, MixedParams &xp, const double E0[3]) {
+    xp.phi = s->phi;
+    for (int j = 0; j < 3; ++j) xp.E0[j] = (float)E0[j];
+    s->E64_stale = true;
+    for (int j = 0; j < 3; ++j) s->E0_last[j] = E0[j];
+}
+
+// The DG0 field a step's push reads (FP64 form).
 static void step_efield(pg_sim *s, const double E0[3]) {
     if (is_mixed(s)) {
         launch_efield_f32(s->dm, s->phi, E0, s->stream);
@@ -2004,6 +2026,7 @@ static void inject_enqueue(pg_sim *s, const DevParticles &Pd, double dt, uint64_
         I.factor = 1.0 / std::pow(std::sqrt(2. * M_PI * I.vth2), 3);
         I.q = S.q;
     }
+    fill_flux32(ip);
     ip.counts_dev = s->run_counts;
     ip.facet_c1 = s->d_inj_c1;
     ip.facet_seed = s->d_inj_seed;
@@ -2068,7 +2091,7 @@ static int enqueue_step(pg_sim *s, const pg_step_args *a, bool first) {
         e.evf = s->Evf;
         const int err = launch_esolve(e, s->stream);
         if (err) return fail(PG_ERR_CUDA, std::string("ESolver launch: ") + cudaGetErrorString((cudaError_t)err));
-    } else {
+    } else if (!is_mixed(s)) {
         step_efield(s, a->E0);
     }
     const double dt_push = first ? 0.5 * a->dt : a->dt;
@@ -2078,6 +2101,7 @@ static int enqueue_step(pg_sim *s, const pg_step_args *a, bool first) {
         MixedParams xp;
         fill_mixed(s, xp, dt_push, a->B, a->use_accel != 0, a->dt, a->periodic_move != 0, a->Ld);
         xp.cg1 = a->efield_cg1 ? 1 : 0;
+        if (!a->efield_cg1) pass_field(s, xp, a->E0);
         launch_mixed_pass(s->dm, Pd, cap, xp, true, true, true, true, s->cfg.max_walk_steps, s->rho_fixed, s->state,
                           s->partials, s->n_part, s->ke_dev, s->stream);
     } else {
@@ -2660,7 +2684,7 @@ int pg_step(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_obje
     if (a->efield_cg1) {
         rc = esolver_internal(s, a->E0, nullptr);
         if (rc) return rc;
-    } else {
+    } else if (!is_mixed(s)) {
         StageScope t(s, "efield");
         step_efield(s, a->E0);
     }
@@ -2681,6 +2705,7 @@ int pg_step(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_obje
             MixedParams xp;
             fill_mixed(s, xp, dt_push, a->B, a->use_accel != 0, a->dt, a->periodic_move != 0, a->Ld);
             xp.cg1 = a->efield_cg1 ? 1 : 0;
+            if (!a->efield_cg1) pass_field(s, xp, a->E0);
             if (s->n_slots > 0)
                 launch_mixed_pass(s->dm, s->P[s->cur], s->n_slots, xp, true, true, true, true, s->cfg.max_walk_steps,
                                   s->rho_fixed, s->state, s->partials, s->n_part, s->ke_dev, s->stream);

@@ -39,7 +39,7 @@ __device__ __forceinline__ void lambdas(const DevMesh &m, const DevParticles &p,
                                         double &l1, double &l2, double &l3) {
     if (MIXED) {
         const float x = p.xf[i], y = p.yf[i], z = p.zf[i];
-        const float4 *A = reinterpret_cast<const float4 *>(m.bary_f) + 3 * (size_t)c;
+        const float4 *A = m.cell_f + 4 * (size_t)c;
         const float4 a0 = __ldg(A), a1 = __ldg(A + 1), a2 = __ldg(A + 2);
         const float f0 = fmaf(a0.w, z, fmaf(a0.z, y, fmaf(a0.y, x, a0.x)));
         const float f1 = fmaf(a1.w, z, fmaf(a1.z, y, fmaf(a1.y, x, a1.x)));

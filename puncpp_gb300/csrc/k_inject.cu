@@ -60,7 +60,7 @@ __global__ void k_inject_count(InjectParams ip, const double *__restrict__ flux_
 }
 
 // One warp per injected particle (grid-stride over particles).
-__global__ void k_inject_generate(DevMesh m, DevParticles p, InjectParams ip, const double *__restrict__ pdf_max,
+__global__ void __launch_bounds__(kThreads, 8) k_inject_generate(DevMesh m, DevParticles p, InjectParams ip, const double *__restrict__ pdf_max,
                                   const double *__restrict__ facets, const int64_t *__restrict__ offsets,
                                   int max_steps, int deposit, const double *__restrict__ qsp,
                                   double *__restrict__ rho_acc, DevState *__restrict__ st) {
@@ -95,7 +95,7 @@ __global__ void k_inject_generate(DevMesh m, DevParticles p, InjectParams ip, co
         for (int c = 0; c < 3; ++c) { B.lo[c] = S.domain_lo[c]; B.w[c] = S.domain_w[c]; B.vd[c] = S.vd[c]; }
         B.vth2 = S.vth2;
         B.factor = S.factor;
-        const FluxBox32 B32 = flux_box32(B);
+        const FluxBox32 &B32 = ip.sp32[s];
         const float nx32 = (float)nx, ny32 = (float)ny, nz32 = (float)nz, pmax32 = (float)pmax;
         const uint32_t k0 = uint32_t(seed), k1 = uint32_t(seed >> 32);
         double vx = 0, vy = 0, vz = 0;

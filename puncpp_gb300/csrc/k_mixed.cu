@@ -38,14 +38,14 @@ __device__ __forceinline__ double block_sum_d(double v) {
 // separate atomics); the group's first lane issues the four atomics.
 __device__ __forceinline__ void deposit_fixed_agg(const DevMesh &m, int c, float x, float y, float z, float q_scaled,
                                                   unsigned long long *rho_fixed) {
-    const float4 *A = reinterpret_cast<const float4 *>(m.bary_f) + 3 * (size_t)c;
+    const float4 *A = m.cell_f + 4 * (size_t)c;
     const float4 a0 = __ldg(A), a1 = __ldg(A + 1), a2 = __ldg(A + 2);
     const float l0 = fmaf(a0.w, z, fmaf(a0.z, y, fmaf(a0.y, x, a0.x)));
     const float l1 = fmaf(a1.w, z, fmaf(a1.z, y, fmaf(a1.y, x, a1.x)));
     const float l2 = fmaf(a2.w, z, fmaf(a2.z, y, fmaf(a2.y, x, a2.x)));
     const float l3 = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, l0), l1), l2);
-    long long v0 = __float2ll_rn(__fmul_rn(l0, q_scaled)), v1 = __float2ll_rn(__fmul_rn(l1, q_scaled));
-    long long v2 = __float2ll_rn(__fmul_rn(l2, q_scaled)), v3 = __float2ll_rn(__fmul_rn(l3, q_scaled));
+    long long v0 = float_to_ll_rn(__fmul_rn(l0, q_scaled)), v1 = float_to_ll_rn(__fmul_rn(l1, q_scaled));
+    long long v2 = float_to_ll_rn(__fmul_rn(l2, q_scaled)), v3 = float_to_ll_rn(__fmul_rn(l3, q_scaled));
     const unsigned peers = __match_any_sync(__activemask(), c);
     const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
     for (unsigned rest = peers & ~(1u << leader); rest; rest &= rest - 1) {
@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(512) k_mixed(DevMesh m, DevParticles p, int64_
                 float4 E;
                 if (mp.cg1) {
                     // CG1 vertex field interpolated at the FP32 position
-                    const float4 *A = reinterpret_cast<const float4 *>(m.bary_f) + 3 * (size_t)c;
+                    const float4 *A = m.cell_f + 4 * (size_t)c;
                     const float4 r0 = __ldg(A), r1 = __ldg(A + 1), r2 = __ldg(A + 2);
                     const float l0 = fmaf(r0.w, z, fmaf(r0.z, y, fmaf(r0.y, x, r0.x)));
                     const float l1 = fmaf(r1.w, z, fmaf(r1.z, y, fmaf(r1.y, x, r1.x)));
@@ -94,6 +94,10 @@ __global__ void __launch_bounds__(512) k_mixed(DevMesh m, DevParticles p, int64_
                     E.y = fmaf(l3, v3.y, fmaf(l2, v2.y, fmaf(l1, v1.y, l0 * v0.y)));
                     E.z = fmaf(l3, v3.z, fmaf(l2, v2.z, fmaf(l1, v1.z, l0 * v0.z)));
                     E.w = 0.0f;
+                } else if (mp.phi) {
+                    const float4 *R = m.cell_f + 4 * (size_t)c;
+                    E = dg0_field_f32(__ldg(R), __ldg(R + 1), __ldg(R + 2), __ldg(m.dofs + c), mp.phi, mp.E0[0],
+                                      mp.E0[1], mp.E0[2]);
                 } else {
                     E = __ldg(reinterpret_cast<const float4 *>(m.E_f) + c);
                 }
@@ -190,12 +194,18 @@ __global__ void k_fixed_to_rho(const unsigned long long *__restrict__ fixed, con
     rho[i] = a * dv_inv[i];
 }
 
-__global__ void k_float_tables(const double *__restrict__ planes, const double *__restrict__ bary, int32_t nc,
-                               float *__restrict__ planes_f, float *__restrict__ bary_f) {
+// The mixed form's cell records: FP32 barycentric rows 0-2 and the
+// neighbour ids (int bits in the fourth float4).
+__global__ void k_float_tables(const double *__restrict__ bary, const int4 *__restrict__ nbr, int32_t nc,
+                               float4 *__restrict__ cell_f) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
-    for (int k = 0; k < 16; ++k) planes_f[16 * (size_t)c + k] = (float)planes[16 * (size_t)c + k];
-    for (int k = 0; k < 12; ++k) bary_f[12 * (size_t)c + k] = (float)bary[12 * (size_t)c + k];
+    const double *A = bary + 12 * (size_t)c;
+    for (int k = 0; k < 3; ++k)
+        cell_f[4 * (size_t)c + k] = make_float4((float)A[4 * k], (float)A[4 * k + 1], (float)A[4 * k + 2], (float)A[4 * k + 3]);
+    const int4 nb = nbr[c];
+    cell_f[4 * (size_t)c + 3] = make_float4(__int_as_float(nb.x), __int_as_float(nb.y), __int_as_float(nb.z),
+                                            __int_as_float(nb.w));
 }
 
 inline int grid_for(int64_t n, int max_blocks) {
@@ -253,11 +263,9 @@ void launch_fixed_to_rho(const unsigned long long *fixed, const double *dv_inv, 
     k_fixed_to_rho<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(fixed, dv_inv, unit, n, rho_acc, rho);
 }
 
-void launch_float_tables(const double *planes, const double *bary, int32_t nc, float *planes_f, float *bary_f,
-                         cudaStream_t st) {
-    if (nc <= 0) return;
+void launch_float_tables(const double *bary, const int4 *nbr, int32_t nc, float4 *cell_f, cudaStream_t st) {
     count_launches(1);
-    k_float_tables<<<(nc + kThreads - 1) / kThreads, kThreads, 0, st>>>(planes, bary, nc, planes_f, bary_f);
+    k_float_tables<<<(nc + kThreads - 1) / kThreads, kThreads, 0, st>>>(bary, nbr, nc, cell_f);
 }
 
 }  // namespace pg

@@ -37,20 +37,14 @@ __global__ void k_efield(DevMesh m, const double *__restrict__ phi, double e0x, 
 }
 
 // The DG0 field of the mixed form's step, FP32 only: E_c = -sum_k phi_k
-// grad lambda_k(c) + E0 from the FP32 barycentric rows (the FP64 field is
-// formed on demand).
+// grad lambda_k(c) + E0 from the FP32 barycentric rows of the cell records
+// (the FP64 field is formed on demand).
 __global__ void k_efield_f32(DevMesh m, const double *__restrict__ phi, float e0x, float e0y, float e0z) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.nc) return;
-    const int4 d = __ldg(m.dofs + c);
-    const double p3 = phi[d.w];
-    const float a = (float)(phi[d.x] - p3), b = (float)(phi[d.y] - p3), e = (float)(phi[d.z] - p3);
-    const float4 *A = reinterpret_cast<const float4 *>(m.bary_f) + 3 * (size_t)c;
-    const float4 r0 = __ldg(A), r1 = __ldg(A + 1), r2 = __ldg(A + 2);
-    const float gx = a * r0.y + b * r1.y + e * r2.y;
-    const float gy = a * r0.z + b * r1.z + e * r2.z;
-    const float gz = a * r0.w + b * r1.w + e * r2.w;
-    reinterpret_cast<float4 *>(m.E_f)[c] = make_float4(-gx + e0x, -gy + e0y, -gz + e0z, 0.0f);
+    const float4 *A = m.cell_f + 4 * (size_t)c;
+    reinterpret_cast<float4 *>(m.E_f)[c] =
+        dg0_field_f32(__ldg(A), __ldg(A + 1), __ldg(A + 2), __ldg(m.dofs + c), phi, e0x, e0y, e0z);
 }
 
 // b = M rho on free rows, minus the Dirichlet columns moved to the right-hand

@@ -12,6 +12,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "pg_screen.h"
 #include "punc_gpu.h"
 
 namespace pg {
@@ -29,9 +30,10 @@ struct DevMesh {
     const int4 *dofs = nullptr;       // [nc]
     double *E = nullptr;              // [nc][4]
     const double *dv_inv = nullptr;   // [ndof]
-    // FP32 copies for the mixed form
-    const float *planes_f = nullptr;  // [nc][16]
-    const float *bary_f = nullptr;    // [nc][12] padded to 16
+    // mixed form: one 64-byte record per cell, {barycentric rows 0-2 in FP32
+    // (float4 each), neighbours (int4 bits)}: what the walk, the deposit and
+    // the field read, in one aligned pair of sectors; and the FP32 field
+    const float4 *cell_f = nullptr;   // [nc][4]
     float *E_f = nullptr;             // [nc][4]
     // CG1 (vertex) field of the ESolver path: [ndof][4] (x, y, z, 0)
     const double *Ev = nullptr;
@@ -121,6 +123,7 @@ struct InjectParams {
     const uint32_t *facet_c1;
     const uint64_t *facet_seed;
     InjectSpecies sp[kMaxSpecies];
+    FluxBox32 sp32[kMaxSpecies];  // FP32 screening boxes of sp (flux_box32), built on the host
     // mixed form: fixed-point deposit target and q * 2^40 / q_max per species
     unsigned long long *rho_fixed;
     float q_scaled[kMaxSpecies];
@@ -141,7 +144,25 @@ struct MixedParams {
     int32_t cg1;                  // 1: field interpolated from the CG1 vertex field
     int32_t threads;              // block size of the particle pass (0: 256; at most 512)
     int32_t dep_agg;              // 1: lanes of a warp in the same cell add their deposits before the atomics
+    // DG0 field formed in the pass from the potential (when phi is set) at
+    // the particle's cell, as dg0_field_f32; else read from the mesh's E_f
+    const double *phi;
+    float E0[3];
 };
+
+// The mixed form's DG0 field of cell c: E = -sum_k phi_k grad lambda_k + E0
+// from the cell record's FP32 rows (grad lambda_3 = -(sum of the others)),
+// phi differences taken in FP64; explicit fmaf chains, so every translation
+// unit forms the same bits.
+__device__ __forceinline__ float4 dg0_field_f32(const float4 r0, const float4 r1, const float4 r2, int4 d,
+                                                const double *phi, float e0x, float e0y, float e0z) {
+    const double p3 = phi[d.w];
+    const float a = (float)(phi[d.x] - p3), b = (float)(phi[d.y] - p3), e = (float)(phi[d.z] - p3);
+    const float gx = fmaf(e, r2.y, fmaf(b, r1.y, __fmul_rn(a, r0.y)));
+    const float gy = fmaf(e, r2.z, fmaf(b, r1.z, __fmul_rn(a, r0.z)));
+    const float gz = fmaf(e, r2.w, fmaf(b, r1.w, __fmul_rn(a, r0.w)));
+    return make_float4(__fadd_rn(-gx, e0x), __fadd_rn(-gy, e0y), __fadd_rn(-gz, e0z), 0.0f);
+}
 
 // ESolver: rhs gather, three-component Jacobi-CG on the mass matrix, packing
 // of the vertex field (+ E0).  fp32 selects the FP32 arrays.
@@ -358,8 +379,7 @@ void launch_kinetic_mixed(const DevParticles &p, int64_t n_slots, const MixedPar
                           int nblocks, double *ke_out, cudaStream_t st);
 void launch_fixed_to_rho(const unsigned long long *fixed, const double *dv_inv, double unit, int32_t n,
                          double *rho_acc, double *rho, cudaStream_t st);
-void launch_float_tables(const double *planes, const double *bary, int32_t nc, float *planes_f, float *bary_f,
-                         cudaStream_t st);
+void launch_float_tables(const double *bary, const int4 *nbr, int32_t nc, float4 *cell_f, cudaStream_t st);
 void launch_image_charge(const DevMesh &m, const double *phi, const double *ofacets, int32_t n_ofacets,
                          int32_t n_obj, double eps0, double *out, cudaStream_t st);
 

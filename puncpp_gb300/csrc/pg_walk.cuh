@@ -46,21 +46,34 @@ __device__ __forceinline__ int walk_fp64(const DevMesh &m, double x, double y, d
     return kWalkFail;
 }
 
-// Relative bound on |FP32 plane value - exact value| in units of the sum of
+// Relative bound on |FP32 affine value - exact value| in units of the sum of
 // the terms' magnitudes: one rounding per coefficient and per fmaf, with a
 // factor two of slack.
 constexpr float kPlaneEps = 8.0f * 5.9604645e-08f;   // 8 * 2^-24
 
-// Sign of facet f's plane value at the FP32 point, decided in FP32 unless the
-// value is within the error bound of zero, then re-tested in FP64 with the
-// FP64 plane (the exact FP64 predicate at this point).
-__device__ __forceinline__ bool facet_positive(const DevMesh &m, int c, int f, float4 pl, float x, float y, float z,
-                                               int &retests) {
-    const float d = fmaf(pl.w, z, fmaf(pl.z, y, fmaf(pl.y, x, pl.x)));
-    const float s = fabsf(pl.x) + fabsf(pl.y * x) + fabsf(pl.z * y) + fabsf(pl.w * z);
-    const float e = kPlaneEps * s;
-    if (d > e) return true;
-    if (d < -e) return false;
+// Barycentric coordinates of the FP32 point from a cell record's rows 0-2
+// (the fourth is 1 - l0 - l1 - l2) and bounds on their FP32 errors.
+__device__ __forceinline__ void lambdas_f32(const float4 r0, const float4 r1, const float4 r2, float x, float y,
+                                            float z, float l[4], float e[4]) {
+    const float4 r[3] = {r0, r1, r2};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        l[k] = fmaf(r[k].w, z, fmaf(r[k].z, y, fmaf(r[k].y, x, r[k].x)));
+        e[k] = kPlaneEps * (fabsf(r[k].x) + fabsf(r[k].y * x) + fabsf(r[k].z * y) + fabsf(r[k].w * z));
+    }
+    l[3] = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, l[0]), l[1]), l[2]);
+    e[3] = e[0] + e[1] + e[2] + kPlaneEps * (1.0f + fabsf(l[0]) + fabsf(l[1]) + fabsf(l[2]));
+}
+
+// Is the FP32 point outside facet f (opposite local vertex f, where lambda_f
+// = 0)?  Decided from the sign of lambda_f when it exceeds its error bound
+// (lambda_f < 0 exactly when the facet's plane value is positive); otherwise
+// re-tested in FP64 with the FP64 plane, the exact FP64 predicate at this
+// point.
+__device__ __forceinline__ bool facet_positive(const DevMesh &m, int c, int f, float l, float e, float x, float y,
+                                               float z, int &retests) {
+    if (l < -e) return true;
+    if (l > e) return false;
     ++retests;
     const double2 *P = reinterpret_cast<const double2 *>(m.planes) + 8 * (size_t)c + 2 * f;
     const double2 a = __ldg(P), b = __ldg(P + 1);
@@ -68,22 +81,36 @@ __device__ __forceinline__ bool facet_positive(const DevMesh &m, int c, int f, f
 }
 
 // The walk of the mixed form: same facet order and semantics as walk_fp64,
-// every decision equal to the FP64 predicate at the FP32 position.
+// every decision equal to the FP64 predicate at the FP32 position.  Reads
+// one 64-byte cell record per cell visited.
 __device__ __forceinline__ int walk_mixed(const DevMesh &m, float x, float y, float z, int c, int max_steps,
                                           int &retests) {
     for (int it = 0; it < max_steps; ++it) {
-        const float4 *P = reinterpret_cast<const float4 *>(m.planes_f) + 4 * (size_t)c;
-        const int4 nb = __ldg(m.nbr + c);
+        const float4 *R = m.cell_f + 4 * (size_t)c;
+        const float4 r0 = __ldg(R), r1 = __ldg(R + 1), r2 = __ldg(R + 2), rn = __ldg(R + 3);
+        float l[4], e[4];
+        lambdas_f32(r0, r1, r2, x, y, z, l, e);
         int next;
-        if (facet_positive(m, c, 0, __ldg(P + 0), x, y, z, retests)) next = nb.x;
-        else if (facet_positive(m, c, 1, __ldg(P + 1), x, y, z, retests)) next = nb.y;
-        else if (facet_positive(m, c, 2, __ldg(P + 2), x, y, z, retests)) next = nb.z;
-        else if (facet_positive(m, c, 3, __ldg(P + 3), x, y, z, retests)) next = nb.w;
+        if (facet_positive(m, c, 0, l[0], e[0], x, y, z, retests)) next = __float_as_int(rn.x);
+        else if (facet_positive(m, c, 1, l[1], e[1], x, y, z, retests)) next = __float_as_int(rn.y);
+        else if (facet_positive(m, c, 2, l[2], e[2], x, y, z, retests)) next = __float_as_int(rn.z);
+        else if (facet_positive(m, c, 3, l[3], e[3], x, y, z, retests)) next = __float_as_int(rn.w);
         else return c;
         if (next < 0) return next;
         c = next;
     }
     return kWalkFail;
+}
+
+// __float2ll_rn(v) for finite |v| < 2^62 on the 32-bit conversion path:
+// below 2^23 in magnitude v rounds to nearest (even) in 32 bits; larger FP32
+// values are integers, rebuilt from the significand and the exponent.
+__device__ __forceinline__ long long float_to_ll_rn(float v) {
+    if (fabsf(v) < 8388608.0f) return (long long)__float2int_rn(v);
+    const unsigned u = __float_as_uint(v);
+    const int sh = (int)((u >> 23) & 0xffu) - 150;
+    const long long mag = (long long)((u & 0x7fffffu) | 0x800000u) << sh;
+    return (u >> 31) ? -mag : mag;
 }
 
 // Cell<3>::barycentric (punc/include/punc/population.h:885-893), FP64.
@@ -103,17 +130,17 @@ __device__ __forceinline__ void barycentric_fp64(const DevMesh &m, int c, double
 // atomics, so the sum is the same in any order.
 __device__ __forceinline__ void deposit_fixed(const DevMesh &m, int c, float x, float y, float z, float q_scaled,
                                               unsigned long long *rho_fixed) {
-    const float4 *A = reinterpret_cast<const float4 *>(m.bary_f) + 3 * (size_t)c;
+    const float4 *A = m.cell_f + 4 * (size_t)c;
     const float4 a0 = __ldg(A), a1 = __ldg(A + 1), a2 = __ldg(A + 2);
     const float l0 = fmaf(a0.w, z, fmaf(a0.z, y, fmaf(a0.y, x, a0.x)));
     const float l1 = fmaf(a1.w, z, fmaf(a1.z, y, fmaf(a1.y, x, a1.x)));
     const float l2 = fmaf(a2.w, z, fmaf(a2.z, y, fmaf(a2.y, x, a2.x)));
     const float l3 = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, l0), l1), l2);
     const int4 d = __ldg(m.dofs + c);
-    atomicAdd(rho_fixed + d.x, (unsigned long long)__float2ll_rn(__fmul_rn(l0, q_scaled)));
-    atomicAdd(rho_fixed + d.y, (unsigned long long)__float2ll_rn(__fmul_rn(l1, q_scaled)));
-    atomicAdd(rho_fixed + d.z, (unsigned long long)__float2ll_rn(__fmul_rn(l2, q_scaled)));
-    atomicAdd(rho_fixed + d.w, (unsigned long long)__float2ll_rn(__fmul_rn(l3, q_scaled)));
+    atomicAdd(rho_fixed + d.x, (unsigned long long)float_to_ll_rn(__fmul_rn(l0, q_scaled)));
+    atomicAdd(rho_fixed + d.y, (unsigned long long)float_to_ll_rn(__fmul_rn(l1, q_scaled)));
+    atomicAdd(rho_fixed + d.z, (unsigned long long)float_to_ll_rn(__fmul_rn(l2, q_scaled)));
+    atomicAdd(rho_fixed + d.w, (unsigned long long)float_to_ll_rn(__fmul_rn(l3, q_scaled)));
 }
 
 }  // namespace pg
