@@ -21,6 +21,7 @@ STATUS_NAMES = {
     5: "PG_ERR_WALK_LIMIT", 6: "PG_ERR_NOT_CONVERGED", 7: "PG_ERR_STATE", 8: "PG_ERR_SINGULAR",
 }
 PG_FP64, PG_MIXED = 0, 1
+PG_ERR_NOT_CONVERGED = 6
 
 (T_CELL_VERTICES, T_BARYCENTRIC, T_PLANES, T_NEIGHBOURS, T_CELL_DOFS, T_VOLUME, T_DV_INV,
  T_CSR_ROWPTR, T_CSR_COL, T_STIFFNESS, T_MASS, T_EXT_FACETS, T_BC_KIND, T_OBJ_FACETS) = range(14)

@@ -670,6 +670,10 @@ static int poisson_solve_internal(pg_sim *s, const double *pot_h, bool zero_rho,
     }
     if (oi[1] == 1) return fail(PG_ERR_NOT_CONVERGED, "PCG reached " + std::to_string(oi[0]) + " iterations, ||r|| = " + std::to_string(std::sqrt(od[0])));
     if (oi[1] == 2) return fail(PG_ERR_NOT_CONVERGED, "PCG breakdown (p.Ap <= 0) at iteration " + std::to_string(oi[0]));
+    if (oi[1] == 3)
+        return fail(PG_ERR_NOT_CONVERGED, "PCG stalled at ||r|| = " + std::to_string(std::sqrt(od[0])) + " after " +
+                                              std::to_string(oi[0]) + " iterations: the tolerance is below the "
+                                              "attainable accuracy of the mixed-precision recurrence");
     return PG_OK;
 }
 

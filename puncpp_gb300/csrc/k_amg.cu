@@ -414,6 +414,12 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M)
         grid.sync();
         grid_sum2(partB, partD, nb, sh, ra, rb);
         if (threadIdx.x == 0) {
+            // between replacements the FP32 recurrence's ||r||^2 falls by 1e6;
+            // a true residual that fell by less than 100 (10 in norm) means
+            // the recurrence has left the true residual at its attainable
+            // accuracy above the requested tolerance: stop (status 3)
+            // instead of iterating on
+            const bool stalled = pass > 0 && ra > 1e-2 * t_rr;
             t_rr = ra;
             if (pass == 0) {
                 t_bb = rb;
@@ -425,6 +431,7 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M)
             t_rmax = t_rr;
             if (t_rr <= t_tol2) { t_status = 0; scal[1] = 0.0; }
             else if (t_it >= a.max_iter) { t_status = 1; scal[1] = 0.0; }
+            else if (stalled) { t_status = 3; scal[1] = 0.0; }
             else scal[1] = 1.0;
         }
         __syncthreads();

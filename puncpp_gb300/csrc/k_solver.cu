@@ -308,6 +308,10 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_rel(PcgArgs a) {
         grid_sum2(partA, partB, nb, sh, ra, rb);
         if (threadIdx.x == 0) {
             const double rz_new = ra;
+            // the recurrence's ||r|| fell tenfold since the last replacement
+            // but the true one by less than half that: the FP32 recurrence's
+            // attainable accuracy (status 3, as k_pcg_amg)
+            scal[2] = (pass > 0 && rb > 0.25 * t_rr) ? 1.0 : 0.0;
             t_rr = rb;
             if (pass > 0) ++t_updates;
             // keep the search direction; its coefficient uses the replaced r.z
@@ -326,6 +330,7 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_rel(PcgArgs a) {
         if (threadIdx.x == 0) {
             if (t_rr <= t_tol2) { t_status = 0; scal[1] = 0.0; }
             else if (t_it >= a.max_iter) { t_status = 1; scal[1] = 0.0; }
+            else if (scal[2] != 0.0) { t_status = 3; scal[1] = 0.0; }
             else scal[1] = 1.0;
         }
         __syncthreads();

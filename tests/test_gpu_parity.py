@@ -432,3 +432,80 @@ def test_population_file_matches_reference_writer_and_round_trips(binary, lib, o
     a, b = pop.particles(), pop2.particles()
     for k in ("x", "v", "q", "m", "cell"):
         assert np.array_equal(a[k], b[k]), k
+
+
+def _permuted(ma, rng):
+    """The same mesh with its vertices renumbered at random (wide column spans
+    in every operator row)."""
+    perm = rng.permutation(ma.n_vertices)
+    coords = np.empty_like(ma.coords)
+    coords[perm] = ma.coords
+    return meshgen.MeshArrays(coords=coords, cells=perm[ma.cells], bfacets=perm[ma.bfacets], btags=ma.btags.copy(),
+                              vertex_to_dof=None, n_dofs=ma.n_dofs, Ld=ma.Ld, origin=ma.origin,
+                              n_objects=ma.n_objects)
+
+
+def _compressed_cycle_bytes(lay):
+    """Operator bytes of one AMG-PCG iteration if every operator took 16-bit
+    columns: A_0 (f32 + u16) twice, S_0 and S_l^T, A_l (l >= 1), U1 in
+    binary16 + u16, G in f32 + i32."""
+    lv, L = lay["levels"], len(lay["levels"]) - 1
+    b = 2 * lv[0]["nnz"] * 6 + lv[0]["nnz_p"] * 4
+    if L >= 2:
+        b += lv[0]["nnz_p"] * 4 + lay["cycle_nnz_u1"] * 4
+    for l in range(1, L):
+        b += lv[l]["nnz"] * 4 + (lv[l]["nnz_p"] * 4 if l < L - 1 else 0)
+    return b + lay["cycle_nnz_g"] * 8
+
+
+def test_amg_operators_with_wide_column_spans(lib, oracle_mod):
+    """A randomly renumbered mesh of more than 65,536 dofs: column offsets
+    within an operator row span more than 16 bits, so some operators keep
+    32-bit columns (more bytes than the all-16-bit layout predicts, while the
+    mesh in its natural order matches it exactly), and the solution still
+    matches a direct solve."""
+    rng = np.random.default_rng(7)
+    base = meshgen.probe_box(44, 4.0, 0.9)
+    assert base.n_dofs > 65536
+    ma = _permuted(base, rng)
+    for m_ in (base, ma):
+        pop = punc.Population(punc.Mesh(m_), pcg_rtol=1e-12, pcg_atol=1e-30, pcg_max_iter=5000)
+        lay = punc.poisson_layout(pop)
+        if m_ is base:
+            assert lay["cycle_bytes"] == _compressed_cycle_bytes(lay)
+        else:
+            assert lay["cycle_bytes"] > _compressed_cycle_bytes(lay)
+            o = oracle_mod.Oracle(ma)
+            xs = uniform_points(ma, 20000, rng)
+            vs = maxwellian_velocities(len(xs), 1.0, rng)
+            assert pop.add_particles(xs, vs, -1.0, 1.0) == o.add_particles(xs, vs, -1.0, 1.0)
+            rho = punc.distribute_cg1(pop)
+            objs = [punc.Object(2, potential=-2.0)]
+            phi_g = punc.PoissonSolver(pop, objs).solve(punc.Function(pop, "phi"), punc.Function(pop, "rho"), objs)
+            phi_o, _ = o.poisson_pcg(rho, potentials=[-2.0], rtol=1e-13, atol=1e-30, max_iter=20000, nthreads=8)
+            assert rel(phi_g, phi_o) < 1e-9
+        pop.close()
+
+
+def test_amg_pcg_reports_an_unattainable_tolerance(lib, oracle_mod):
+    """rtol 1e-16 is below what the FP32 recurrence attains on 90k dofs: the
+    solve ends with PG_ERR_NOT_CONVERGED ("stalled") instead of iterating to
+    the cap, and the solution it leaves is still at the attainable accuracy
+    (checked against the oracle's FP64 Jacobi-PCG at rtol 1e-13)."""
+    ma = meshgen.probe_box(44, 4.0, 0.9)
+    rng = np.random.default_rng(8)
+    pop = punc.Population(punc.Mesh(ma), pcg_rtol=1e-16, pcg_atol=1e-30, pcg_max_iter=5000)
+    o = oracle_mod.Oracle(ma)
+    xs = uniform_points(ma, 20000, rng)
+    vs = maxwellian_velocities(len(xs), 1.0, rng)
+    assert pop.add_particles(xs, vs, -1.0, 1.0) == o.add_particles(xs, vs, -1.0, 1.0)
+    rho = punc.distribute_cg1(pop)
+    objs = [punc.Object(2, potential=-2.0)]
+    solver = punc.PoissonSolver(pop, objs)
+    with pytest.raises(L.PgError) as err:
+        solver.solve(punc.Function(pop, "phi"), punc.Function(pop, "rho"), objs)
+    assert err.value.code == L.PG_ERR_NOT_CONVERGED and "stalled" in str(err.value)
+    phi_g = punc.Function(pop, "phi").vector()
+    phi_o, _ = o.poisson_pcg(rho, potentials=[-2.0], rtol=1e-13, atol=1e-30, max_iter=20000, nthreads=8)
+    assert rel(phi_g, phi_o) < 1e-9
+    pop.close()
