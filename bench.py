@@ -453,6 +453,186 @@ def run_reference(args):
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# ---------------------------------------------------------------------------
+# Further workloads (not the headline): the Langmuir oscillation, a batch of
+# independent probe runs, and the adjoint run.  Each prints one JSON line of
+# the same shape.
+
+def _event_ms(lib, pop, fn):
+    from puncpp_gb300 import _lib as L
+    L.check(lib.pg_synchronize(pop.handle))
+    L.check(lib.pg_event_record(pop.handle, 0))
+    out = fn()
+    L.check(lib.pg_event_record(pop.handle, 1))
+    return ctypes_ms(lib, pop, 0, 1), out
+
+
+def langmuir_load(n_side, ppc, seed=0x5EED0001):
+    """Periodic unit cube of n_side^3 x 6 cells, ppc electrons per cell
+    uniform in the cube with x displaced by 0.01 sin(2 pi x), at rest; weight
+    such that the density is 1 (omega_p = 1 with eps0 = 1)."""
+    import numpy as np
+
+    from puncpp_gb300 import meshgen
+    ma = meshgen.langmuir_cube(n_side)
+    n = ppc * ma.n_cells
+    rng = np.random.default_rng(seed)
+    x = rng.random((n, 3))
+    x[:, 0] = np.mod(x[:, 0] + 0.01 * np.sin(2 * np.pi * x[:, 0]), 1.0)
+    w = 1.0 / n
+    return ma, x, np.zeros((n, 3)), -w, w
+
+
+def run_langmuir(args):
+    """Config: periodic Langmuir cube, 16 electrons per cell, Boris dt = 0.251,
+    P1 periodic Poisson with the mean fixed to zero, K steps; FP64 plain form
+    (the headline of this workload) and the mixed form beside it; the oracle
+    (single thread, like the reference) timed on a few steps."""
+    from puncpp_gb300 import _lib as L
+    from puncpp_gb300 import punc
+    ma, x, v, q, m = langmuir_load(args.n_side, 16)
+    lib = L.load()
+    res = {}
+    for form, prec in (("fp64", L.PG_FP64), ("mixed", L.PG_MIXED)):
+        pop = punc.Population(punc.Mesh(ma), precision=prec, periodic=True, pcg_rtol=1e-10, pcg_atol=1e-12,
+                              pcg_max_iter=4000)
+        n0 = pop.add_particles(x, v, q, m)
+        punc.run_steps(pop, [], 0.251, args.warmup, first_step=True, Ld=ma.Ld)
+        punc.run_steps(pop, [], 0.251, 1, Ld=ma.Ld, step_no=args.warmup)        # graph capture
+        ms, rs = _event_ms(lib, pop, lambda: punc.run_steps(pop, [], 0.251, args.steps, Ld=ma.Ld,
+                                                             step_no=args.warmup + 1))
+        res[form] = {"value": round(n0 * args.steps / (ms / 1e3), 1), "ms_per_step": round(ms / args.steps, 4),
+                     "pcg_iterations_per_step": round(sum(r.pcg_iterations for r in rs) / args.steps, 1),
+                     "particles": n0}
+        pop.close()
+    out = {"metric": "particle-steps/s on 1 GB300 (Langmuir oscillation, FP64 plain form)",
+           "value": res["fp64"]["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": res["fp64"]["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic: seeded uniform electrons with a sin(2 pi x) "
+           "displacement on a generated periodic Kuhn cube",
+           "config": {"workload": f"langmuir-{args.n_side}: periodic unit cube {args.n_side}^3x6, 16 e- per cell, "
+                                  f"v = 0, x += 0.01 sin(2 pi x), Boris dt = 0.251, Poisson rtol 1e-10",
+                      "fp64": res["fp64"], "mixed": res["mixed"]}}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        o = O.Oracle(ma)
+        o.add_particles(x, v, q, m)
+        _, M = o.matrices()
+        solve = O.PeriodicPoisson(o, 1)
+        t0, k = time.perf_counter(), 0
+        while k < 3 or (time.perf_counter() - t0 < 10.0 and k < 20):
+            phi = solve(M @ o.distribute_cg1())
+            o.boris(o.efield(phi), (0.0, 0.0, 0.0), 0.251 * (0.5 if k == 0 else 1.0))
+            o.move(0.251, ma.Ld)
+            o.update([], 0.251)
+            k += 1
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(len(x) * k / el, 1), "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": f"{k} full steps on the oracle, one thread (the reference is "
+                                         f"single-threaded), Jacobi PCG"}
+    return out
+
+
+def run_batch(args):
+    """A batch of independent probe runs in one engine (a scaled bias sweep):
+    run r is the box [-h_r, h_r]^3 (h_r uniform in [6, 10]) of 30..50
+    sub-cubes per side x 6 tetrahedra around a sphere of radius 0.5, 1, 2 or 4,
+    biased uniformly in [-5, 5], with its own injection seed; all runs share
+    the species (simulation density 125 per unit volume: 0.2M..1M particles per
+    species per run).  Every stage is one launch for all runs, each step a
+    captured graph, launch configuration from the autotuner."""
+    import numpy as np
+
+    from puncpp_gb300 import _lib as L
+    from puncpp_gb300 import batch as B
+    from puncpp_gb300 import meshgen, punc
+    R = args.runs
+    rng = np.random.default_rng(0x5EED0004)
+    sides = rng.integers(30, 51, R)
+    halves = rng.uniform(6.0, 10.0, R)
+    radii = rng.choice([0.5, 1.0, 2.0, 4.0], R)
+    biases = rng.uniform(-5.0, 5.0, R)
+    n_sim, mi = 125.0, 1836.0
+    w = 1.0 / n_sim
+    meshes = [meshgen.probe_box(int(n), float(h), float(r)) for n, h, r in zip(sides, halves, radii)]
+    nper = [int(n_sim * ((2 * h) ** 3 - 4.0 / 3.0 * math.pi * r ** 3)) for h, r in zip(halves, radii)]
+    bt = B.Batch(meshes, precision=L.PG_MIXED, capacity=int(2.6 * 2 * sum(nper)), pcg_rtol=RTOL, pcg_atol=ATOL,
+                 pcg_max_iter=4000)
+    species = ((-w, w, 1.0), (w, mi * w, 1.0 / math.sqrt(mi)))
+    for r in range(R):
+        h = halves[r]
+        for q, m_, vth in species:
+            xs = -h + rng.random((int(nper[r] * (2 * h) ** 3 / ((2 * h) ** 3 - 4.0 / 3.0 * math.pi * radii[r] ** 3)) + 1,
+                                  3)) * (2 * h)
+            bt.add_particles(r, xs, rng.normal(0.0, vth, xs.shape), q, m_)
+    bt.create_flux([punc.Species(q, m_, n=n_sim, vth=vth) for q, m_, vth in species],
+                   seeds=[0x5EED0004 + r for r in range(R)])
+    objs = bt.objects()
+    bt.circuit(objs, biases, DT)
+    pop = bt.pop
+    lib = L.load()
+    punc.run_steps(pop, objs, DT, args.warmup, first_step=True, inject=True, seed=0x5EED0004)
+    tuning = punc.autotune(pop, objs, DT, steps_per_trial=2, inject=True, seed=0x5EED0004, step_no=args.warmup)
+    step_no = args.warmup + (24 * 2 + 41)
+    rs0 = punc.run_steps(pop, objs, DT, 1, inject=True, seed=0x5EED0004, step_no=step_no)
+    n_now = rs0[-1].n_particles
+    ms, rs = _event_ms(lib, pop, lambda: punc.run_steps(pop, objs, DT, args.steps, inject=True, seed=0x5EED0004,
+                                                         step_no=step_no + 1))
+    pushed = n_now + sum(r.n_particles for r in rs[:-1])
+    cells = sum(m.n_cells for m in meshes)
+    return {"metric": "particle-steps/s on 1 GB300 (batched independent probe runs, mixed form)",
+            "value": round(pushed / (ms / 1e3), 1), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64",
+            "data": "synthetic: seeded Maxwellian loads on generated Kuhn probe meshes",
+            "config": {"workload": f"batch-{R}: {R} probe runs in one engine, boxes [-h,h]^3 (h in [6,10]) of "
+                                   f"30..50 sub-cubes per side x 6, radii in {{0.5,1,2,4}}, biases in [-5,5], "
+                                   f"0.2M..1M particles per species per run, flux injection, dt = 0.05, captured "
+                                   f"step graph",
+                       "runs": R, "cells": cells, "particles_mean_pushed": round(pushed / args.steps),
+                       "pcg_iterations_per_step": round(sum(r.pcg_iterations for r in rs) / args.steps, 1),
+                       "tuning": tuning}}
+
+
+def run_adjoint(args):
+    """Config: periodic Langmuir mesh 32^3 x 6, 2M electrons with v ~ N(0,
+    0.1^2), uniform E0 = (0.01, 0, 0), K = 50 steps with checkpoints every 10,
+    loss ||rho_K - target||^2; value = particle-steps of the forward K steps
+    per second of forward + backward (checkpointed recompute and reverse
+    sweep with a second PCG per step)."""
+    import numpy as np
+
+    from puncpp_gb300 import _lib as L
+    from puncpp_gb300 import meshgen, punc
+    ma = meshgen.langmuir_cube(args.n_side)
+    n, K, Cc = args.adjoint_particles, 50, 10
+    rng = np.random.default_rng(32)
+    x = rng.random((n, 3))
+    v0 = rng.normal(0.0, 0.1, size=(n, 3))
+    w = 1.0 / n
+    pop = punc.Population(punc.Mesh(ma), periodic=True, pcg_rtol=1e-12, pcg_atol=1e-30, pcg_max_iter=5000)
+    target = rng.normal(0.0, 1.0, size=ma.n_dofs) * 0.05
+    pop.add_particles(x, v0, -w, w)
+    lib = L.load()
+    L.check(lib.pg_synchronize(pop.handle))
+    t0 = time.perf_counter()
+    loss = punc.adjoint_forward(pop, [], 0.1, K, Cc, target, first_step=True, E0=(0.01, 0.0, 0.0), Ld=ma.Ld)
+    t1 = time.perf_counter()
+    gv, ge, gx = punc.adjoint_backward(pop, n)
+    t2 = time.perf_counter()
+    pop.close()
+    return {"metric": "adjoint particle-steps/s on 1 GB300 (K forward steps per second of forward + backward)",
+            "value": round(n * K / (t2 - t0), 1), "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": 0,
+            "ms_per_step": round((t2 - t0) / K * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded uniform electrons, Gaussian velocities, seeded target charge vector",
+            "config": {"workload": f"adjoint-{args.n_side}: periodic {args.n_side}^3x6, {n / 1e6:g}M e-, "
+                                   f"v ~ N(0, 0.1^2), E0 = (0.01, 0, 0), K = {K}, checkpoints every {Cc}",
+                       "forward_s": round(t1 - t0, 4), "backward_s": round(t2 - t1, 4), "loss": loss,
+                       "grad_E0": [float(g) for g in ge], "host_wall_clock": True}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -460,7 +640,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="probe-80", help="probe-N: N^3 sub-cubes, particles scaled by (N/80)^3")
+    ap.add_argument("--workload", default="probe-80",
+                    help="probe-N (the headline: N^3 sub-cubes, particles scaled by (N/80)^3), langmuir-N, "
+                         "batch-R (R independent probe runs), adjoint-N")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
                     help="mixed (the headline form: FP32 particles, fixed-point deposit, mixed PCG) or fp64")
     ap.add_argument("--no-fp64-form", dest="fp64_form", action="store_false",
@@ -476,10 +658,22 @@ def main():
                     help="field path: EFieldDG0 + accel/boris, or ESolver (CG1) + accel_cg1/boris_cg1")
     ap.add_argument("--pcg-precond", default="amg", choices=sorted(PRECONDS),
                     help="Poisson preconditioner: one AMG V-cycle or Jacobi per iteration")
+    ap.add_argument("--runs", type=int, default=16, help="batch-R: runs in the batch (from the workload name)")
+    ap.add_argument("--adjoint-particles", type=int, default=2_000_000)
     args = ap.parse_args()
-    if not args.workload.startswith("probe-"):
-        ap.error("--workload must be probe-N")
+    kind = args.workload.split("-")[0]
+    if kind not in ("probe", "langmuir", "batch", "adjoint"):
+        ap.error("--workload must be probe-N, langmuir-N, batch-R or adjoint-N")
     args.n_side = int(args.workload.split("-")[1])
+    if kind != "probe":
+        if kind == "batch":
+            args.runs = args.n_side
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference arm runs the probe workload"}))
+            return
+        fn = {"langmuir": run_langmuir, "batch": run_batch, "adjoint": run_adjoint}[kind]
+        print(json.dumps(fn(args)))
+        return
     args.n_per = int(round(N_PER_SPECIES * (args.n_side / N_SIDE) ** 3))
     if args.warmup < 3:
         args.warmup = 3
