@@ -33,37 +33,43 @@ __device__ __forceinline__ double block_sum_d(double v) {
     return s;
 }
 
-// Deposit of one particle with the lanes of the warp in the same cell adding
-// their fixed-point contributions first (integer sums: the same bits as
-// separate atomics); the group's first lane issues the four atomics.
-__device__ __forceinline__ void deposit_fixed_agg(const DevMesh &m, int c, float x, float y, float z, float q_scaled,
-                                                  unsigned long long *rho_fixed) {
-    const float4 *A = m.cell_f + 4 * (size_t)c;
-    const float4 a0 = __ldg(A), a1 = __ldg(A + 1), a2 = __ldg(A + 2);
-    const float l0 = fmaf(a0.w, z, fmaf(a0.z, y, fmaf(a0.y, x, a0.x)));
-    const float l1 = fmaf(a1.w, z, fmaf(a1.z, y, fmaf(a1.y, x, a1.x)));
-    const float l2 = fmaf(a2.w, z, fmaf(a2.z, y, fmaf(a2.y, x, a2.x)));
-    const float l3 = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, l0), l1), l2);
-    long long v0 = float_to_ll_rn(__fmul_rn(l0, q_scaled)), v1 = float_to_ll_rn(__fmul_rn(l1, q_scaled));
-    long long v2 = float_to_ll_rn(__fmul_rn(l2, q_scaled)), v3 = float_to_ll_rn(__fmul_rn(l3, q_scaled));
-    const unsigned peers = __match_any_sync(__activemask(), c);
-    const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
-    for (unsigned rest = peers & ~(1u << leader); rest; rest &= rest - 1) {
-        const int src = __ffs(rest) - 1;
-        const long long w0 = __shfl_sync(peers, v0, src), w1 = __shfl_sync(peers, v1, src);
-        const long long w2 = __shfl_sync(peers, v2, src), w3 = __shfl_sync(peers, v3, src);
-        if (lane == leader) { v0 += w0; v1 += w1; v2 += w2; v3 += w3; }
+// Fixed-point deposit of one particle in cell c with barycentric
+// coordinates l[] and the cell's dofs d (deposit_fixed's arithmetic).  agg:
+// the lanes of the warp in the same cell add their contributions first
+// (integer sums: the same bits as separate atomics) and the group's first
+// lane issues the four atomics.
+__device__ __forceinline__ void deposit_lambdas(bool agg, int c, const float l[4], int4 d, float q_scaled,
+                                                unsigned long long *rho_fixed) {
+    long long v0 = float_to_ll_rn(__fmul_rn(l[0], q_scaled)), v1 = float_to_ll_rn(__fmul_rn(l[1], q_scaled));
+    long long v2 = float_to_ll_rn(__fmul_rn(l[2], q_scaled)), v3 = float_to_ll_rn(__fmul_rn(l[3], q_scaled));
+    if (agg) {
+        const unsigned peers = __match_any_sync(__activemask(), c);
+        const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+        for (unsigned rest = peers & ~(1u << leader); rest; rest &= rest - 1) {
+            const int src = __ffs(rest) - 1;
+            const long long w0 = __shfl_sync(peers, v0, src), w1 = __shfl_sync(peers, v1, src);
+            const long long w2 = __shfl_sync(peers, v2, src), w3 = __shfl_sync(peers, v3, src);
+            if (lane == leader) { v0 += w0; v1 += w1; v2 += w2; v3 += w3; }
+        }
+        if (lane != leader) return;
     }
-    if (lane != leader) return;
-    const int4 d = __ldg(m.dofs + c);
     atomicAdd(rho_fixed + d.x, (unsigned long long)v0);
     atomicAdd(rho_fixed + d.y, (unsigned long long)v1);
     atomicAdd(rho_fixed + d.z, (unsigned long long)v2);
     atomicAdd(rho_fixed + d.w, (unsigned long long)v3);
 }
 
+// Cell record of c: barycentric rows 0-2 and the neighbours (int bits).
+struct CellRec {
+    float4 r0, r1, r2, nb;
+};
+__device__ __forceinline__ CellRec load_rec(const DevMesh &m, int c) {
+    const float4 *R = m.cell_f + 4 * (size_t)c;
+    return CellRec{__ldg(R), __ldg(R + 1), __ldg(R + 2), __ldg(R + 3)};
+}
+
 template <bool PUSH, bool HAS_B, bool ACCEL, bool MOVE, bool PERIODIC, bool WALK, bool DEPOSIT>
-__global__ void __launch_bounds__(512) k_mixed(DevMesh m, DevParticles p, int64_t n_slots, MixedParams mp,
+__global__ void __launch_bounds__(512, 2) k_mixed(DevMesh m, DevParticles p, int64_t n_slots, MixedParams mp,
                                                    int max_steps, unsigned long long *__restrict__ rho_fixed,
                                                    DevState *__restrict__ st, double *__restrict__ partials) {
     double ke = 0.0;
@@ -75,29 +81,38 @@ __global__ void __launch_bounds__(512) k_mixed(DevMesh m, DevParticles p, int64_
         if (c < 0) continue;
         const int s = p.sp[i];
         float x = p.xf[i], y = p.yf[i], z = p.zf[i];
+        // the record and dofs of the particle's cell, loaded once for the
+        // field, the walk's first cell and the deposit
+        CellRec R;
+        bool have_rec = false;
+        int4 dd = make_int4(0, 0, 0, 0);
+        bool have_d = false;
         if (PUSH || MOVE) {
             float vx = p.vxf[i], vy = p.vyf[i], vz = p.vzf[i];
             if (PUSH) {
                 float4 E;
                 if (mp.cg1) {
                     // CG1 vertex field interpolated at the FP32 position
-                    const float4 *A = m.cell_f + 4 * (size_t)c;
-                    const float4 r0 = __ldg(A), r1 = __ldg(A + 1), r2 = __ldg(A + 2);
-                    const float l0 = fmaf(r0.w, z, fmaf(r0.z, y, fmaf(r0.y, x, r0.x)));
-                    const float l1 = fmaf(r1.w, z, fmaf(r1.z, y, fmaf(r1.y, x, r1.x)));
-                    const float l2 = fmaf(r2.w, z, fmaf(r2.z, y, fmaf(r2.y, x, r2.x)));
+                    R = load_rec(m, c);
+                    have_rec = true;
+                    const float l0 = fmaf(R.r0.w, z, fmaf(R.r0.z, y, fmaf(R.r0.y, x, R.r0.x)));
+                    const float l1 = fmaf(R.r1.w, z, fmaf(R.r1.z, y, fmaf(R.r1.y, x, R.r1.x)));
+                    const float l2 = fmaf(R.r2.w, z, fmaf(R.r2.z, y, fmaf(R.r2.y, x, R.r2.x)));
                     const float l3 = 1.0f - l0 - l1 - l2;
-                    const int4 d = __ldg(m.dofs + c);
+                    dd = __ldg(m.dofs + c);
+                    have_d = true;
                     const float4 *V = reinterpret_cast<const float4 *>(m.Evf);
-                    const float4 v0 = __ldg(V + d.x), v1 = __ldg(V + d.y), v2 = __ldg(V + d.z), v3 = __ldg(V + d.w);
+                    const float4 v0 = __ldg(V + dd.x), v1 = __ldg(V + dd.y), v2 = __ldg(V + dd.z), v3 = __ldg(V + dd.w);
                     E.x = fmaf(l3, v3.x, fmaf(l2, v2.x, fmaf(l1, v1.x, l0 * v0.x)));
                     E.y = fmaf(l3, v3.y, fmaf(l2, v2.y, fmaf(l1, v1.y, l0 * v0.y)));
                     E.z = fmaf(l3, v3.z, fmaf(l2, v2.z, fmaf(l1, v1.z, l0 * v0.z)));
                     E.w = 0.0f;
                 } else if (mp.phi) {
-                    const float4 *R = m.cell_f + 4 * (size_t)c;
-                    E = dg0_field_f32(__ldg(R), __ldg(R + 1), __ldg(R + 2), __ldg(m.dofs + c), mp.phi, mp.E0[0],
-                                      mp.E0[1], mp.E0[2]);
+                    R = load_rec(m, c);
+                    have_rec = true;
+                    dd = __ldg(m.dofs + c);
+                    have_d = true;
+                    E = dg0_field_f32(R.r0, R.r1, R.r2, dd, mp.phi, mp.E0[0], mp.E0[1], mp.E0[2]);
                 } else {
                     E = __ldg(reinterpret_cast<const float4 *>(m.E_f) + c);
                 }
@@ -135,24 +150,48 @@ __global__ void __launch_bounds__(512) k_mixed(DevMesh m, DevParticles p, int64_
                 p.xf[i] = x; p.yf[i] = y; p.zf[i] = z;
             }
         }
+        float l[4];
         if (WALK) {
-            const int nc = walk_mixed(m, x, y, z, c, max_steps, retests);
-            if (nc == kWalkFail) {
+            // walk_mixed with the first cell's record already loaded; the
+            // last cell's lambdas are the deposit's
+            float e[4];
+            int cc = c, end = kWalkFail;
+            for (int it = 0; it < max_steps; ++it) {
+                if (!have_rec) R = load_rec(m, cc);
+                have_rec = false;
+                lambdas_f32(R.r0, R.r1, R.r2, x, y, z, l, e);
+                int next;
+                if (facet_positive(m, cc, 0, l[0], e[0], x, y, z, retests)) next = __float_as_int(R.nb.x);
+                else if (facet_positive(m, cc, 1, l[1], e[1], x, y, z, retests)) next = __float_as_int(R.nb.y);
+                else if (facet_positive(m, cc, 2, l[2], e[2], x, y, z, retests)) next = __float_as_int(R.nb.z);
+                else if (facet_positive(m, cc, 3, l[3], e[3], x, y, z, retests)) next = __float_as_int(R.nb.w);
+                else { end = cc; break; }
+                if (next < 0) { end = next; break; }
+                cc = next;
+            }
+            if (end == kWalkFail) {
                 raise_device_error(st, PG_ERR_WALK_LIMIT, i);
                 continue;
             }
-            if (nc < 0) {
-                const int tag = -nc;
+            if (end < 0) {
+                const int tag = -end;
                 atomicAdd(reinterpret_cast<unsigned long long *>(&st->absorbed[tag < kMaxTags ? tag : 0][s]), 1ull);
                 atomicAdd(reinterpret_cast<unsigned long long *>(&st->live[s]), ~0ull);
                 p.cell[i] = kDead;
                 continue;
             }
-            if (nc != c) { p.cell[i] = nc; c = nc; }
+            if (end != c) { p.cell[i] = end; c = end; have_d = false; }
         }
         if (DEPOSIT) {
-            if (mp.dep_agg) deposit_fixed_agg(m, c, x, y, z, mp.q_scaled[s], rho_fixed);
-            else deposit_fixed(m, c, x, y, z, mp.q_scaled[s], rho_fixed);
+            if (!WALK) {
+                if (!have_rec) R = load_rec(m, c);
+                l[0] = fmaf(R.r0.w, z, fmaf(R.r0.z, y, fmaf(R.r0.y, x, R.r0.x)));
+                l[1] = fmaf(R.r1.w, z, fmaf(R.r1.z, y, fmaf(R.r1.y, x, R.r1.x)));
+                l[2] = fmaf(R.r2.w, z, fmaf(R.r2.z, y, fmaf(R.r2.y, x, R.r2.x)));
+                l[3] = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, l[0]), l[1]), l[2]);
+            }
+            if (!have_d) dd = __ldg(m.dofs + c);
+            deposit_lambdas(mp.dep_agg != 0, c, l, dd, mp.q_scaled[s], rho_fixed);
         }
     }
     if (PUSH) {
