@@ -26,6 +26,7 @@ struct pg_sim {
     int32_t nc = 0, ndof = 0, n_obj = 0, n_ext = 0, n_ofac = 0;
     std::vector<double> ext_facets_h, obj_facets_h;
     double *d_ext_facets = nullptr, *d_ofacets = nullptr;
+    float4 *d_ext_facets_f = nullptr;     // mixed form: exterior facets in FP32 (InjectParams::facets_f)
 
     // particles (two buffers for the cell sort)
     DevParticles P[2]{};
@@ -912,6 +913,7 @@ static int inject_internal(pg_sim *s, double dt, uint64_t seed, uint64_t step, b
     rc = ensure_scan_tmp(s, total + 1);
     if (rc) return rc;
     fill_flux32(ip);
+    ip.facets_f = s->d_ext_facets_f;
     // the species slots of the injection table are engine species ids
     InjectParams ipd = ip;
     for (int k = 0; k < ip.n_species; ++k) ipd.sp[k] = ip.sp[k];
@@ -1200,6 +1202,22 @@ int pg_create(const pg_mesh *mesh, const pg_config *cfg_in, pg_sim **out) {
     s->n_ext = (int32_t)(h.ext_facets.size() / 14);
     s->n_ofac = (int32_t)(h.obj_facets.size() / 7);
     if ((rc = upload(s, &s->d_ext_facets, h.ext_facets)) || (rc = upload(s, &s->d_ofacets, h.obj_facets))) return bail(rc);
+    if (cfg.precision == PG_MIXED && s->n_ext > 0) {
+        std::vector<float4> ff(4 * (size_t)s->n_ext);
+        for (int64_t j = 0; j < s->n_ext; ++j) {
+            const double *F = &h.ext_facets[14 * (size_t)j];
+            float v[12];
+            for (int k = 0; k < 12; ++k) v[k] = (float)F[1 + k];
+            int cellj = (int)F[13];
+            ff[4 * j] = make_float4(v[0], v[1], v[2], v[3]);
+            ff[4 * j + 1] = make_float4(v[4], v[5], v[6], v[7]);
+            ff[4 * j + 2] = make_float4(v[8], v[9], v[10], v[11]);
+            float cf;
+            std::memcpy(&cf, &cellj, sizeof(cf));
+            ff[4 * j + 3] = make_float4(cf, 0.0f, 0.0f, 0.0f);
+        }
+        if ((rc = upload(s, &s->d_ext_facets_f, ff))) return bail(rc);
+    }
 
     // state, reductions, sort scratch
     if ((rc = dalloc(s, &s->state, 1))) return bail(rc);
@@ -2031,6 +2049,7 @@ static void inject_enqueue(pg_sim *s, const DevParticles &Pd, double dt, uint64_
         I.q = S.q;
     }
     fill_flux32(ip);
+    ip.facets_f = s->d_ext_facets_f;
     ip.counts_dev = s->run_counts;
     ip.facet_c1 = s->d_inj_c1;
     ip.facet_seed = s->d_inj_seed;

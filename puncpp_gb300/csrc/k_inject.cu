@@ -85,7 +85,12 @@ __global__ void __launch_bounds__(kThreads, 8) k_inject_generate(DevMesh m, DevP
         const int s = idx / ip.n_facets, j = idx % ip.n_facets;
         const InjectSpecies &S = ip.sp[s];
         const double *F = facets + 14 * (size_t)j;
-        const double nx = F[10], ny = F[11], nz = F[12];
+        const bool mixed = p.xf != nullptr;
+        float4 G0 = make_float4(0, 0, 0, 0), G1 = G0, G2 = G0, G3 = G0;
+        if (mixed) {
+            const float4 *G = ip.facets_f + 4 * (size_t)j;
+            G0 = __ldg(G); G1 = __ldg(G + 1); G2 = __ldg(G + 2); G3 = __ldg(G + 3);
+        }
         const uint32_t c1 = ip.facet_c1 ? ip.facet_c1[j] : (uint32_t)j, c2 = (uint32_t)(s + 8 * (k + 1)), c3 = step;
         const uint64_t seed = ip.facet_seed ? ip.seed + ip.facet_seed[j] : ip.seed;
         const double pmax = pdf_max[idx];
@@ -96,31 +101,35 @@ __global__ void __launch_bounds__(kThreads, 8) k_inject_generate(DevMesh m, DevP
         B.vth2 = S.vth2;
         B.factor = S.factor;
         const FluxBox32 &B32 = ip.sp32[s];
-        const float nx32 = (float)nx, ny32 = (float)ny, nz32 = (float)nz, pmax32 = (float)pmax;
+        float nx32, ny32, nz32;
+        if (mixed) { nx32 = G2.y; ny32 = G2.z; nz32 = G2.w; }
+        else { nx32 = (float)F[10]; ny32 = (float)F[11]; nz32 = (float)F[12]; }
+        const float pmax32 = (float)pmax;
         const uint32_t k0 = uint32_t(seed), k1 = uint32_t(seed >> 32);
         double vx = 0, vy = 0, vz = 0;
+        uint32_t wv0 = 0, wv1 = 0, wv2 = 0, wv3 = 0, wv4 = 0, wv5 = 0;   // the accepted candidate's words
         int found = -1;
         for (int round = 0; round < kMaxRounds && found < 0; ++round) {
             const uint32_t cand = (uint32_t)round * 32u + (uint32_t)lane;
             const Philox4 ra = philox4x32_10(2u + 2u * cand, c1, c2, c3, k0, k1);
             const Philox4 rb = philox4x32_10(3u + 2u * cand, c1, c2, c3, k0, k1);
             int dec = flux_screen_fp32(B32, nx32, ny32, nz32, pmax32, ra.v[0], ra.v[2], rb.v[0], rb.v[2]);
-            double t[3];
-            if (dec < 0)
-                dec = flux_accept_fp64(B, nx, ny, nz, pmax, u01_from(ra.v[0], ra.v[1]), u01_from(ra.v[2], ra.v[3]),
-                                       u01_from(rb.v[0], rb.v[1]), u01_from(rb.v[2], rb.v[3]), t) ? 1 : 0;
+            if (dec < 0) {
+                double t[3];
+                dec = flux_accept_fp64(B, F[10], F[11], F[12], pmax, u01_from(ra.v[0], ra.v[1]),
+                                       u01_from(ra.v[2], ra.v[3]), u01_from(rb.v[0], rb.v[1]),
+                                       u01_from(rb.v[2], rb.v[3]), t) ? 1 : 0;
+            }
             const unsigned acc = __ballot_sync(0xffffffffu, dec == 1);
             if (acc) {
                 const int first = __ffs(acc) - 1;
                 found = first;
-                if (lane == first) {
-                    t[0] = B.lo[0] + B.w[0] * u01_from(ra.v[0], ra.v[1]);
-                    t[1] = B.lo[1] + B.w[1] * u01_from(ra.v[2], ra.v[3]);
-                    t[2] = B.lo[2] + B.w[2] * u01_from(rb.v[0], rb.v[1]);
-                }
-                vx = __shfl_sync(0xffffffffu, t[0], first);
-                vy = __shfl_sync(0xffffffffu, t[1], first);
-                vz = __shfl_sync(0xffffffffu, t[2], first);
+                wv0 = __shfl_sync(0xffffffffu, ra.v[0], first);
+                wv1 = __shfl_sync(0xffffffffu, ra.v[1], first);
+                wv2 = __shfl_sync(0xffffffffu, ra.v[2], first);
+                wv3 = __shfl_sync(0xffffffffu, ra.v[3], first);
+                wv4 = __shfl_sync(0xffffffffu, rb.v[0], first);
+                wv5 = __shfl_sync(0xffffffffu, rb.v[1], first);
             }
         }
         if (lane != 0) continue;
@@ -128,6 +137,42 @@ __global__ void __launch_bounds__(kThreads, 8) k_inject_generate(DevMesh m, DevP
         p.sp[i] = (uint8_t)s;
         p.pid[i] = pid_base + t;
         if (found < 0) { raise_device_error(st, PG_ERR_ARG, idx); p.cell[i] = kDead; continue; }
+        if (mixed) {
+            // mixed form: the velocity and the position in FP32 from the same
+            // random words (24-bit uniforms), the facet in FP32; the
+            // acceptance above is the FP64 decision
+            const float vxf = B32.lo[0] + B32.w[0] * u01_24(wv0);
+            const float vyf = B32.lo[1] + B32.w[1] * u01_24(wv2);
+            const float vzf = B32.lo[2] + B32.w[2] * u01_24(wv4);
+            const Philox4 q0 = philox4x32_10(0u, c1, c2, c3, k0, k1);
+            const Philox4 q1 = philox4x32_10(1u, c1, c2, c3, k0, k1);
+            const float r1 = u01_24(q0.v[0]), r2 = u01_24(q0.v[2]), r = u01_24(q1.v[0]);
+            float x = (1.0f - r1) * G0.x + r1 * G0.w;
+            float y = (1.0f - r1) * G0.y + r1 * G1.x;
+            float z = (1.0f - r1) * G0.z + r1 * G1.y;
+            const float sr = sqrtf(r2);
+            x = sr * x + (1.0f - sr) * G1.z;
+            y = sr * y + (1.0f - sr) * G1.w;
+            z = sr * z + (1.0f - sr) * G2.x;
+            const float rdt = r * (float)ip.dt;
+            x = x + rdt * vxf;
+            y = y + rdt * vyf;
+            z = z + rdt * vzf;
+            p.xf[i] = x; p.yf[i] = y; p.zf[i] = z;
+            p.vxf[i] = vxf; p.vyf[i] = vyf; p.vzf[i] = vzf;
+            int retests = 0;
+            const int c = walk_mixed(m, x, y, z, __float_as_int(G3.x), max_steps, retests);
+            if (c == kWalkFail) { raise_device_error(st, PG_ERR_WALK_LIMIT, i); p.cell[i] = kDead; continue; }
+            if (c < 0) { p.cell[i] = kDead; continue; }
+            p.cell[i] = c;
+            atomicAdd(reinterpret_cast<unsigned long long *>(&st->injected[s]), 1ull);
+            atomicAdd(reinterpret_cast<unsigned long long *>(&st->live[s]), 1ull);
+            if (deposit) deposit_fixed(m, c, x, y, z, ip.q_scaled[s], ip.rho_fixed);
+            continue;
+        }
+        vx = B.lo[0] + B.w[0] * u01_from(wv0, wv1);
+        vy = B.lo[1] + B.w[1] * u01_from(wv2, wv3);
+        vz = B.lo[2] + B.w[2] * u01_from(wv4, wv5);
         double r1, r2, r, unused;
         uniforms2(seed, 0u, c1, c2, c3, r1, r2);
         uniforms2(seed, 1u, c1, c2, c3, r, unused);
@@ -141,22 +186,6 @@ __global__ void __launch_bounds__(kThreads, 8) k_inject_generate(DevMesh m, DevP
         x = x + r * ip.dt * vx;
         y = y + r * ip.dt * vy;
         z = z + r * ip.dt * vz;
-        if (p.xf) {
-            // mixed form: round to FP32 first so the stored position and the
-            // located cell agree
-            const float xf = (float)x, yf = (float)y, zf = (float)z;
-            p.xf[i] = xf; p.yf[i] = yf; p.zf[i] = zf;
-            p.vxf[i] = (float)vx; p.vyf[i] = (float)vy; p.vzf[i] = (float)vz;
-            int retests = 0;
-            const int c = walk_mixed(m, xf, yf, zf, (int)F[13], max_steps, retests);
-            if (c == kWalkFail) { raise_device_error(st, PG_ERR_WALK_LIMIT, i); p.cell[i] = kDead; continue; }
-            if (c < 0) { p.cell[i] = kDead; continue; }
-            p.cell[i] = c;
-            atomicAdd(reinterpret_cast<unsigned long long *>(&st->injected[s]), 1ull);
-            atomicAdd(reinterpret_cast<unsigned long long *>(&st->live[s]), 1ull);
-            if (deposit) deposit_fixed(m, c, xf, yf, zf, ip.q_scaled[s], ip.rho_fixed);
-            continue;
-        }
         p.x[i] = x; p.y[i] = y; p.z[i] = z;
         p.vx[i] = vx; p.vy[i] = vy; p.vz[i] = vz;
         const int c = walk_fp64(m, x, y, z, (int)F[13], max_steps);

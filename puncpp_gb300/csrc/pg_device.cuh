@@ -124,6 +124,10 @@ struct InjectParams {
     const uint64_t *facet_seed;
     InjectSpecies sp[kMaxSpecies];
     FluxBox32 sp32[kMaxSpecies];  // FP32 screening boxes of sp (flux_box32), built on the host
+    // mixed form: exterior facets in FP32, 4 float4 each: (v0, v1.x), (v1.yz,
+    // v2.xy), (v2.z, inward normal), (cell as int bits, 0, 0, 0); null in the
+    // FP64 form
+    const float4 *facets_f;
     // mixed form: fixed-point deposit target and q * 2^40 / q_max per species
     unsigned long long *rho_fixed;
     float q_scaled[kMaxSpecies];
