@@ -1626,16 +1626,12 @@ static void pass_field(pg_sim *s, MixedParams &xp, const double E0[3]) {
     for (int j = 0; j < 3; ++j) s->E0_last[j] = E0[j];
 }
 
-// The DG0 field a step's push reads (FP64 form).
-static void step_efield(pg_sim *s, const double E0[3]) {
-    if (is_mixed(s)) {
-        launch_efield_f32(s->dm, s->phi, E0, s->stream);
-        s->E64_stale = true;
-        for (int j = 0; j < 3; ++j) s->E0_last[j] = E0[j];
-    } else {
-        launch_efield(s->dm, s->phi, E0, s->stream);
-        s->E64_stale = false;
-    }
+// The FP64 form's step field: the field kernel (the FP64 pass is bound by
+// FP64 issue, so forming the field per particle in the pass costs as much as
+// this per-cell kernel).
+static void step_field_f64(pg_sim *s, const double E0[3]) {
+    launch_efield(s->dm, s->phi, E0, s->stream);
+    s->E64_stale = false;
 }
 
 int pg_efield_dg0(pg_sim *s, const double *phi) {
@@ -2115,7 +2111,7 @@ static int enqueue_step(pg_sim *s, const pg_step_args *a, bool first) {
         const int err = launch_esolve(e, s->stream);
         if (err) return fail(PG_ERR_CUDA, std::string("ESolver launch: ") + cudaGetErrorString((cudaError_t)err));
     } else if (!is_mixed(s)) {
-        step_efield(s, a->E0);
+        step_field_f64(s, a->E0);
     }
     const double dt_push = first ? 0.5 * a->dt : a->dt;
     cudaMemsetAsync(s->state->absorbed, 0, sizeof(s->state->absorbed), s->stream);
@@ -2709,7 +2705,7 @@ int pg_step(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_obje
         if (rc) return rc;
     } else if (!is_mixed(s)) {
         StageScope t(s, "efield");
-        step_efield(s, a->E0);
+        step_field_f64(s, a->E0);
     }
     // accelerator + move + update, depositing the next step's charge
     {

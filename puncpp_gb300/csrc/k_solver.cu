@@ -22,29 +22,12 @@ constexpr int kThreads = 256;
 __global__ void k_efield(DevMesh m, const double *__restrict__ phi, double e0x, double e0y, double e0z) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.nc) return;
-    const int4 d = m.dofs[c];
-    const double p3 = phi[d.w];
-    const double a = phi[d.x] - p3, b = phi[d.y] - p3, e = phi[d.z] - p3;
-    const double *A = m.bary + 12 * (size_t)c;
-    const double gx = a * A[1] + b * A[5] + e * A[9];
-    const double gy = a * A[2] + b * A[6] + e * A[10];
-    const double gz = a * A[3] + b * A[7] + e * A[11];
+    double ex, ey, ez;
+    dg0_field_f64(m.bary + 12 * (size_t)c, m.dofs[c], phi, e0x, e0y, e0z, ex, ey, ez);
     double2 *E = reinterpret_cast<double2 *>(m.E) + 2 * (size_t)c;
-    const double ex = -gx + e0x, ey = -gy + e0y, ez = -gz + e0z;
     E[0] = make_double2(ex, ey);
     E[1] = make_double2(ez, 0.0);
     if (m.E_f) reinterpret_cast<float4 *>(m.E_f)[c] = make_float4((float)ex, (float)ey, (float)ez, 0.0f);
-}
-
-// The DG0 field of the mixed form's step, FP32 only: E_c = -sum_k phi_k
-// grad lambda_k(c) + E0 from the FP32 barycentric rows of the cell records
-// (the FP64 field is formed on demand).
-__global__ void k_efield_f32(DevMesh m, const double *__restrict__ phi, float e0x, float e0y, float e0z) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= m.nc) return;
-    const float4 *A = m.cell_f + 4 * (size_t)c;
-    reinterpret_cast<float4 *>(m.E_f)[c] =
-        dg0_field_f32(__ldg(A), __ldg(A + 1), __ldg(A + 2), __ldg(m.dofs + c), phi, e0x, e0y, e0z);
 }
 
 // b = M rho on free rows, minus the Dirichlet columns moved to the right-hand
@@ -472,13 +455,6 @@ void launch_efield(const DevMesh &m, const double *phi, const double E0[3], cuda
     if (m.nc <= 0) return;
     count_launches(1);
     k_efield<<<(m.nc + kThreads - 1) / kThreads, kThreads, 0, st>>>(m, phi, E0[0], E0[1], E0[2]);
-}
-
-void launch_efield_f32(const DevMesh &m, const double *phi, const double E0[3], cudaStream_t st) {
-    if (m.nc <= 0) return;
-    count_launches(1);
-    k_efield_f32<<<(m.nc + kThreads - 1) / kThreads, kThreads, 0, st>>>(m, phi, (float)E0[0], (float)E0[1],
-                                                                          (float)E0[2]);
 }
 
 void launch_rhs(const DevMesh &m, const int64_t *msptr, const int32_t *mswidth, const int32_t *mscol,

@@ -93,6 +93,22 @@ struct PushParams {
     int32_t threads;              // block size of the particle pass (0: 256; at most 512)
 };
 
+// EFieldDG0 (punc/src/efield.cpp:95-99) for cell c with barycentric matrix A
+// ([12], rows 0-2): E = -(sum_k (phi_k - phi_3) grad lambda_k) + E0, each
+// product and sum rounded in this order (the oracle's order, independent of
+// the translation unit's --fmad setting).
+__device__ __forceinline__ void dg0_field_f64(const double *A, int4 d, const double *phi, double e0x, double e0y,
+                                              double e0z, double &ex, double &ey, double &ez) {
+    const double p3 = phi[d.w];
+    const double a = __dadd_rn(phi[d.x], -p3), b = __dadd_rn(phi[d.y], -p3), e = __dadd_rn(phi[d.z], -p3);
+    const double gx = __dadd_rn(__dadd_rn(__dmul_rn(a, A[1]), __dmul_rn(b, A[5])), __dmul_rn(e, A[9]));
+    const double gy = __dadd_rn(__dadd_rn(__dmul_rn(a, A[2]), __dmul_rn(b, A[6])), __dmul_rn(e, A[10]));
+    const double gz = __dadd_rn(__dadd_rn(__dmul_rn(a, A[3]), __dmul_rn(b, A[7])), __dmul_rn(e, A[11]));
+    ex = __dadd_rn(-gx, e0x);
+    ey = __dadd_rn(-gy, e0y);
+    ez = __dadd_rn(-gz, e0z);
+}
+
 struct MoveParams {
     double dt;
     int32_t periodic;
@@ -276,8 +292,6 @@ void count_launches(int n);
 long long launches_so_far();
 
 void launch_efield(const DevMesh &m, const double *phi, const double E0[3], cudaStream_t st);
-// FP32 field only (mixed form), from the FP32 barycentric rows
-void launch_efield_f32(const DevMesh &m, const double *phi, const double E0[3], cudaStream_t st);
 void launch_push(const DevMesh &m, const DevParticles &p, int64_t n_slots, const PushParams &pp,
                  double *partials, int nblocks, double *ke_out, cudaStream_t st);
 void launch_move(const DevParticles &p, int64_t n_slots, const MoveParams &mp, cudaStream_t st);
