@@ -12,12 +12,13 @@
 //     S = (I - w D^-1 A) P,
 // with the last restriction and the coarse solve in one product
 // (G = C^-1 S^T) and the up-sweep of levels >= 1 collapsed into one product
-// (U1 = [S_1 | S_1 S_2 | ...]): L + 1 grid-wide phases for L >= 2 levels
-// above the coarsest.  The product A z of the search direction update is
+// (U1 = [S_1 | S_1 S_2 | ...]): L + 2 grid-wide phases (L down, the
+// up-sweep, the prolongation to level 0) for L >= 2 levels above the
+// coarsest.  The product A z of the search direction update is
 // folded into the next matrix phase (A p = A z + beta A p_old), r.z into the
 // last cycle phase, and the x and r update of a CG step into the cycle's
-// first phase (r - alpha Ap gathered on the fly, two residual buffers): an
-// iteration is L + 2 grid barriers.  The smoothing products W_l b_l, needed
+// first phase (r - alpha Ap gathered on the fly, two residual buffers): with
+// the phase of A p, an iteration is L + 3 grid barriers.  The smoothing products W_l b_l, needed
 // only by the up-sweep, run in the down-sweep phases whose restrictions are
 // small.
 #include <cooperative_groups.h>
