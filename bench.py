@@ -633,6 +633,25 @@ def run_adjoint(args):
                        "grad_E0": [float(g) for g in ge], "host_wall_clock": True}}
 
 
+def combine_replicas(res, world):
+    """Whole-job line of N independent replicas (one per rank, process group
+    initialised): the slowest rank's time per step, and the particle-steps
+    all ranks processed divided by it."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([res["ms_per_step"]], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    v = torch.tensor([res["value"] * res["ms_per_step"]], dtype=torch.float64)
+    dist.all_reduce(v)
+    out = dict(res)
+    out["config"] = dict(res["config"])
+    out["ms_per_step"] = float(t.item())
+    out["value"] = round(float(v.item()) / float(t.item()), 1)
+    out["n_gpus"] = world
+    out["config"]["parallelism"] = f"replicas x{world}"
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -715,15 +734,7 @@ def main():
                               "max": float(np.abs(d).max() / np.abs(rho64).max()),
                               "bar": 1e-5, "after": "one step from identical particles and injection streams"}
     if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([res["ms_per_step"]], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        v = torch.tensor([res["value"] * res["ms_per_step"]], dtype=torch.float64)
-        dist.all_reduce(v)
-        res["ms_per_step"] = float(t.item())
-        res["value"] = round(float(v.item()) / float(t.item()), 1)
-        res["config"]["parallelism"] = f"replicas x{world}"
+        res = combine_replicas(res, world)
     if rank == 0:
         if not args.no_cpu_baseline:
             res["cpu_baseline"] = cpu_baseline(args)
