@@ -200,11 +200,12 @@ __device__ __forceinline__ void apply_t(const SpOp &S, XV xv, PRE pre, EPI epi, 
     } else {
         // g / 32 warps of one block per row; partial sums meet in shared memory
         __shared__ float red[kPcgThreads / 32];
+        // (t0, ts) cover whole blocks: block t0 / blockDim of ts / blockDim
         const int g = S.g;
         const int per_block = blockDim.x / g;
         const int lane = threadIdx.x & (g - 1);
-        const int grp = blockIdx.x * per_block + threadIdx.x / g;
-        const int ngrp = gridDim.x * per_block;
+        const int grp = (t0 / (int)blockDim.x) * per_block + threadIdx.x / g;
+        const int ngrp = (ts / (int)blockDim.x) * per_block;
         const int rounds = (S.n + ngrp - 1) / ngrp;
         for (int t = 0; t < rounds; ++t) {
             const int i = grp + t * ngrp;
@@ -233,6 +234,46 @@ __device__ __forceinline__ void apply(const SpOp &S, XV xv, PRE pre, EPI epi, in
         if (S.val16) apply_t<false, true>(S, xv, pre, epi, t0, ts);
         else apply_t<false, false>(S, xv, pre, epi, t0, ts);
     }
+}
+
+// Blocks that take one pass over S (kRows rows per thread or lane group,
+// one row per lane group of the block path).
+__device__ __forceinline__ int pass_blocks(const SpOp &S) {
+    const int bd = blockDim.x;
+    if (S.g > 32) {
+        const int per_block = bd / S.g;
+        return (S.n + per_block - 1) / per_block;
+    }
+    const int64_t threads = (int64_t)((S.n + kRows - 1) / kRows) * S.g;
+    return (int)((threads + bd - 1) / bd);
+}
+
+// Independent products of one grid phase on disjoint ranges of blocks, so
+// that their latency chains run side by side instead of one after another:
+// when the k <= 4 products' one-pass needs n0..n3 fit in the grid, each gets
+// its need (the largest also the spare blocks).  Returns this block's product
+// and range, or -1 (run them all, one after another, on the whole grid) when
+// they do not fit: a product squeezed into fewer blocks would take a second
+// pass and lengthen its chain.
+__device__ __forceinline__ int split_blocks(int k, int n0, int n1, int n2, int n3, int nb, int &lo, int &hi) {
+    const int need[4] = {n0 > 0 ? n0 : 1, n1 > 0 ? n1 : 1, n2 > 0 ? n2 : 1, n3 > 0 ? n3 : 1};
+    int tot = 0, big = 0, bigv = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        if (i < k) {
+            tot += need[i];
+            if (need[i] > bigv) { bigv = need[i]; big = i; }
+        }
+    if (k < 2 || tot > nb) return -1;
+    int mine = -1, b = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        if (i < k) {
+            const int share = need[i] + (i == big ? nb - tot : 0);
+            if ((int)blockIdx.x >= b && (int)blockIdx.x < b + share) { mine = i; lo = b; hi = b + share; }
+            b += share;
+        }
+    return mine;
 }
 
 // The residual as phase 0 of a V-cycle reads it: right after a CG step the
@@ -312,23 +353,48 @@ __device__ double vcycle_phase0(const AmgDev &M, const PcgArgs &a, const float *
 // and t_1 = W_1 b_1 in phase L-1, where the restrictions leave the grid
 // idle), the collapsed up-sweep y_1 = t_1 + U1 [t_2 .. t_{L-1}, y_L]
 // (L >= 2), then z = t_0 + S_0 y_1; returns this thread's share of r.z.
-__device__ double vcycle_rest(const AmgDev &M, const float *r, float *z, cg::grid_group &grid, int t0, int ts) {
+__device__ __forceinline__ double vcycle_rest(const AmgDev &M, const float *r, float *z, cg::grid_group &grid,
+                                              int t0, int ts) {
     const int L = M.nlev - 1;
     for (int l = 1; l < L; ++l) {
         const float *b = M.lev[l].b;
         const auto gb = [=](int j) { return b[j]; };
-        if (l < L - 1) {
-            float *bn = M.lev[l + 1].b;
-            apply(M.lev[l].ST, gb, NoPre{}, [=](int i, float s, int) { bn[i] = s; }, t0, ts);
-        } else {
-            float *yL = M.yL;
-            apply(M.G, gb, NoPre{}, [=](int i, float s, int) { yL[i] = s; }, t0, ts);
+        // this phase's independent products, each on its own blocks
+        const SpOp &R = l < L - 1 ? M.lev[l].ST : M.G;
+        const int nR = pass_blocks(R);
+        const int nS = l >= 2 ? pass_blocks(M.lev[l].A) : 0;
+        const int n0 = l == 1 ? pass_blocks(M.lev[0].A) : 0;
+        const int n1 = l == L - 1 ? pass_blocks(M.lev[1].A) : 0;
+        // product order: R, then W_l (l >= 2), W_0 (l == 1), W_1 (l == L-1)
+        int need[4] = {nR, 0, 0, 0}, k = 1;
+        if (l >= 2) need[k++] = nS;
+        if (l == 1) need[k++] = n0;
+        if (l == L - 1) need[k++] = n1;
+        int lo = 0, hi = 0;
+        const int my = split_blocks(k, need[0], k > 1 ? need[1] : 0, k > 2 ? need[2] : 0, k > 3 ? need[3] : 0,
+                                    (int)gridDim.x, lo, hi);
+        int idx = 0, pt0 = t0, pts = ts;
+        const auto mine = [&](int q) {
+            if (my < 0) { pt0 = t0; pts = ts; return true; }
+            if (q != my) return false;
+            pt0 = ((int)blockIdx.x - lo) * (int)blockDim.x + (int)threadIdx.x;
+            pts = (hi - lo) * (int)blockDim.x;
+            return true;
+        };
+        if (mine(idx++)) {
+            if (l < L - 1) {
+                float *bn = M.lev[l + 1].b;
+                apply(R, gb, NoPre{}, [=](int i, float s, int) { bn[i] = s; }, pt0, pts);
+            } else {
+                float *yL = M.yL;
+                apply(R, gb, NoPre{}, [=](int i, float s, int) { yL[i] = s; }, pt0, pts);
+            }
         }
-        if (l >= 2) smooth(M.lev[l], gb, M.lev[l].t, t0, ts);
-        if (l == 1) smooth(M.lev[0], [=](int j) { return r[j]; }, M.lev[0].t, t0, ts);
-        if (l == L - 1) {
+        if (l >= 2 && mine(idx++)) smooth(M.lev[l], gb, M.lev[l].t, pt0, pts);
+        if (l == 1 && mine(idx++)) smooth(M.lev[0], [=](int j) { return r[j]; }, M.lev[0].t, pt0, pts);
+        if (l == L - 1 && mine(idx++)) {
             const float *b1 = M.lev[1].b;
-            smooth(M.lev[1], [=](int j) { return b1[j]; }, M.lev[1].t, t0, ts);
+            smooth(M.lev[1], [=](int j) { return b1[j]; }, M.lev[1].t, pt0, pts);
         }
         grid.sync();
     }
