@@ -42,6 +42,14 @@ def workload_name(n_side, n_per):
             f"{n_per / 1e6:g}M e- + {n_per / 1e6:g}M ions (m_i=1836), Maxwellian T_e=T_i, CM bias -2 kT/e, "
             f"flux injection, dt=0.05, Poisson rtol 1e-10 atol 1e-12")
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# dominant kernels on probe-80 in the mixed form, from one ncu capture each
+# of this bench's command (the summaries under profiles/ give the commands)
+PROFILED_TRAFFIC = {
+    "k_pcg_amg": (1.204e9, "profiles/k_pcg_amg_probe80_mixed.md: 987 MB read + 217 MB written per solve"),
+    "k_mixed": (0.562e9, "profiles/k_mixed_probe80.md: 455 MB read + 106 MB written per launch"),
+}
+
 DT = 0.05
 BIAS = -2.0
 RTOL, ATOL = 1e-10, 1e-12
@@ -285,9 +293,14 @@ def run_ours(args):
 
     def roof_of(name, bytes_total, t_ms, model):
         ach = bytes_total / (t_ms / 1e3) / 1e9 if t_ms > 0 else 0.0
-        return {"bound": "hbm", "kernel": name, "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
-                "frac": round(ach / hbm, 4), "peak_source": peak_src, "traffic": None,
-                "algorithmic_bytes": model}
+        out = {"bound": "hbm", "kernel": name, "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
+               "frac": round(ach / hbm, 4), "peak_source": peak_src, "traffic": None,
+               "algorithmic_bytes": model}
+        key = name.split(" ")[0]
+        if mixed and args.n_side == N_SIDE and key in PROFILED_TRAFFIC and args.pcg_precond == "amg":
+            out["traffic"], out["traffic_source"] = PROFILED_TRAFFIC[key]
+            out["traffic_unit"] = "bytes per launch"
+        return out
 
     r_part = roof_of("k_mixed (fused FP32 DG0 field+push+move+walk, fixed-point deposit)" if mixed
                      else "k_particles (fused FP64 push+move+walk+deposit)", args.steps * pb, part_ms, pmodel)
