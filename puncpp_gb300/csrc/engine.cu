@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "pg_device.cuh"
+#include "pg_reduce.cuh"
 #include "pg_amg.h"
 #include "pg_internal.h"
 
@@ -393,12 +394,39 @@ std::vector<std::vector<int>> charge_sharing_sets(std::vector<pg_source> vs, int
 // Lanes per row of an AMG operator: SELL-32 with one thread per row up to 12
 // entries a row on average, else CSR with a power of two of lanes (at most
 // 512, the block) giving each lane three to six entries.
-static int lanes_per_row(const Csr &A) {
-    const double avg = A.n > 0 ? (double)A.ci.size() / (double)A.n : 0.0;
-    if (avg <= 12.0) return 1;
-    int g = 2;
-    while (g < 512 && 2.0 * g * 3.0 <= avg) g *= 2;
-    return g;
+// Lanes per row for an operator applied by `threads` threads of the
+// cooperative PCG: the choice with the shortest chain of dependent memory
+// round trips per thread, the quantity that bounds a latency-bound phase.
+// g == 1: SELL-32, one thread per row, four rows and two entries of each per
+// step; g = 2..32: CSR, g lanes per row, four rows per lane group, two entries
+// per lane per step; g = 64..512: the warps of one block per row, four
+// entries per lane per step.  A round (rows of one pass) costs one trip for
+// the row offsets plus two (column, then value gathered) per step.
+static int lanes_per_row(const Csr &A, int64_t threads) {
+    const double n = (double)std::max<int64_t>(1, A.n);
+    double avg = A.n > 0 ? (double)A.ci.size() / n : 0.0, wmax = 0.0;
+    for (int64_t r = 0; r < A.n; ++r) wmax = std::max(wmax, (double)(A.rp[r + 1] - A.rp[r]));
+    const double T = (double)std::max<int64_t>(threads, 32);
+    auto chain = [&](int g) {
+        if (g == 1) {
+            // SELL slices pad to their longest row
+            const double rounds = std::ceil(n / T / 4.0), steps = std::ceil(std::min(wmax, 1.25 * avg) / 2.0);
+            return rounds * (1.0 + 2.0 * steps);
+        }
+        if (g <= 32) {
+            const double groups = std::floor(T / g), rounds = std::ceil(n / groups / 4.0);
+            return rounds * (1.0 + 2.0 * std::ceil(avg / g / 2.0));
+        }
+        const double per_round = std::floor(T / g), rounds = std::ceil(n / per_round);
+        return rounds * (2.0 + 2.0 * std::ceil(avg / g / 4.0));   // + the block's partial-sum barriers
+    };
+    int best = avg <= 12.0 ? 1 : 2;
+    double bc = chain(best);
+    for (int g = 2; g <= 512; g *= 2) {
+        const double c = chain(g);
+        if (c < bc - 1e-9) { bc = c; best = g; }
+    }
+    return best;
 }
 
 // Upload a CSR operator: SELL-32 (padding: the slice's first column, value
@@ -530,6 +558,9 @@ static int setup_amg(pg_sim *s, const std::vector<int32_t> &arow, const std::vec
     s->amg_nnz_u1 = (int64_t)cyc.U1.ci.size();
     AmgDev &M = s->amg;
     M = AmgDev{};
+    // threads of the solve's grid (fewer blocks for small systems)
+    const int64_t gt = (int64_t)std::min<int64_t>(pcg_amg_grid_blocks(), (A0.n + kPcgThreads - 1) / kPcgThreads) *
+                       kPcgThreads;
     M.nlev = (int32_t)h.levels.size();
     const int L = M.nlev - 1;
     s->amg_rows.assign(M.nlev, 0);
@@ -552,14 +583,14 @@ static int setup_amg(pg_sim *s, const std::vector<int32_t> &arow, const std::vec
         }
         if (l == L) break;   // the coarsest level lives in G (or cinv when L == 0)
         if (l > 0) {
-            if ((rc = upload_op(s, Lv.A, lanes_per_row(Lv.A), D.A, true, true))) return rc;
+            if ((rc = upload_op(s, Lv.A, lanes_per_row(Lv.A, gt), D.A, true, true))) return rc;
             std::vector<float> dinv(Lv.dinv.begin(), Lv.dinv.end());
             float *d_dinv;
             if ((rc = upload(s, &d_dinv, dinv)) || (rc = dalloc(s, &D.b, Lv.A.n))) return rc;
             D.dinv = d_dinv;
         }
         D.omega = (float)Lv.omega;
-        if (l < L - 1 && (rc = upload_op(s, Lv.ST, lanes_per_row(Lv.ST), D.ST, true, true))) return rc;
+        if (l < L - 1 && (rc = upload_op(s, Lv.ST, lanes_per_row(Lv.ST, gt), D.ST, true, true))) return rc;
         if (l >= 2) D.t = M.stack + cyc.stack_off[l];
         else if ((rc = dalloc(s, &D.t, Lv.A.n))) return rc;
     }
@@ -573,13 +604,13 @@ static int setup_amg(pg_sim *s, const std::vector<int32_t> &arow, const std::vec
         for (int64_t i = 0; i <= nc; ++i) C.rp[i] = i * nc;
         for (int64_t k = 0; k < nc * nc; ++k) C.ci[k] = (int32_t)(k % nc);
         C.v = h.coarse_inv;
-        if ((rc = upload_op(s, C, lanes_per_row(C), M.cinv))) return rc;
+        if ((rc = upload_op(s, C, lanes_per_row(C, gt), M.cinv))) return rc;
     } else {
-        if ((rc = upload_op(s, h.levels[0].S, lanes_per_row(h.levels[0].S), M.S0, true, true)) ||
-            (rc = upload_op(s, cyc.G, lanes_per_row(cyc.G), M.G)))
+        if ((rc = upload_op(s, h.levels[0].S, lanes_per_row(h.levels[0].S, gt), M.S0, true, true)) ||
+            (rc = upload_op(s, cyc.G, lanes_per_row(cyc.G, gt), M.G)))
             return rc;
         M.yL = L >= 2 ? M.stack + cyc.stack_off[L] : M.stack;
-        if (L >= 2 && ((rc = upload_op(s, cyc.U1, lanes_per_row(cyc.U1), M.U1, true, true)) ||
+        if (L >= 2 && ((rc = upload_op(s, cyc.U1, lanes_per_row(cyc.U1, gt), M.U1, true, true)) ||
                        (rc = dalloc(s, &M.y1, h.levels[1].A.n))))
             return rc;
     }
