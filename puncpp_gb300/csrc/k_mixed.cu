@@ -72,7 +72,7 @@ template <bool PUSH, bool HAS_B, bool ACCEL, bool MOVE, bool PERIODIC, bool WALK
 __global__ void __launch_bounds__(512, 2) k_mixed(DevMesh m, DevParticles p, int64_t n_slots, MixedParams mp,
                                                    int max_steps, unsigned long long *__restrict__ rho_fixed,
                                                    DevState *__restrict__ st, double *__restrict__ partials) {
-    double ke = 0.0;
+    float ke = 0.0f;   // this thread's particles in FP32 (~13 per thread), the block sum in FP64
     int retests = 0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t n_use = slots_in_use(p, n_slots);
@@ -119,12 +119,12 @@ __global__ void __launch_bounds__(512, 2) k_mixed(DevMesh m, DevParticles p, int
                 const float coef = mp.coef[s], hm = mp.half_m[s];
                 if (ACCEL) {
                     const float ax = E.x * coef, ay = E.y * coef, az = E.z * coef;
-                    ke += (double)(hm * fmaf(vx, vx + ax, fmaf(vy, vy + ay, vz * (vz + az))));
+                    ke += hm * fmaf(vx, vx + ax, fmaf(vy, vy + ay, vz * (vz + az)));
                     vx += ax; vy += ay; vz += az;
                 } else {
                     const float hx = coef * E.x, hy = coef * E.y, hz = coef * E.z;
                     const float mx = vx + hx, my = vy + hy, mz = vz + hz;
-                    ke += (double)(hm * fmaf(mx, mx, fmaf(my, my, mz * mz)));
+                    ke += hm * fmaf(mx, mx, fmaf(my, my, mz * mz));
                     float px = mx, py = my, pz = mz;
                     if (HAS_B) {
                         const float t0 = mp.t[s][0], t1 = mp.t[s][1], t2 = mp.t[s][2];
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(512, 2) k_mixed(DevMesh m, DevParticles p, int
         }
     }
     if (PUSH) {
-        const double t = block_sum_d(ke);
+        const double t = block_sum_d((double)ke);
         if (threadIdx.x == 0) partials[blockIdx.x] = t;
     }
     if (WALK && retests) atomicAdd(reinterpret_cast<unsigned long long *>(&st->retests), (unsigned long long)retests);
