@@ -239,7 +239,7 @@ def run_ours(args):
 
     # e2e: step by step through the C ABI, each step's outputs read back to host
     # memory (potential, objects, the result row)
-    phi_host = np.zeros(mesh.n_dofs)
+    phi_host, pinned = pinned_host(mesh.n_dofs)
     L.check(lib.pg_synchronize(pop.handle))
     e2e_pushed = 0
     t0 = time.perf_counter()
@@ -336,13 +336,27 @@ def run_ours(args):
         "roofline": roof, "roofline_particles": r_part, "roofline_pcg": r_pcg,
         "e2e": {"value": round(e2e_pushed / e2e_s, 1), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
-                "path": "pg_step + pg_get_phi per step through the C ABI, host wall clock"},
+                "path": "pg_step + pg_get_phi per step through the C ABI, host wall clock",
+                "host_buffer": "pinned" if pinned else "pageable"},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "wall_s_timed": round(t_wall, 3),
     }
     pop.close()
     return out, rho_first
+
+
+def pinned_host(n):
+    """An FP64 host buffer in page-locked memory (a numpy view of a pinned
+    torch tensor) for the per-step read-back of the e2e leg; pageable memory
+    if torch cannot pin."""
+    import numpy as np
+    try:
+        import torch
+        t = torch.empty(n, dtype=torch.float64, pin_memory=True)
+        return t.numpy(), True
+    except Exception:
+        return np.zeros(n), False
 
 
 def amg_iteration_bytes(lay):
