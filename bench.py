@@ -274,7 +274,7 @@ def run_ours(args):
     part_ms = stages.get("push_move_update_deposit", 0.0) * sc
     pcg_ms = stages.get("pcg", 0.0) * sc
     mixed = args.precision == "mixed"
-    # algorithmic bytes (see DESIGN.md): particle pass per particle / occupied cell / dof,
+    # algorithmic bytes: particle pass per particle / occupied cell / dof,
     # PCG per iteration per nonzero / dof
     if mixed:
         pb, cb, pmodel = (n_avg * 57 + occ * 80 + nv * 16, None,

@@ -311,6 +311,12 @@ int pg_adjoint_forward(pg_sim *sim, const pg_step_args *args, pg_object *objects
  * adjoint is a second PCG on the same symmetric matrix.  Any output may be
  * NULL.  The state returns to the one after the forward steps. */
 int pg_adjoint_backward(pg_sim *sim, double *grad_v, int64_t n_out, double *grad_E0, double *grad_x0);
+/* After pg_adjoint_backward: the gradient of the loss with respect to the
+ * fixed potentials of the objects passed to pg_adjoint_forward (the object
+ * bias), grad_pot[k] for object k: phi is affine in each potential V_k with
+ * slope the unit-potential Laplace solution L_k, so the gradient is the sum
+ * over the steps of <phibar_n, L_k>.  n_objects must match the forward call. */
+int pg_adjoint_potential_gradient(pg_sim *sim, double *grad_pot, int32_t n_objects);
 int pg_adjoint_release(pg_sim *sim);
 /* Sort particles by cell and drop absorbed slots. */
 int pg_sort(pg_sim *sim);

@@ -145,6 +145,7 @@ SIGNATURES = {
     "pg_adjoint_forward": ([_P, C.POINTER(StepArgs), C.POINTER(Object), C.c_int32, C.c_int32, C.c_int32, _D, _D],
                            C.c_int),
     "pg_adjoint_backward": ([_P, _D, C.c_int64, _D, _D], C.c_int),
+    "pg_adjoint_potential_gradient": ([_P, _D, C.c_int32], C.c_int),
     "pg_adjoint_release": ([_P], C.c_int),
     "pg_set_tuning": ([_P, C.POINTER(Tuning)], C.c_int),
     "pg_get_tuning": ([_P, C.POINTER(Tuning)], C.c_int),

@@ -115,6 +115,8 @@ struct pg_sim {
         double *bar = nullptr;                // xbar, ybar, zbar, vxbar, vybar, vzbar ([6][n])
         double *Ebar = nullptr, *phibar = nullptr, *y = nullptr, *rhobar = nullptr, *target = nullptr;
         double *small = nullptr;              // [0..2] E0bar, [3] loss, [8..15] push coefficients
+        double *lap = nullptr;                // [n_obj][ndof] unit-potential Laplace solutions L_k
+        double *gpot = nullptr;               // [n_obj] sum over steps of <phibar, L_k>
     } adj;
 
     // diagnostics scratch (allocated on first use)
@@ -2568,6 +2570,29 @@ int pg_adjoint_forward(pg_sim *s, const pg_step_args *a, pg_object *objects, int
         (rc = adj_alloc(s, (void **)&J.small, sizeof(double) * 16)))
         return rc;
     PG_CUDA(cudaMemcpyAsync(J.target, rho_target, sizeof(double) * nd, cudaMemcpyHostToDevice, s->stream));
+    if (s->n_obj > 0) {
+        // dphi/dV_k: the unit-potential Laplace solutions (the circuit's when
+        // it has them, else solved here; the charge is re-deposited by the
+        // first step)
+        if ((rc = adj_alloc(s, (void **)&J.lap, sizeof(double) * nd * (size_t)s->n_obj)) ||
+            (rc = adj_alloc(s, (void **)&J.gpot, sizeof(double) * (size_t)s->n_obj)))
+            return rc;
+        for (int k = 0; k < s->n_obj; ++k) {
+            if (s->lap) {
+                PG_CUDA(cudaMemcpyAsync(J.lap + (size_t)k * nd, s->lap + (size_t)k * nd, sizeof(double) * nd,
+                                        cudaMemcpyDeviceToDevice, s->stream));
+                continue;
+            }
+            std::vector<double> pot(s->n_obj, 0.0);
+            pot[k] = 1.0;
+            if ((rc = poisson_solve_internal(s, pot.data(), true, false, std::min(1e-13, s->cfg.pcg_rtol),
+                                             std::min(1e-15, s->cfg.pcg_atol), nullptr)))
+                return rc;
+            PG_CUDA(cudaMemcpyAsync(J.lap + (size_t)k * nd, s->phi, sizeof(double) * nd, cudaMemcpyDeviceToDevice,
+                                    s->stream));
+        }
+        s->phi_valid = false;
+    }
     int64_t live0 = 0, neg = 0, pos = 0;
     if ((rc = pg_num_particles(s, &live0, &neg, &pos))) return rc;
     std::vector<pg_object> obj = J.objects;
@@ -2626,6 +2651,7 @@ int pg_adjoint_backward(pg_sim *s, double *grad_v, int64_t n_out, double *grad_E
     const DevParticles &P = s->P[s->cur];
     PG_CUDA(cudaMemsetAsync(J.bar, 0, sizeof(double) * 6 * n, s->stream));
     PG_CUDA(cudaMemsetAsync(J.small, 0, sizeof(double) * 3, s->stream));
+    if (J.gpot) PG_CUDA(cudaMemsetAsync(J.gpot, 0, sizeof(double) * (size_t)s->n_obj, s->stream));
     // d loss / d x_K through rho_K (cells at step K); rhobar holds 2 (rho_K - target)
     launch_adj_deposit(s->dm, J.n, J.fin_c, P.sp, s->d_q, J.rhobar, xb, yb, zb, s->stream);
     std::vector<pg_object> obj = J.objects;
@@ -2654,6 +2680,8 @@ int pg_adjoint_backward(pg_sim *s, double *grad_v, int64_t n_out, double *grad_E
             launch_adj_move_push(J.n, cells, P.sp, J.small + 8, ak.dt, xb, yb, zb, vxb, vyb, vzb, J.Ebar, J.small,
                                  s->stream);
             launch_adj_field(s->dm, J.Ebar, J.phibar, s->stream);
+            for (int o = 0; o < s->n_obj && J.gpot; ++o)
+                launch_dot_accum(s->ndof, J.phibar, J.lap + (size_t)o * s->ndof, J.gpot + o, s->stream);
             if ((rc = adj_poisson(s))) break;
             launch_adj_deposit(s->dm, J.n, cells, P.sp, s->d_q, J.rhobar, xb, yb, zb, s->stream);
         }
@@ -2691,6 +2719,17 @@ int pg_adjoint_backward(pg_sim *s, double *grad_v, int64_t n_out, double *grad_E
     if (rc == PG_OK) rc = rc2;
     if (rc == PG_OK) rc = check_state(s);
     return rc;
+}
+
+int pg_adjoint_potential_gradient(pg_sim *s, double *grad_pot, int32_t n_objects) {
+    if (!s || (n_objects > 0 && !grad_pot)) return fail(PG_ERR_ARG, "pg_adjoint_potential_gradient: bad arguments");
+    if (!s->adj.ready) return fail(PG_ERR_STATE, "pg_adjoint_potential_gradient: call pg_adjoint_forward first");
+    if (n_objects != s->n_obj) return fail(PG_ERR_ARG, "pg_adjoint_potential_gradient: n_objects differs from the mesh's");
+    if (n_objects == 0) return PG_OK;
+    PG_CUDA(cudaMemcpyAsync(grad_pot, s->adj.gpot, sizeof(double) * (size_t)n_objects, cudaMemcpyDeviceToHost,
+                            s->stream));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    return PG_OK;
 }
 
 int pg_adjoint_release(pg_sim *s) {

@@ -115,6 +115,22 @@ __global__ void k_zero_dirichlet(int32_t n, const int32_t *__restrict__ bc_kind,
     if (i < n && bc_kind[i] >= 0) v[i] = 0.0;
 }
 
+// out += sum_i a_i b_i (block sums, one FP64 atomic per block)
+__global__ void k_dot_accum(int32_t n, const double *__restrict__ a, const double *__restrict__ b,
+                            double *__restrict__ out) {
+    __shared__ double sh[kThreads / 32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = i < n ? a[i] * b[i] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sh[k];
+        atomicAdd(out, s);
+    }
+}
+
 // rhobar = 2 (rho - target)
 __global__ void k_loss_grad(int32_t n, const double *__restrict__ rho, const double *__restrict__ target,
                             double *__restrict__ rhobar, double *__restrict__ loss) {
@@ -178,6 +194,10 @@ void launch_csr_matvec(int32_t n, const int32_t *row, const int32_t *col, const 
 void launch_zero_dirichlet(int32_t n, const int32_t *bc_kind, double *v, cudaStream_t st) {
     count_launches(1);
     k_zero_dirichlet<<<blocks(n), kThreads, 0, st>>>(n, bc_kind, v);
+}
+void launch_dot_accum(int32_t n, const double *a, const double *b, double *out, cudaStream_t st) {
+    count_launches(1);
+    k_dot_accum<<<blocks(n), kThreads, 0, st>>>(n, a, b, out);
 }
 void launch_loss_grad(int32_t n, const double *rho, const double *target, double *rhobar, double *loss,
                       cudaStream_t st) {

@@ -384,6 +384,7 @@ void launch_adj_field(const DevMesh &m, const double *Ebar, double *phibar, cuda
 void launch_csr_matvec(int32_t n, const int32_t *row, const int32_t *col, const double *val, const double *x,
                        double *y, cudaStream_t st);
 void launch_zero_dirichlet(int32_t n, const int32_t *bc_kind, double *v, cudaStream_t st);
+void launch_dot_accum(int32_t n, const double *a, const double *b, double *out, cudaStream_t st);
 void launch_loss_grad(int32_t n, const double *rho, const double *target, double *rhobar, double *loss,
                       cudaStream_t st);
 void launch_scatter_by_id(int64_t n, const int32_t *cell, const int64_t *pid, int64_t pid_base, int64_t n_out,

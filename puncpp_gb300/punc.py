@@ -554,6 +554,13 @@ def adjoint_backward(pop: Population, n_particles: int):
     return gv, ge, gx
 
 
+def adjoint_potential_gradient(pop: Population, n_objects: int) -> np.ndarray:
+    """After adjoint_backward: d loss / d (fixed potential of object k)."""
+    g = np.zeros(max(1, n_objects))
+    L.check(L.load().pg_adjoint_potential_gradient(pop.handle, L.dptr(g), n_objects))
+    return g[:n_objects]
+
+
 def stage_times(pop: Population) -> dict:
     lib = L.load()
     n = C.c_int32()

@@ -165,3 +165,47 @@ def test_adjoint_full_size(oracle_mod):
             raise AssertionError("no jump-free step found")
         fd = (lp - lm) / (2 * h)
         assert abs(gv[i, j] - fd) <= 1e-5 * np.abs(gv).max() + 1e-4 * abs(fd), (i, j, gv[i, j], fd)
+
+
+def test_adjoint_object_potential_gradient():
+    """Probe mesh with its object held at a fixed potential V (the object
+    bias): d loss / d V from the adjoint (sum over the steps of <phibar, L>,
+    L the unit-potential Laplace solution) against jump-free central
+    differences in V.  Slow particles away from the object and the box faces,
+    so that none is absorbed during the K steps."""
+    from helpers import uniform_points
+
+    ma = meshgen.probe_box(8, 2.0, 0.6)
+    mesh = punc.Mesh(ma)
+    rng = np.random.default_rng(11)
+    pts = uniform_points(ma, 4000, rng)
+    r = np.linalg.norm(pts, axis=1)
+    x = pts[(r > 0.9) & (np.abs(pts).max(axis=1) < 1.5)][:600]
+    v0 = rng.normal(0.0, 0.02, size=x.shape)
+    K, C, dt = 4, 2, 0.1
+    target = rng.normal(0.0, 1.0, size=mesh.n_dofs) * 0.05
+    state = {}
+
+    def loss(V):
+        if "pop" in state:
+            state["pop"].close()
+        pop = punc.Population(mesh, pcg_rtol=1e-13, pcg_atol=1e-30, pcg_max_iter=5000)
+        state["pop"] = pop
+        assert pop.add_particles(x, v0, -1.0 / len(x), 1.0 / len(x)) == len(x)
+        return punc.adjoint_forward(pop, [punc.Object(2, potential=V)], dt, K, C, target, first_step=True)
+
+    V0 = -0.5
+    base = loss(V0)
+    gv, ge, gx = punc.adjoint_backward(state["pop"], len(x))
+    gpot = punc.adjoint_potential_gradient(state["pop"], 1)
+    assert np.all(np.isfinite(gv)) and gpot.shape == (1,)
+    for h in (1e-6, 1e-7, 1e-8):
+        lp, lm = loss(V0 + h), loss(V0 - h)
+        dp, dm = (lp - base) / h, (base - lm) / h
+        if abs(dp - dm) <= 1e-3 * max(abs(dp), abs(dm), 1e-12):
+            break
+    else:
+        raise AssertionError("no jump-free step found")
+    fd = (lp - lm) / (2 * h)
+    assert abs(gpot[0] - fd) <= 1e-4 * abs(fd) + 1e-9, (gpot[0], fd)
+    state["pop"].close()
