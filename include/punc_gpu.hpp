@@ -17,6 +17,7 @@
 #ifndef PUNC_GPU_HPP
 #define PUNC_GPU_HPP
 
+#include <algorithm>
 #include <cstddef>
 #include <cstdio>
 #include <cstdlib>
@@ -350,6 +351,57 @@ inline std::size_t inject_particles(Population<3> &pop, const std::vector<Specie
     int64_t n = 0;
     check(pg_inject(pop.handle, dt, seed, step, &n));
     return (std::size_t)n;
+}
+
+// Extensions without a reference counterpart (the C ABI's pg_run_steps,
+// pg_autotune and pg_adjoint_*), with the shim's object conventions.
+
+// n_steps fused steps with the bookkeeping on the device, replaying a
+// captured CUDA graph per step when `graph`; one result per step.
+inline std::vector<pg_step_result> run_steps(Population<3> &pop, ObjectVector &objects, const pg_step_args &args,
+                                             int32_t n_steps, bool graph = true) {
+    auto v = detail::to_c(objects);
+    std::vector<pg_step_result> res((std::size_t)std::max<int32_t>(1, n_steps));
+    check(pg_run_steps(pop.handle, &args, v.data(), (int32_t)v.size(), n_steps, graph ? 1 : 0, res.data()));
+    detail::from_c(v, objects);
+    res.resize((std::size_t)std::max<int32_t>(0, n_steps));
+    return res;
+}
+
+// Launch configuration and cell-sort interval chosen from timed real steps
+// (the steps advance the simulation).
+inline pg_tuning autotune(Population<3> &pop, ObjectVector &objects, const pg_step_args &args,
+                          int32_t steps_per_trial = 2) {
+    auto v = detail::to_c(objects);
+    pg_tuning t{};
+    check(pg_autotune(pop.handle, &args, v.data(), (int32_t)v.size(), steps_per_trial, &t));
+    detail::from_c(v, objects);
+    return t;
+}
+
+// Adjoint of K fused FP64 steps: forward (returns ||rho_K - target||^2), then
+// the gradients with respect to the initial velocities and positions (by
+// particle id), the uniform field E0 and the objects' fixed potentials.
+struct AdjointGradients {
+    std::vector<double> v0, x0, potentials;
+    double E0[3] = {0, 0, 0};
+};
+inline double adjoint_forward(Population<3> &pop, ObjectVector &objects, const pg_step_args &args, int32_t n_steps,
+                              int32_t ckpt_every, const std::vector<double> &rho_target) {
+    auto v = detail::to_c(objects);
+    double loss = 0;
+    check(pg_adjoint_forward(pop.handle, &args, v.data(), (int32_t)v.size(), n_steps, ckpt_every, rho_target.data(),
+                             &loss));
+    return loss;
+}
+inline AdjointGradients adjoint_backward(Population<3> &pop, std::size_t n_particles, std::size_t n_objects) {
+    AdjointGradients g;
+    g.v0.assign(3 * n_particles, 0.0);
+    g.x0.assign(3 * n_particles, 0.0);
+    g.potentials.assign(n_objects, 0.0);
+    check(pg_adjoint_backward(pop.handle, g.v0.data(), (int64_t)n_particles, g.E0, g.x0.data()));
+    check(pg_adjoint_potential_gradient(pop.handle, g.potentials.data(), (int32_t)n_objects));
+    return g;
 }
 
 }  // namespace gpu

@@ -33,5 +33,11 @@ int main() {
         pop.update(objects, dt);
         std::printf("step %d KE %.6e particles %zu\n", n, KE, pop.num_of_particles());
     }
+    // the same loop body as fused steps replayed from a captured graph
+    pg_step_args args{};
+    args.dt = dt;
+    args.step = 3;
+    for (const pg_step_result &r : pg::run_steps(pop, objects, args, 2, true))
+        std::printf("fused KE %.6e particles %lld\n", r.KE, (long long)r.n_particles);
     return 0;
 }

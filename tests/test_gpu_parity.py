@@ -304,7 +304,8 @@ def test_fused_deposit_equals_distribute(lib, oracle_mod):
 
 
 def test_cpp_time_loop_runs(lib, tmp_path):
-    """The C++ front end (include/punc_gpu.hpp) drives three reference-shaped steps."""
+    """The C++ front end (include/punc_gpu.hpp) drives three reference-shaped
+    steps, then two fused steps replayed from a captured graph (run_steps)."""
     import subprocess
 
     from test_abi import build_cpp_time_loop
@@ -313,6 +314,8 @@ def test_cpp_time_loop_runs(lib, tmp_path):
     assert r.returncode == 0, r.stderr
     lines = [l for l in r.stdout.splitlines() if l.startswith("step")]
     assert len(lines) == 3 and all(l.endswith("particles 1") for l in lines)
+    fused = [l for l in r.stdout.splitlines() if l.startswith("fused")]
+    assert len(fused) == 2 and all(l.endswith("particles 1") for l in fused)
 
 
 def test_sort_keeps_the_particle_set(lib, oracle_mod):
