@@ -20,7 +20,10 @@
 // the facet's cell stays in the mesh.  Built with --fmad=false; exp is the
 // portable series, so accept/reject decisions equal a CPU evaluation.  Each
 // candidate is first decided in FP32 with an error bound (pg_screen.h); the
-// FP64 test runs only when the FP32 margin is inside the bound.
+// FP64 test runs only when the FP32 margin is inside the bound.  The FP64 form
+// forms the kept particle's velocity and position in FP64 (the oracle's bits);
+// the mixed form forms them in FP32 from the same random words (the top 24
+// bits of each uniform) and an FP32 copy of the facet.
 #include <cuda_runtime.h>
 
 #include <algorithm>

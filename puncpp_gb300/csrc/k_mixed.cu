@@ -1,12 +1,14 @@
-// Mixed-precision particle kernels: FP32 positions and velocities, FP32
-// push and move with fused multiply-adds, the FP32 facet walk with an FP64
-// re-test of facets the particle lies within the FP32 error bound of, and the
-// int64 fixed-point CG1 deposit (bitwise identical from run to run).
+// Mixed-precision particle kernels: FP32 positions and velocities, the DG0
+// field formed from the potential at the particle's cell, FP32 push and move
+// with fused multiply-adds, the FP32 facet walk (the sign of each barycentric
+// coordinate, with an FP64 re-test of facets the particle lies within the
+// FP32 error bound of), and the int64 fixed-point CG1 deposit (bitwise
+// identical from run to run) from the walk's last barycentric coordinates.
 //
 // Per particle a pass reads 24 B of FP32 position and velocity, 4 B of cell
 // id and 1 B of species, and writes back 28 B; per occupied cell it reads
-// 64 B of FP32 planes, 16 B of neighbours, 48 B of FP32 barycentric rows,
-// 16 B of dofs and 16 B of FP32 field.
+// the 64-byte cell record (FP32 barycentric rows, neighbours), 16 B of dofs
+// and four potentials, once per particle.
 #include <cuda_runtime.h>
 
 #include "pg_device.cuh"
