@@ -616,6 +616,16 @@ static int setup_amg(pg_sim *s, const std::vector<int32_t> &arow, const std::vec
                        (rc = dalloc(s, &M.y1, h.levels[1].A.n))))
             return rc;
     }
+    // the solver kernel takes each operator's value format from its role:
+    // binary16 for the preconditioner's transfer and coarse operators, FP32
+    // for A_0, G and the coarsest inverse
+    bool fmt = M.lev[0].A.val16 == nullptr;
+    for (int l = 1; l < L; ++l) fmt = fmt && M.lev[l].A.val16 != nullptr;
+    for (int l = 0; l + 1 < L; ++l) fmt = fmt && M.lev[l].ST.val16 != nullptr;
+    if (L >= 1) fmt = fmt && M.S0.val16 != nullptr && M.G.val16 == nullptr;
+    if (L >= 2) fmt = fmt && M.U1.val16 != nullptr;
+    if (L == 0) fmt = fmt && M.cinv.val16 == nullptr;
+    if (!fmt) return fail(PG_ERR_ARG, "AMG: operator value formats differ from the solver's");
     // operator bytes of one iteration: A_0 twice (A p and the level-0
     // smoother), then each operator of the cycle once
     auto opb = [](const SpOp &o, int64_t entries) {

@@ -223,17 +223,14 @@ __device__ __forceinline__ void apply_t(const SpOp &S, XV xv, PRE pre, EPI epi, 
     }
 }
 
-// epi(i, (S xv)_i, pre(i)) over the whole grid, in the operator's storage
-// form (uniform branch).
-template <class XV, class PRE, class EPI>
+// epi(i, (S xv)_i, pre(i)) over the whole grid.  V16: the operator's values
+// are binary16 (fixed per operator at upload: the preconditioner's transfer
+// and coarse operators; A_0, G and the coarsest inverse keep FP32, which the
+// set-up checks); the column width is chosen by a uniform branch.
+template <bool V16, class XV, class PRE, class EPI>
 __device__ __forceinline__ void apply(const SpOp &S, XV xv, PRE pre, EPI epi, int t0, int ts) {
-    if (S.col16) {
-        if (S.val16) apply_t<true, true>(S, xv, pre, epi, t0, ts);
-        else apply_t<true, false>(S, xv, pre, epi, t0, ts);
-    } else {
-        if (S.val16) apply_t<false, true>(S, xv, pre, epi, t0, ts);
-        else apply_t<false, false>(S, xv, pre, epi, t0, ts);
-    }
+    if (S.col16) apply_t<true, V16>(S, xv, pre, epi, t0, ts);
+    else apply_t<false, V16>(S, xv, pre, epi, t0, ts);
 }
 
 // Blocks that take one pass over S (kRows rows per thread or lane group,
@@ -288,11 +285,11 @@ struct ResGather {
 };
 
 // t = W x for level Lv: W = w D^-1 (2 I - A w D^-1), xg(j) the input vector.
-template <class XG>
+template <bool V16, class XG>
 __device__ __forceinline__ void smooth(const AmgLevelDev &Lv, XG xg, float *t, int t0, int ts) {
     const float om = Lv.omega;
     const float *dinv = Lv.dinv;
-    apply(Lv.A, [=](int j) { return om * __ldg(dinv + j) * xg(j); },
+    apply<V16>(Lv.A, [=](int j) { return om * __ldg(dinv + j) * xg(j); },
           [=](int i) { return make_float2(__ldg(dinv + i), xg(i)); },
           [=](int i, float s, float2 dx) { t[i] = om * dx.x * (2.0f * dx.y - s); }, t0, ts);
 }
@@ -334,15 +331,15 @@ __device__ double vcycle_phase0(const AmgDev &M, const PcgArgs &a, const float *
     const int L = M.nlev - 1;
     double rz = 0.0;
     if (L == 0) {
-        apply(M.cinv, gr, [=](int i) { return gr(i); },
+        apply<false>(M.cinv, gr, [=](int i) { return gr(i); },
               [&](int i, float s, float ri) { z[i] = s; rz = fma((double)s, (double)ri, rz); }, t0, ts);
     } else if (L == 1) {
         float *yL = M.yL;
-        apply(M.G, gr, NoPre{}, [=](int i, float s, int) { yL[i] = s; }, t0, ts);
-        smooth(M.lev[0], gr, M.lev[0].t, t0, ts);
+        apply<false>(M.G, gr, NoPre{}, [=](int i, float s, int) { yL[i] = s; }, t0, ts);
+        smooth<false>(M.lev[0], gr, M.lev[0].t, t0, ts);
     } else {
         float *b1 = M.lev[1].b;
-        apply(M.lev[0].ST, gr, NoPre{}, [=](int i, float s, int) { b1[i] = s; }, t0, ts);
+        apply<true>(M.lev[0].ST, gr, NoPre{}, [=](int i, float s, int) { b1[i] = s; }, t0, ts);
     }
     return rz;
 }
@@ -384,17 +381,17 @@ __device__ __forceinline__ double vcycle_rest(const AmgDev &M, const float *r, f
         if (mine(idx++)) {
             if (l < L - 1) {
                 float *bn = M.lev[l + 1].b;
-                apply(R, gb, NoPre{}, [=](int i, float s, int) { bn[i] = s; }, pt0, pts);
+                apply<true>(R, gb, NoPre{}, [=](int i, float s, int) { bn[i] = s; }, pt0, pts);
             } else {
                 float *yL = M.yL;
-                apply(R, gb, NoPre{}, [=](int i, float s, int) { yL[i] = s; }, pt0, pts);
+                apply<false>(R, gb, NoPre{}, [=](int i, float s, int) { yL[i] = s; }, pt0, pts);
             }
         }
-        if (l >= 2 && mine(idx++)) smooth(M.lev[l], gb, M.lev[l].t, pt0, pts);
-        if (l == 1 && mine(idx++)) smooth(M.lev[0], [=](int j) { return r[j]; }, M.lev[0].t, pt0, pts);
+        if (l >= 2 && mine(idx++)) smooth<true>(M.lev[l], gb, M.lev[l].t, pt0, pts);
+        if (l == 1 && mine(idx++)) smooth<false>(M.lev[0], [=](int j) { return r[j]; }, M.lev[0].t, pt0, pts);
         if (l == L - 1 && mine(idx++)) {
             const float *b1 = M.lev[1].b;
-            smooth(M.lev[1], [=](int j) { return b1[j]; }, M.lev[1].t, pt0, pts);
+            smooth<true>(M.lev[1], [=](int j) { return b1[j]; }, M.lev[1].t, pt0, pts);
         }
         grid.sync();
     }
@@ -402,14 +399,14 @@ __device__ __forceinline__ double vcycle_rest(const AmgDev &M, const float *r, f
     if (L >= 2) {
         const float *t1 = M.lev[1].t, *st = M.stack;
         float *y1 = M.y1;
-        apply(M.U1, [=](int j) { return st[j]; }, [=](int i) { return t1[i]; },
+        apply<true>(M.U1, [=](int j) { return st[j]; }, [=](int i) { return t1[i]; },
               [=](int i, float s, float ti) { y1[i] = ti + s; }, t0, ts);
         grid.sync();
         yup = M.y1;
     }
     const float *tz = M.lev[0].t;
     double rz = 0.0;
-    apply(M.S0, [=](int j) { return yup[j]; }, [=](int i) { return make_float2(tz[i], r[i]); },
+    apply<true>(M.S0, [=](int j) { return yup[j]; }, [=](int i) { return make_float2(tz[i], r[i]); },
           [&](int i, float s, float2 tr) {
               const float zi = tr.x + s;
               z[i] = zi;
@@ -534,7 +531,7 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M)
             {
                 const float *z = a.z32;
                 float *p = a.p32, *Ap = a.Ap32;
-                apply(A0, [=](int j) { return z[j]; }, [=](int i) { return make_float3(z[i], p[i], Ap[i]); },
+                apply<false>(A0, [=](int j) { return z[j]; }, [=](int i) { return make_float3(z[i], p[i], Ap[i]); },
                       [&](int i, float s, float3 zpa) {
                           const float pi = first ? zpa.x : fmaf(beta, zpa.y, zpa.x);
                           const float api = first ? s : fmaf(beta, zpa.z, s);
