@@ -2447,7 +2447,7 @@ int pg_autotune(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_
     for (int th : threads)
         for (int b : bps)
             for (int agg = 0; agg <= (is_mixed(s) ? 1 : 0); ++agg) {
-                pg_tuning t{th, b, agg, 0};
+                pg_tuning t{th, b, agg, 0, 0.0, 0.0};
                 if ((rc = pg_set_tuning(s, &t))) goto done;
                 if ((rc = do_sort(s))) goto done;
                 double ms = 0;
