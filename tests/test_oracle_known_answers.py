@@ -6,7 +6,6 @@ demo/langmuir, demo/injection, test/test.py), regenerated on the synthetic
 meshes.  They pin the oracle's physics; the GPU tests then pin the engine to
 the oracle."""
 import numpy as np
-import pytest
 
 from puncpp_gb300 import meshgen
 from helpers import langmuir_load
