@@ -48,6 +48,16 @@ def union(meshes):
     return u, {"vertex": np.array(v_off), "cell": np.array(c_off), "object": np.array(o_off)}
 
 
+def facet_runs(mesh, cell_off):
+    """Run and run-local index of each exterior facet of the union mesh, in
+    the engine's facet order (a facet belongs to the run of its cell)."""
+    ext = mesh.table(L.T_EXT_FACETS).reshape(-1, 14)
+    cell = ext[:, 13].astype(np.int64)
+    run = np.searchsorted(cell_off, cell, side="right") - 1
+    first = np.searchsorted(run, np.arange(len(cell_off) - 1), side="left")
+    return run, (np.arange(len(cell)) - first[run]).astype(np.uint32)
+
+
 class Batch:
     """R runs in one engine.  Object k of run r is object o_off[r] + k of the
     batch (boundary tag 2 + o_off[r] + k)."""
@@ -57,13 +67,7 @@ class Batch:
         self.union, self.off = union(self.meshes)
         self.mesh = punc.Mesh(self.union)
         self.pop = punc.Population(self.mesh, **population_kwargs)
-        # run of each exterior facet, from the facet's cell (engine facet order)
-        ext = self.mesh.table(L.T_EXT_FACETS).reshape(-1, 14)
-        cell = ext[:, 13].astype(np.int64)
-        run = np.searchsorted(self.off["cell"], cell, side="right") - 1
-        first = np.searchsorted(run, np.arange(len(self.meshes)), side="left")
-        self.facet_run = run
-        self.facet_local = (np.arange(len(cell)) - first[run]).astype(np.uint32)
+        self.facet_run, self.facet_local = facet_runs(self.mesh, self.off["cell"])
         self.n_runs = len(self.meshes)
 
     def add_particles(self, r: int, xs, vs, q: float, m: float) -> int:
