@@ -51,3 +51,42 @@ def test_periodic_box_identifies_opposite_faces(tmp_path):
     # the same vertex classes as the generator's periodic map
     pairs = {(int(a), int(b)) for a, b in zip(ma.vertex_to_dof, mb.vertex_to_dof)}
     assert len(pairs) == ma.n_dofs
+
+
+def test_only_xml_meshes_are_read(tmp_path):
+    with pytest.raises(ValueError, match="only DOLFIN .xml"):
+        dolfin_xml.read_mesh(tmp_path / "m.h5")
+
+
+def test_non_tetrahedral_cells_are_refused(tmp_path):
+    ma = meshgen.probe_box(3, 2.0, 0.6)
+    fname = tmp_path / "m.xml"
+    dolfin_xml.write_mesh(fname, ma)
+    text = fname.read_text()
+    assert 'celltype="tetrahedron"' in text
+    fname.write_text(text.replace('celltype="tetrahedron"', 'celltype="triangle"'))
+    with pytest.raises(ValueError, match="only tetrahedra"):
+        dolfin_xml.read_mesh(fname)
+
+
+def test_facet_tags_of_another_dimension_are_refused(tmp_path):
+    ma = meshgen.probe_box(3, 2.0, 0.6)
+    fname = tmp_path / "m.xml"
+    dolfin_xml.write_mesh(fname, ma)
+    region = tmp_path / "m_facet_region.xml"
+    text = region.read_text()
+    assert 'dim="2"' in text
+    region.write_text(text.replace('dim="2"', 'dim="1"'))
+    with pytest.raises(ValueError, match="dim 2"):
+        dolfin_xml.read_mesh(fname)
+
+
+def test_missing_cells_are_an_error(tmp_path):
+    ma = meshgen.probe_box(3, 2.0, 0.6)
+    fname = tmp_path / "m.xml"
+    dolfin_xml.write_mesh(fname, ma)
+    lines = fname.read_text().split("\n")
+    k = next(i for i, l in enumerate(lines) if "<tetrahedron " in l)
+    fname.write_text("\n".join(lines[:k] + lines[k + 1:]))
+    with pytest.raises(ValueError, match="missing vertices or cells"):
+        dolfin_xml.read_mesh(fname)
