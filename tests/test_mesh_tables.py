@@ -120,3 +120,39 @@ def test_repeated_vertex_is_a_mesh_error(lib):
     ma.cells[0, 1] = ma.cells[0, 0]
     with pytest.raises(L.PgError):
         punc.Mesh(ma)
+
+
+def _interior_cell(ma):
+    """A cell none of whose facets is a boundary facet."""
+    bnd = {tuple(f) for f in np.sort(ma.bfacets, axis=1).tolist()}
+    for c, cell in enumerate(ma.cells):
+        faces = [tuple(sorted(int(v) for k, v in enumerate(cell) if k != i)) for i in range(4)]
+        if not any(f in bnd for f in faces):
+            return c
+    raise AssertionError("no interior cell")
+
+
+def test_facet_shared_by_three_cells_is_a_mesh_error(lib):
+    ma = meshgen.probe_box(4, 1.0, 0.3)
+    c = _interior_cell(ma)
+    ma.cells = np.ascontiguousarray(np.concatenate([ma.cells, ma.cells[c:c + 1]]))
+    with pytest.raises(L.PgError, match="shared by more than two cells") as e:
+        punc.Mesh(ma)
+    assert e.value.code == 3
+
+
+@pytest.mark.parametrize("what", ["cell_vertex", "facet_vertex", "tag"])
+def test_out_of_range_inputs_are_mesh_errors(what, lib):
+    ma = meshgen.probe_box(4, 1.0, 0.3)
+    if what == "cell_vertex":
+        ma.cells = ma.cells.copy()
+        ma.cells[3, 2] = ma.n_vertices
+    elif what == "facet_vertex":
+        ma.bfacets = ma.bfacets.copy()
+        ma.bfacets[0, 1] = -1
+    else:
+        ma.btags = ma.btags.copy()
+        ma.btags[0] = 0
+    with pytest.raises(L.PgError) as e:
+        punc.Mesh(ma)
+    assert e.value.code == 3
