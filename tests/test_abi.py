@@ -82,3 +82,23 @@ def test_errors_are_status_codes_not_aborts(lib):
     assert b"empty" in lib.pg_last_error()
     assert lib.pg_mesh_array(None, 0, None, None) == 1
     assert _lib.STATUS_NAMES[lib.pg_philox4x32_10(None, None, None)] == "PG_ERR_ARG"
+
+
+def test_every_handle_entry_point_refuses_a_null_handle(lib):
+    """Each entry point that takes an engine handle returns PG_ERR_ARG for a
+    NULL handle before it touches the device (no GPU needed)."""
+    from puncpp_gb300 import _lib
+    scalars = (C.c_int64, C.c_int32, C.c_double, C.c_uint64, C.c_uint32, C.c_int)
+    skip = {"pg_mesh_build", "pg_mesh_array", "pg_mesh_free", "pg_destroy"}
+    checked = 0
+    for name, (args, res) in _lib.SIGNATURES.items():
+        if name in skip or not args or args[0] is not C.c_void_p:
+            continue
+        call = [0 if a in scalars else None for a in args]
+        if res is C.c_int:
+            assert getattr(lib, name)(*call) == 1, name
+        else:
+            assert getattr(lib, name)(*call) is None, name   # pg_stage_name
+        checked += 1
+    assert checked >= 40
+    assert lib.pg_destroy(None) == 0
