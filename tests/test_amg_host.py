@@ -272,3 +272,38 @@ def test_periodic_constant_null_space(amgd, oracle_mod):
     b -= b.mean()
     x, it = pcg(A, b, lambda r: vcycle(levels, cinv, r), 1e-10)
     assert it < 25
+
+
+def test_hierarchy_is_deterministic(amgd, probe):
+    """Two set-ups of the same matrix give identical operators, so a run's
+    solver iterations and potentials are reproducible."""
+    ma, A = probe
+    c1, c2 = {}, {}
+    l1, i1 = hierarchy(amgd, A, cycle=c1)
+    l2, i2 = hierarchy(amgd, A, cycle=c2)
+    assert len(l1) == len(l2)
+    for a, b in zip(l1, l2):
+        for k in ("A", "P", "S", "ST"):
+            if k in a:
+                assert (a[k] != b[k]).nnz == 0
+        assert a["omega"] == b["omega"]
+    assert np.array_equal(i1, i2)
+    for k in ("G", "U1"):
+        if c1[k] is not None:
+            assert (c1[k] != c2[k]).nnz == 0
+
+
+@pytest.mark.parametrize("coarse_max", [400, 10])
+def test_collapsed_preconditioner_is_symmetric_positive_definite(coarse_max, amgd, probe22):
+    """CG needs a symmetric positive definite preconditioner: x.By = y.Bx and
+    x.Bx > 0 for the cycle the device applies."""
+    ma, A = probe22
+    cyc = {}
+    levels, cinv = hierarchy(amgd, A, coarse_max=coarse_max, cycle=cyc)
+    rng = np.random.default_rng(11)
+    B = lambda v: vcycle_collapsed(levels, cinv, cyc, v)
+    for _ in range(8):
+        x, y = rng.standard_normal(A.shape[0]), rng.standard_normal(A.shape[0])
+        bx, by = B(x), B(y)
+        assert abs(x @ by - y @ bx) <= 1e-11 * np.linalg.norm(x) * np.linalg.norm(by)
+        assert x @ bx > 0.0
