@@ -78,3 +78,37 @@ def test_injection_streams_depend_only_on_seed_and_step(oracle_mod):
     for k in ("x", "v", "cell"):
         np.testing.assert_array_equal(runs[0][k], runs[1][k])
     assert len(runs[0]["q"]) != len(runs[2]["q"]) or not np.array_equal(runs[0]["x"], runs[2]["x"])
+
+
+def test_empty_population_passes_every_stage(oracle_mod):
+    ma = meshgen.probe_box(4, 2.0, 0.6)
+    o = oracle_mod.Oracle(ma)
+    assert o.add_particles(np.zeros((0, 3)), np.zeros((0, 3)), -1.0, 1.0) == 0
+    E = o.efield(np.zeros(o.ndof))
+    o.boris(E, np.array([0.0, 0.0, 1.0]), 0.1)
+    o.move(0.1)
+    objects = [dict(bnd_id=2, charge=0.0, current=0.0, potential=0.0)]
+    assert o.update(objects, 0.1).sum() == 0
+    assert objects[0]["charge"] == 0.0 and objects[0]["current"] == 0.0
+    assert not o.distribute_cg1().any()
+    assert o.kinetic_energy() == 0.0 and o.num_particles() == 0
+
+
+def test_periodic_move_wraps_into_the_box(oracle_mod):
+    ma = meshgen.langmuir_cube(4)
+    o = oracle_mod.Oracle(ma)
+    Ld = np.asarray(ma.Ld, float)
+    rng = np.random.default_rng(4)
+    xs = rng.uniform(0.0, 1.0, (500, 3)) * Ld
+    vs = rng.normal(0.0, 3.0, (500, 3)) * Ld
+    o.add_particles(xs, vs, -1.0, 1.0)
+    p0 = o.particles()
+    o.move(0.7, Ld=Ld)
+    p1 = o.particles(sort=False)
+    order = np.argsort(p1["id"])
+    x1 = p1["x"][order]
+    x0 = p0["x"][np.argsort(p0["id"])] + 0.7 * p0["v"][np.argsort(p0["id"])]
+    assert np.all((x1 >= 0.0) & (x1 < Ld))
+    # the wrapped position differs from the free flight by whole box lengths
+    k = (x0 - x1) / Ld
+    np.testing.assert_allclose(k, np.round(k), atol=1e-9)
