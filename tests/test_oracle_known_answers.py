@@ -174,3 +174,29 @@ def test_esolver_projects_a_uniform_field_exactly(oracle_mod):
         ke2 = o2.boris(Ec, (0.1, 0.0, 0.3), 0.05)
         assert abs(ke1 - ke2) <= 1e-13 * abs(ke2)
         np.testing.assert_allclose(o.particles()["v"], o2.particles()["v"], rtol=0, atol=1e-14)
+
+
+def test_drifting_maxwellian_flux_count(oracle_mod):
+    # the flux of a drifting Maxwellian through a face whose inward normal
+    # carries the drift component u: n (vth/sqrt(2 pi) exp(-u^2/2vth^2)
+    # + u/2 (1 + erf(u/(sqrt(2) vth)))), summed over the box's six faces
+    from math import erf
+    ma = meshgen.kuhn_box(6, -3.0, 3.0)
+    o = oracle_mod.Oracle(ma)
+    n_dens, vth, vd, dt = 30.0, 1.0, 0.8, 0.05
+    o.create_flux([dict(q=-1.0, m=1.0, n=n_dens, vth=vth, vd=(vd, 0.0, 0.0))])
+
+    def flux(u):
+        return n_dens * (vth / np.sqrt(2 * np.pi) * np.exp(-u * u / (2 * vth * vth))
+                         + 0.5 * u * (1.0 + erf(u / (np.sqrt(2.0) * vth))))
+
+    area = 36.0
+    expect_per_step = area * dt * (flux(vd) + flux(-vd) + 4 * flux(0.0))
+    steps = 200
+    total = sum(o.inject(dt, 4321, s)[0] for s in range(steps))
+    mean = total / steps
+    assert abs(mean - expect_per_step) < 4 * np.sqrt(expect_per_step / steps)
+    # the injected velocities carry the drift: mean v_x exceeds the
+    # zero-drift value, and v_y, v_z stay centred
+    v = o.particles()["v"]
+    assert v[:, 0].mean() > 0.3 and abs(v[:, 1].mean()) < 4 * vth / np.sqrt(len(v))
