@@ -200,3 +200,25 @@ def test_drifting_maxwellian_flux_count(oracle_mod):
     # zero-drift value, and v_y, v_z stay centred
     v = o.particles()["v"]
     assert v[:, 0].mean() > 0.3 and abs(v[:, 1].mean()) < 4 * vth / np.sqrt(len(v))
+
+
+def test_boris_e_cross_b_drift(oracle_mod):
+    # uniform E perpendicular to B: the gyro-averaged velocity is the drift
+    # E x B / B^2 for either charge sign (demo/boris with an electric field)
+    ma = meshgen.kuhn_box(4, -500.0, 500.0)
+    E0, B = np.array([0.1, 0.0, 0.0]), np.array([0.0, 0.0, 1.0])
+    drift = np.cross(E0, B) / (B @ B)
+    for q in (-1.0, 1.0):
+        o = oracle_mod.Oracle(ma)
+        o.add_particles(np.zeros((1, 3)), np.array([[0.5, 0.0, 0.0]]), q, 1.0)
+        E = np.tile(E0, (o.nc, 1))
+        dt, steps = 0.05, 4000
+        vs = []
+        for _ in range(steps):
+            o.boris(E, B, dt)
+            vs.append(o.particles()["v"][0].copy())
+        # average over a whole number of gyro-periods (omega_c = 1)
+        per = int(round(2 * np.pi / dt))
+        k = (steps // per) * per
+        v_mean = np.mean(vs[:k], axis=0)
+        np.testing.assert_allclose(v_mean, drift, atol=3e-3)
