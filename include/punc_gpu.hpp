@@ -18,6 +18,7 @@
 #define PUNC_GPU_HPP
 
 #include <algorithm>
+#include <cmath>
 #include <cstddef>
 #include <cstdio>
 #include <cstdlib>
@@ -63,6 +64,22 @@ public:
     ~Mesh() { pg_mesh_free(handle); }
     Mesh(const Mesh &) = delete;
     Mesh &operator=(const Mesh &) = delete;
+    std::size_t num_cells() const {
+        const void *p = nullptr;
+        int64_t n = 0;
+        check(pg_mesh_array(handle, PG_T_VOLUME, &p, &n));
+        return (std::size_t)n;
+    }
+    // Mesh::volume (punc/src/mesh.cpp:147-170): cell volumes summed in cell order.
+    double volume() const {
+        const void *p = nullptr;
+        int64_t n = 0;
+        check(pg_mesh_array(handle, PG_T_VOLUME, &p, &n));
+        const double *v = static_cast<const double *>(p);
+        double s = 0.0;
+        for (int64_t c = 0; c < n; ++c) s += v[c];
+        return s;
+    }
     pg_mesh *handle = nullptr;
     double eps0;
 };
@@ -83,12 +100,65 @@ struct ISource { int node_a, node_b; double value; };
 using VSourceVector = std::vector<VSource>;
 using ISourceVector = std::vector<ISource>;
 
-// Maxwellian species of simulation particles (punc/src/population.cpp:41-70).
+// Maxwellian species of simulation particles (punc/src/population.cpp:41-70):
+// q, m and n of a simulation particle and the velocity distribution; weight,
+// num and debye as make_species derives them.
 struct Species {
     double q, m, n, vth;
     double vd[3] = {0, 0, 0};
     double vdf_range = 5.0;
+    double weight = 1.0;      // physical particles per simulation particle
+    std::size_t num = 0;      // initial number of simulation particles
+    double debye = 0.0;       // Debye length
 };
+
+// How the amount of simulation particles is given (punc/include/punc/population.h:50-55).
+enum class ParticleAmountType { in_total, per_cell, per_volume, phys_per_sim };
+
+// Species::Species (punc/src/population.cpp:41-70) with a Maxwellian velocity
+// distribution of thermal speed vth and drift vd (Maxwellian::debye,
+// punc/src/distributions.cpp:74-77); eps0 = 0 takes the mesh's.  The amount
+// becomes physical particles per simulation particle through the reference's
+// chain per cell -> in total -> per volume -> weight.
+inline Species make_species(double charge, double mass, double density, double amount, ParticleAmountType type,
+                            const Mesh &mesh, double vth, const double *vd = nullptr, double vdf_range = 5.0,
+                            double eps0 = 0.0) {
+    const double volume = mesh.volume();
+    switch (type) {
+    case ParticleAmountType::per_cell:
+        amount *= (double)mesh.num_cells();
+        [[fallthrough]];
+    case ParticleAmountType::in_total:
+        amount /= volume;
+        [[fallthrough]];
+    case ParticleAmountType::per_volume:
+        amount = density / amount;
+        [[fallthrough]];
+    case ParticleAmountType::phys_per_sim:
+        break;
+    default:
+        throw Error(PG_ERR_ARG, "make_species: invalid ParticleAmountType");
+    }
+    Species s{charge * amount, mass * amount, density / amount, vth};
+    if (vd)
+        for (int k = 0; k < 3; ++k) s.vd[k] = vd[k];
+    s.vdf_range = vdf_range;
+    s.weight = amount;
+    s.num = (std::size_t)(s.n * volume);
+    const double e0 = eps0 != 0.0 ? eps0 : mesh.eps0;
+    s.debye = std::sqrt(e0 * s.m / (s.n * s.q * s.q)) * vth;
+    return s;
+}
+
+// min_plasma_period (punc/src/population.cpp:72-80).
+inline double min_plasma_period(const std::vector<Species> &species, double eps0) {
+    double wp_max = 0;
+    for (auto &s : species) {
+        const double wp = std::sqrt(s.q * s.q * s.n / (eps0 * s.m));
+        if (wp > wp_max) wp_max = wp;
+    }
+    return 2 * 3.14159265358979323846 / wp_max;
+}
 
 namespace detail {
 inline std::vector<pg_object> to_c(const ObjectVector &objs) {

@@ -18,6 +18,8 @@ download on .vector().
 from __future__ import annotations
 
 import ctypes as C
+import enum
+import math
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -68,6 +70,16 @@ class Mesh:
     def n_dofs(self) -> int:
         return int(self.arrays.n_dofs)
 
+    @property
+    def num_cells(self) -> int:
+        return int(self.arrays.n_cells)
+
+    def volume(self) -> float:
+        """Mesh::volume (punc/src/mesh.cpp:147-170): the cell volumes summed in
+        cell order, as the assembly of the form 1 dx accumulates them."""
+        vol = self.table(L.T_VOLUME)
+        return float(np.cumsum(vol)[-1]) if len(vol) else 0.0
+
     def __del__(self):
         h = getattr(self, "handle", None)
         if h:
@@ -102,15 +114,64 @@ def _objects_out(arr, objects):
         o.charge, o.current, o.potential = arr[k].charge, arr[k].current, arr[k].potential
 
 
+class ParticleAmountType(enum.IntEnum):
+    """How the amount of simulation particles is given to Species.from_physical
+    (punc/include/punc/population.h:50-55)."""
+    in_total = 0       # total number of simulation particles
+    per_cell = 1       # simulation particles per cell
+    per_volume = 2     # simulation particles per volume
+    phys_per_sim = 3   # physical particles per simulation particle
+
+
 @dataclass
 class Species:
-    """Maxwellian species of simulation particles (punc/src/population.cpp:41-70)."""
+    """Maxwellian species of simulation particles (punc/src/population.cpp:41-70):
+    q, m and n of a simulation particle, the velocity distribution's vth, drift
+    and range; weight (physical particles per simulation particle), num (the
+    initial number of simulation particles) and debye (the Debye length) as
+    the reference's constructor derives them in from_physical."""
     q: float
     m: float
     n: float = 0.0
     vth: float = 0.0
     vd: tuple = (0.0, 0.0, 0.0)
     vdf_range: float = 5.0
+    weight: float = 1.0
+    num: int = 0
+    debye: float = 0.0
+
+    @classmethod
+    def from_physical(cls, charge: float, mass: float, density: float, amount: float, amount_type, mesh: Mesh,
+                      vth: float = 0.0, vd=(0.0, 0.0, 0.0), vdf_range: float = 5.0, eps0: float | None = None):
+        """Species::Species (punc/src/population.cpp:41-70) with a Maxwellian
+        velocity distribution (Maxwellian::debye, punc/src/distributions.cpp:74-77):
+        the amount becomes physical particles per simulation particle by the
+        reference's chain of steps (per cell -> in total -> per volume -> weight),
+        and the physical charge, mass and density scale by it."""
+        t = ParticleAmountType(amount_type)
+        volume = mesh.volume()
+        a = float(amount)
+        if t == ParticleAmountType.per_cell:
+            a *= mesh.num_cells
+        if t in (ParticleAmountType.per_cell, ParticleAmountType.in_total):
+            a /= volume
+        if t != ParticleAmountType.phys_per_sim:
+            a = density / a
+        q, m, n = charge * a, mass * a, density / a
+        e0 = mesh.eps0 if eps0 is None else eps0
+        return cls(q, m, n=n, vth=vth, vd=tuple(vd), vdf_range=vdf_range, weight=a, num=int(n * volume),
+                   debye=math.sqrt(e0 * m / (n * q * q)) * vth)
+
+
+def min_plasma_period(species, eps0: float) -> float:
+    """min_plasma_period (punc/src/population.cpp:72-80): 2 pi over the largest
+    plasma frequency sqrt(q^2 n / (eps0 m)) of the species."""
+    wp_max = 0.0
+    for s in species:
+        wp = math.sqrt(s.q * s.q * s.n / (eps0 * s.m))
+        if wp > wp_max:
+            wp_max = wp
+    return 2 * math.pi / wp_max
 
 
 class Population:

@@ -1,0 +1,42 @@
+// Species weights of the C++ front end (include/punc_gpu.hpp make_species,
+// min_plasma_period) on a mesh read from raw arrays; prints one line per
+// amount type: weight q m n num debye, then the plasma period, all %.17g.
+// Host only: building the mesh tables needs no GPU.
+#include <cstdint>
+#include <cstdio>
+#include <vector>
+
+#include "punc_gpu.hpp"
+
+template <class T>
+static std::vector<T> read_all(const char *path) {
+    std::vector<T> v;
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return v;
+    T x;
+    while (std::fread(&x, sizeof(T), 1, f) == 1) v.push_back(x);
+    std::fclose(f);
+    return v;
+}
+
+int main(int argc, char **argv) {
+    if (argc < 5) return 2;
+    const auto coords = read_all<double>(argv[1]);
+    const auto cells = read_all<int64_t>(argv[2]);
+    const auto bf = read_all<int64_t>(argv[3]);
+    const auto bt = read_all<int32_t>(argv[4]);
+    punc::gpu::Mesh mesh(coords, cells, bf, bt, 1.0);
+    using T = punc::gpu::ParticleAmountType;
+    const T types[] = {T::in_total, T::per_cell, T::per_volume, T::phys_per_sim};
+    const double amounts[] = {20000.0, 16.0, 40.0, 3.0};
+    const double vd[3] = {0.5, 0.0, -0.25};
+    std::vector<punc::gpu::Species> all;
+    for (int k = 0; k < 4; ++k) {
+        const auto s = punc::gpu::make_species(-1.0, 1.0, 100.0, amounts[k], types[k], mesh, 1.0, vd);
+        std::printf("%.17g %.17g %.17g %.17g %zu %.17g\n", s.weight, s.q, s.m, s.n, s.num, s.debye);
+        all.push_back(s);
+        all.push_back(punc::gpu::make_species(1.0, 1836.0, 100.0, amounts[k], types[k], mesh, 0.05));
+    }
+    std::printf("%.17g %.17g\n", punc::gpu::min_plasma_period(all, 1.0), mesh.volume());
+    return 0;
+}
