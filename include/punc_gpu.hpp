@@ -270,6 +270,19 @@ inline void move(Population<3> &pop, double dt) { check(pg_move(pop.handle, dt))
 inline void move_periodic(Population<3> &pop, double dt, const std::vector<double> &Ld) {
     check(pg_move_periodic(pop.handle, dt, Ld.data()));
 }
+// element_volume (punc/src/distributor.cpp:35-69): per dof, (d + 1) over the
+// volume of its cells (voronoi) or one over that volume; the engine keeps the
+// first as a mesh table, and the second is it divided by 4 (exact).
+inline std::vector<double> element_volume(const Mesh &mesh, bool voronoi = true) {
+    const void *p = nullptr;
+    int64_t n = 0;
+    check(pg_mesh_array(mesh.handle, PG_T_DV_INV, &p, &n));
+    const double *dv = static_cast<const double *>(p);
+    std::vector<double> out(dv, dv + n);
+    if (!voronoi)
+        for (auto &x : out) x /= 4.0;
+    return out;
+}
 // distributor.h:168-210; dv_inv is the engine's own element_volume table.
 inline void distribute_cg1(Population<3> &pop, Function &, const std::vector<double> &) {
     check(pg_distribute_cg1(pop.handle, nullptr));

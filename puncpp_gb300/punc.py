@@ -350,6 +350,14 @@ def move_periodic(pop: Population, dt: float, Ld):
     L.check(L.load().pg_move_periodic(pop.handle, dt, L.dptr(Ld)))
 
 
+def element_volume(mesh: Mesh, voronoi: bool = True) -> np.ndarray:
+    """element_volume (punc/src/distributor.cpp:35-69): per dof, (d + 1) over
+    the volume of its cells (voronoi) or one over that volume.  The engine
+    keeps the first as a mesh table; the second is it divided by 4 (exact)."""
+    dv = mesh.table(L.T_DV_INV)
+    return dv if voronoi else dv / 4.0
+
+
 def distribute_cg1(pop: Population, rho: Function | None = None, dv_inv=None) -> np.ndarray:
     """distribute_cg1 (punc/include/punc/distributor.h:168-210); dv_inv is the
     engine's element_volume table, so the argument is accepted and unused."""

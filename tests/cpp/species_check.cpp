@@ -1,6 +1,7 @@
 // Species weights of the C++ front end (include/punc_gpu.hpp make_species,
 // min_plasma_period) on a mesh read from raw arrays; prints one line per
-// amount type: weight q m n num debye, then the plasma period, all %.17g.
+// amount type: weight q m n num debye, then the plasma period and the mesh
+// volume, then the sums of element_volume with and without voronoi, all %.17g.
 // Host only: building the mesh tables needs no GPU.
 #include <cstdint>
 #include <cstdio>
@@ -38,5 +39,9 @@ int main(int argc, char **argv) {
         all.push_back(punc::gpu::make_species(1.0, 1836.0, 100.0, amounts[k], types[k], mesh, 0.05));
     }
     std::printf("%.17g %.17g\n", punc::gpu::min_plasma_period(all, 1.0), mesh.volume());
+    const auto dv = punc::gpu::element_volume(mesh, true), dv1 = punc::gpu::element_volume(mesh, false);
+    double s_dv = 0.0, s_dv1 = 0.0;
+    for (std::size_t k = 0; k < dv.size(); ++k) { s_dv += dv[k]; s_dv1 += dv1[k]; }
+    std::printf("%.17g %.17g\n", s_dv, s_dv1);
     return 0;
 }

@@ -77,7 +77,7 @@ def test_cpp_front_end_agrees_bitwise(lib, box, tmp_path):
     out = subprocess.run([str(exe)] + files, capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stderr
     lines = out.stdout.strip().split("\n")
-    assert len(lines) == 5
+    assert len(lines) == 6
     species = []
     for line, kind in zip(lines, [T.in_total, T.per_cell, T.per_volume, T.phys_per_sim]):
         w, q, m, n, num, debye = line.split()
@@ -88,3 +88,21 @@ def test_cpp_front_end_agrees_bitwise(lib, box, tmp_path):
     period, volume = (float(x) for x in lines[4].split())
     assert volume == mesh.volume()
     assert period == punc.min_plasma_period(species, 1.0)
+    s_dv, s_dv1 = (float(x) for x in lines[5].split())
+    assert s_dv == float(np.cumsum(punc.element_volume(mesh, True))[-1])
+    assert s_dv1 == float(np.cumsum(punc.element_volume(mesh, False))[-1])
+
+
+@pytest.mark.parametrize("voronoi", [True, False])
+def test_element_volume(voronoi, lib, box):
+    """element_volume (punc/src/distributor.cpp:35-69) from the cell volumes:
+    each dof's patch is the cells around its vertex."""
+    ma, mesh = box
+    vol = mesh.table(punc.L.T_VOLUME)
+    patch = np.zeros(mesh.n_dofs)
+    for k in range(4):
+        np.add.at(patch, ma.cells[:, k], vol)
+    dv = punc.element_volume(mesh, voronoi)
+    np.testing.assert_allclose(dv, (4.0 if voronoi else 1.0) / patch, rtol=1e-13)
+    # the patches cover the mesh four times
+    assert np.sum((4.0 if voronoi else 1.0) / dv) == pytest.approx(4 * mesh.volume(), rel=1e-13)
