@@ -175,6 +175,23 @@ inline void from_c(const std::vector<pg_object> &v, ObjectVector &objs) {
 }
 }  // namespace detail
 
+// Particle<len> (punc/include/punc/population.h:74-94): the 64-byte record
+// {x, v, q, m} of a particle.
+template <std::size_t len = 3>
+struct Particle {
+    double x[len];
+    double v[len];
+    double q;
+    double m;
+    Particle(const double *x_, const double *v_, double q_, double m_) : q(q_), m(m_) {
+        for (std::size_t i = 0; i < len; ++i) {
+            x[i] = x_[i];
+            v[i] = v_[i];
+        }
+    }
+    Particle() {}
+};
+
 template <std::size_t len> class Population;
 
 // Population<3> (punc/include/punc/population.h:236-308) on the device.
@@ -191,6 +208,26 @@ public:
     void add_particles(const std::vector<double> &xs, const std::vector<double> &vs, double q, double m) {
         int64_t added = 0;
         check(pg_add_particles(handle, xs.data(), vs.data(), (int64_t)(xs.size() / 3), q, m, &added));
+    }
+    // add_particles(const std::vector<Particle<len>> &) (population.h:437-446):
+    // records outside the mesh are dropped; each run of consecutive records
+    // with the same charge and mass goes in one call, so the engine's particle
+    // ids follow the input order as the reference's cell vectors do.
+    void add_particles(const std::vector<Particle<3>> &ps) {
+        std::vector<double> xs, vs;
+        std::size_t i = 0;
+        while (i < ps.size()) {
+            std::size_t j = i;
+            xs.clear();
+            vs.clear();
+            while (j < ps.size() && ps[j].q == ps[i].q && ps[j].m == ps[i].m) {
+                xs.insert(xs.end(), ps[j].x, ps[j].x + 3);
+                vs.insert(vs.end(), ps[j].v, ps[j].v + 3);
+                ++j;
+            }
+            add_particles(xs, vs, ps[i].q, ps[i].m);
+            i = j;
+        }
     }
     signed long int locate(const double *p) {
         int64_t c = -1;

@@ -20,6 +20,15 @@ static std::vector<T> read_all(const char *path) {
     return v;
 }
 
+// Compiled, not run (it needs a GPU): the Particle<3> overload of
+// add_particles type-checks against the reference's record.
+[[maybe_unused]] static void add_records(punc::gpu::Population<3> &pop) {
+    const double x[3] = {0.1, 0.2, 0.3}, v[3] = {1.0, 0.0, 0.0};
+    std::vector<punc::gpu::Particle<3>> ps{punc::gpu::Particle<3>(x, v, -1.0, 1.0), punc::gpu::Particle<3>()};
+    static_assert(sizeof(punc::gpu::Particle<3>) == 64, "64-byte particle record");
+    pop.add_particles(ps);
+}
+
 int main(int argc, char **argv) {
     if (argc < 5) return 2;
     const auto coords = read_all<double>(argv[1]);
