@@ -47,8 +47,8 @@ class Mesh {
 public:
     Mesh(const std::vector<double> &coords, const std::vector<int64_t> &cells,
          const std::vector<int64_t> &bfacet_vertices, const std::vector<int32_t> &bfacet_tags,
-         double eps0 = 1.0, const std::vector<int64_t> *vertex_to_dof = nullptr, int64_t n_dofs = 0)
-        : eps0(eps0) {
+         double eps0_ = 1.0, const std::vector<int64_t> *vertex_to_dof = nullptr, int64_t n_dofs = 0)
+        : eps0(eps0_) {
         pg_mesh_desc d{};
         d.n_vertices = (int64_t)(coords.size() / 3);
         d.coords = coords.data();
@@ -86,7 +86,7 @@ public:
 
 // Object (punc/include/punc/object.h:80-130).
 struct Object {
-    explicit Object(std::size_t bnd_id) : bnd_id(bnd_id) {}
+    explicit Object(std::size_t bnd_id_) : bnd_id(bnd_id_) {}
     void set_potential(double p) { potential = p; }
     double get_potential() const { return potential; }
     double charge = 0, current = 0;
