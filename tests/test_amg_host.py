@@ -307,3 +307,22 @@ def test_collapsed_preconditioner_is_symmetric_positive_definite(coarse_max, amg
         bx, by = B(x), B(y)
         assert abs(x @ by - y @ bx) <= 1e-11 * np.linalg.norm(x) * np.linalg.norm(by)
         assert x @ bx > 0.0
+
+
+def _setup_rc(d, A):
+    A = sp.csr_matrix(A)
+    A.sort_indices()
+    rp, ci, v = A.indptr.astype(np.int64), A.indices.astype(np.int32), A.data.astype(np.float64)
+    rc = C.c_int(-1)
+    h = d.amgd_setup(A.shape[0], rp.ctypes.data, ci.ctypes.data, v.ctypes.data, 0, -1.0, 0.0, 0, C.byref(rc))
+    d.amgd_free(h)
+    return rc.value
+
+
+def test_setup_reports_stalled_coarsening_and_a_singular_coarsest_operator(amgd):
+    """Set-up errors the engine turns into status codes: coarsening that stops
+    above the dense-inverse limit (4096 rows; 9, PG_ERR_ARG) and a singular
+    coarsest operator (8, PG_ERR_SINGULAR)."""
+    assert _setup_rc(amgd, sp.identity(5000, format="csr")) == 9
+    assert _setup_rc(amgd, sp.csr_matrix(np.array([[1.0, 1.0], [1.0, 1.0]]))) == 8
+    assert _setup_rc(amgd, sp.csr_matrix(np.array([[2.0, -1.0], [-1.0, 2.0]]))) == 0
