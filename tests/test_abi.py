@@ -102,3 +102,60 @@ def test_every_handle_entry_point_refuses_a_null_handle(lib):
         checked += 1
     assert checked >= 40
     assert lib.pg_destroy(None) == 0
+
+
+_SCALAR = {"int": "i32", "int32_t": "i32", "int64_t": "i64", "uint32_t": "u32", "uint64_t": "u64",
+           "double": "f64", "char": "i8"}
+
+
+def _header_prototypes():
+    src = open(os.path.join(ROOT, "include", "punc_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    protos = {}
+    for ret, name, args in re.findall(r"([A-Za-z_][\w\s\*]*?)\b(pg_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", src):
+        kinds = []
+        for a in [x.strip() for x in args.split(",") if x.strip() and x.strip() != "void"]:
+            is_ptr = "*" in a or "[" in a
+            words = re.sub(r"\[.*?\]", "", a).replace("*", " ").replace("const", " ").split()
+            base = words[0]
+            kinds.append(("ptr", base) if is_ptr else ("val", _SCALAR[base]))
+        protos[name] = (ret.replace("const", "").strip(), kinds)
+    return protos
+
+
+def _ctypes_kind(t):
+    simple = {C.c_int32: "i32", C.c_int: "i32", C.c_int64: "i64", C.c_uint32: "u32", C.c_uint64: "u64",
+              C.c_double: "f64", C.c_char: "i8"}
+    if t in simple:
+        return ("val", simple[t])
+    if t in (C.c_void_p, C.c_char_p):
+        return ("ptr", None if t is C.c_void_p else "char")
+    target = getattr(t, "_type_", None)
+    if target is C.c_void_p:
+        return ("ptr", "void")       # void ** data, or an opaque handle's address (pg_sim **)
+    if target in simple:
+        return ("ptr", {v: k for k, v in _SCALAR.items() if k != "int"}.get(simple[target], simple[target]))
+    return ("ptr", "struct")
+
+
+def test_binding_argument_types_match_the_header():
+    """Every ctypes signature passes each argument with the header's kind:
+    the same integer width and signedness, double, or a pointer to the same
+    element type (opaque handles and structures as pointers)."""
+    from puncpp_gb300 import _lib
+    protos = _header_prototypes()
+    assert set(protos) == set(_lib.SIGNATURES)
+    for name, (args, _) in _lib.SIGNATURES.items():
+        ret, kinds = protos[name]
+        assert len(args) == len(kinds), name
+        for k, (t, (hk, hb)) in enumerate(zip(args, kinds)):
+            ck, cb = _ctypes_kind(t)
+            assert ck == hk, (name, k)
+            if hk == "val":
+                assert cb == hb, (name, k, cb, hb)
+            elif cb == "void":
+                assert hb == "void" or hb.startswith("pg_"), (name, k, hb)
+            elif cb not in (None, "struct"):
+                assert cb == hb or (cb == "int32_t" and hb == "int"), (name, k, cb, hb)
+            elif cb == "struct":
+                assert hb.startswith("pg_"), (name, k, hb)
