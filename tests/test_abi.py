@@ -159,3 +159,37 @@ def test_binding_argument_types_match_the_header():
                 assert cb == hb or (cb == "int32_t" and hb == "int"), (name, k, cb, hb)
             elif cb == "struct":
                 assert hb.startswith("pg_"), (name, k, hb)
+
+
+_STRUCTS = {"MeshDesc": "pg_mesh_desc", "Config": "pg_config", "Object": "pg_object", "Source": "pg_source",
+            "Species": "pg_species", "SolveInfo": "pg_solve_info", "StepArgs": "pg_step_args",
+            "StepResult": "pg_step_result", "Tuning": "pg_tuning", "PoissonLayout": "pg_poisson_layout"}
+
+
+def test_binding_structures_match_the_header_layout(tmp_path):
+    """Each ctypes Structure has the size and field offsets of its C struct
+    (a C program built against include/punc_gpu.h prints them)."""
+    import shutil
+    import subprocess
+    from puncpp_gb300 import _lib
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not available")
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "punc_gpu.h"', "int main(void) {"]
+    expect = []
+    for py, cs in _STRUCTS.items():
+        cls = getattr(_lib, py)
+        lines.append(f'    printf("%zu\\n", sizeof({cs}));')
+        expect.append(C.sizeof(cls))
+        for fname, *_ in cls._fields_:
+            lines.append(f'    printf("%zu\\n", offsetof({cs}, {fname}));')
+            expect.append(getattr(cls, fname).offset)
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c11", "-I" + os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    got = [int(x) for x in out.stdout.split()]
+    assert got == expect
