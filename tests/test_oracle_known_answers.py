@@ -222,3 +222,25 @@ def test_boris_e_cross_b_drift(oracle_mod):
         k = (steps // per) * per
         v_mean = np.mean(vs[:k], axis=0)
         np.testing.assert_allclose(v_mean, drift, atol=3e-3)
+
+
+def test_langmuir_energy_exchange(oracle_mod):
+    # demo/langmuir (langmuir.cpp:291-307 writes KE, PE, TE): the field and
+    # the electrons trade energy back and forth while KE + PE stays constant
+    ma = meshgen.langmuir_cube(8)
+    o = oracle_mod.Oracle(ma)
+    x, v, q, m = langmuir_load(ma, 16, np.random.default_rng(11), amplitude=0.02)
+    o.add_particles(x, v, q, m)
+    dt, KE, PE = 0.1, [], []
+    for n in range(70):
+        phi = o.poisson_direct(o.distribute_cg1(), periodic=True)
+        PE.append(o.potential_energy(phi))
+        KE.append(o.boris(o.efield(phi), (0, 0, 0), dt * (0.5 if n == 0 else 1.0)))
+        o.move(dt, (1.0, 1.0, 1.0))
+        o.update([], dt)
+    KE, PE = np.array(KE[1:]), np.array(PE[1:])
+    TE = KE + PE
+    swing = KE.max() - KE.min()
+    assert KE.min() < 0.05 * KE.max() and PE.min() < 0.05 * PE.max()   # full exchange
+    assert np.corrcoef(KE, PE)[0, 1] < -0.999
+    assert TE.max() - TE.min() < 0.01 * swing
