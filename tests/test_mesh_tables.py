@@ -156,3 +156,19 @@ def test_out_of_range_inputs_are_mesh_errors(what, lib):
     with pytest.raises(L.PgError) as e:
         punc.Mesh(ma)
     assert e.value.code == 3
+
+
+def test_tables_do_not_depend_on_the_vertex_order_within_cells(lib):
+    """Cells may list their vertices in any order (the builder sorts them into
+    the ascending UFC order): permuting each cell's vertex ids and each
+    boundary facet's gives bit-identical tables."""
+    ma = meshgen.probe_box(5, 1.0, 0.3)
+    rng = np.random.default_rng(21)
+    mb = meshgen.MeshArrays(coords=ma.coords, cells=np.ascontiguousarray(rng.permuted(ma.cells, axis=1)),
+                            bfacets=np.ascontiguousarray(rng.permuted(ma.bfacets, axis=1)), btags=ma.btags,
+                            n_dofs=ma.n_dofs, Ld=ma.Ld, origin=ma.origin, n_objects=ma.n_objects)
+    assert not np.array_equal(mb.cells, ma.cells)
+    a, b = punc.Mesh(ma), punc.Mesh(mb)
+    for t in (L.T_CELL_VERTICES, L.T_BARYCENTRIC, L.T_PLANES, L.T_NEIGHBOURS, L.T_CELL_DOFS, L.T_VOLUME,
+              L.T_DV_INV, L.T_EXT_FACETS):
+        np.testing.assert_array_equal(a.table(t), b.table(t), err_msg=str(t))
