@@ -172,3 +172,14 @@ def test_tables_do_not_depend_on_the_vertex_order_within_cells(lib):
     for t in (L.T_CELL_VERTICES, L.T_BARYCENTRIC, L.T_PLANES, L.T_NEIGHBOURS, L.T_CELL_DOFS, L.T_VOLUME,
               L.T_DV_INV, L.T_EXT_FACETS):
         np.testing.assert_array_equal(a.table(t), b.table(t), err_msg=str(t))
+
+
+def test_tables_do_not_depend_on_the_boundary_facet_list_order(lib):
+    ma = meshgen.probe_box(5, 1.0, 0.3)
+    perm = np.random.default_rng(22).permutation(len(ma.btags))
+    mb = meshgen.MeshArrays(coords=ma.coords, cells=ma.cells, bfacets=np.ascontiguousarray(ma.bfacets[perm]),
+                            btags=np.ascontiguousarray(ma.btags[perm]), n_dofs=ma.n_dofs, Ld=ma.Ld,
+                            origin=ma.origin, n_objects=ma.n_objects)
+    a, b = punc.Mesh(ma), punc.Mesh(mb)
+    for t in (L.T_NEIGHBOURS, L.T_EXT_FACETS, L.T_BC_KIND, L.T_OBJ_FACETS):
+        np.testing.assert_array_equal(a.table(t), b.table(t), err_msg=str(t))
