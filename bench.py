@@ -681,11 +681,12 @@ def combine_replicas(res, world):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--gpus", type=int, default=1, help="GPUs of the job (N > 1: one replica per rank under torchrun)")
+    ap.add_argument("--steps", type=int, default=20, help="timed steps")
+    ap.add_argument("--warmup", type=int, default=3, help="untimed warm-up steps (at least 3)")
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"],
+                    help="ours: the engine; reference: the reference's algorithm on the host cores")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the timed CPU baseline sample")
     ap.add_argument("--workload", default="probe-80",
                     help="probe-N (the headline: N^3 sub-cubes, particles scaled by (N/80)^3), langmuir-N, "
                          "batch-R (R independent probe runs), adjoint-N")
@@ -705,7 +706,7 @@ def main():
     ap.add_argument("--pcg-precond", default="amg", choices=sorted(PRECONDS),
                     help="Poisson preconditioner: one AMG V-cycle or Jacobi per iteration")
     ap.add_argument("--runs", type=int, default=16, help="batch-R: runs in the batch (from the workload name)")
-    ap.add_argument("--adjoint-particles", type=int, default=2_000_000)
+    ap.add_argument("--adjoint-particles", type=int, default=2_000_000, help="adjoint-N: particles of the run")
     args = ap.parse_args()
     kind = args.workload.split("-")[0]
     if kind not in ("probe", "langmuir", "batch", "adjoint"):
