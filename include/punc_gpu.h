@@ -18,8 +18,9 @@
 extern "C" {
 #endif
 
-/* 2: pg_poisson_layout gained cycle_bytes */
-#define PG_ABI_VERSION 2
+/* 2: pg_poisson_layout gained cycle_bytes; 3: pg_step_args.potential_energy
+ * and pg_step_result.PE */
+#define PG_ABI_VERSION 3
 
 typedef enum pg_status {
     PG_OK = 0,
@@ -151,6 +152,10 @@ typedef struct pg_step_args {
     int32_t efield_cg1;      /* 1: CG1 field by ESolver and accel_cg1 / boris_cg1, the reference
                                 time loop's default (interaction/interaction.cpp:361-389);
                                 0: DG0 field (EFieldDG0) and accel / boris */
+    int32_t potential_energy; /* 1: pg_step returns the potential energy of the particles at the
+                                step's start in the step's potential, where the time loop takes
+                                it (particle_potential_energy_cg1 after the field,
+                                interaction/interaction.cpp:367-372); pg_run_steps refuses it */
 } pg_step_args;
 
 typedef struct pg_step_result {
@@ -160,6 +165,7 @@ typedef struct pg_step_result {
     int64_t n_injected;
     int32_t pcg_iterations;  /* summed over the step's solves */
     double pcg_residual;
+    double PE;               /* potential energy when pg_step_args.potential_energy = 1, else 0 */
 } pg_step_result;
 
 /* ---- library ---------------------------------------------------------- */
@@ -207,8 +213,10 @@ int pg_get_particles(pg_sim *sim, int64_t capacity, double *x, double *v, double
                      double *m, int64_t *cell, int64_t *pid, int64_t *n_out);
 /* Population::save_file / load_file (punc/include/punc/population.h:806-878):
  * binary = 64-byte {x[3], v[3], q, m} records, text = "%.17g" columns; cells in
- * order, by particle id inside a cell.  Loading adds the particles (grouped by
- * q, m) as pg_add_particles; n_added may be NULL. */
+ * order, by particle id inside a cell.  Loading adds the particles in file
+ * order (ids follow the records, as the reference's one-by-one
+ * add_particles), one pg_add_particles call per run of records with the same
+ * q, m; n_added may be NULL. */
 int pg_population_save(pg_sim *sim, const char *fname, int32_t binary);
 int pg_population_load(pg_sim *sim, const char *fname, int32_t binary, int64_t *n_added);
 /* Population::locate (punc/src/population.cpp:24-39), for n points. */

@@ -13,7 +13,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libpunc_gpu.so")
-ABI_VERSION = 2   # include/punc_gpu.h PG_ABI_VERSION, which these structures follow
+ABI_VERSION = 3   # include/punc_gpu.h PG_ABI_VERSION, which these structures follow
 
 PG_OK = 0
 STATUS_NAMES = {
@@ -76,12 +76,13 @@ class StepArgs(C.Structure):
     _fields_ = [("dt", C.c_double), ("B", C.c_double * 3), ("first_step", C.c_int32),
                 ("use_accel", C.c_int32), ("periodic_move", C.c_int32), ("Ld", C.c_double * 3),
                 ("inject", C.c_int32), ("seed", C.c_uint64), ("step", C.c_uint64), ("E0", C.c_double * 3),
-                ("efield_cg1", C.c_int32)]
+                ("efield_cg1", C.c_int32), ("potential_energy", C.c_int32)]
 
 
 class StepResult(C.Structure):
     _fields_ = [("KE", C.c_double), ("n_particles", C.c_int64), ("n_absorbed", C.c_int64),
-                ("n_injected", C.c_int64), ("pcg_iterations", C.c_int32), ("pcg_residual", C.c_double)]
+                ("n_injected", C.c_int64), ("pcg_iterations", C.c_int32), ("pcg_residual", C.c_double),
+                ("PE", C.c_double)]
 
 
 class Tuning(C.Structure):

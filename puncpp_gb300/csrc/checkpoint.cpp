@@ -14,9 +14,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <map>
 #include <string>
-#include <utility>
 #include <vector>
 
 #include "pg_internal.h"
@@ -99,32 +97,24 @@ extern "C" int pg_population_load(pg_sim *sim, const char *fname, int32_t binary
         }
     }
     std::fclose(f);
-    // group by (q, m) in order of first appearance
-    std::vector<std::pair<double, double>> keys;
-    std::map<std::pair<double, double>, size_t> index;
-    std::vector<std::vector<double>> xs, vs;
-    for (const Record &r : recs) {
-        const auto key = std::make_pair(r.q, r.m);
-        auto it = index.find(key);
-        size_t k;
-        if (it == index.end()) {
-            k = keys.size();
-            index.emplace(key, k);
-            keys.push_back(key);
-            xs.emplace_back();
-            vs.emplace_back();
-        } else {
-            k = it->second;
-        }
-        for (int c = 0; c < 3; ++c) { xs[k].push_back(r.x[c]); vs[k].push_back(r.v[c]); }
-    }
+    // add in file order (the reference adds the records one by one,
+    // population.h:857-878), batching each run of consecutive records with
+    // the same (q, m) into one pg_add_particles call
     int64_t total = 0;
-    for (size_t k = 0; k < keys.size(); ++k) {
+    std::vector<double> xs, vs;
+    size_t i = 0;
+    while (i < recs.size()) {
+        const double q = recs[i].q, m = recs[i].m;
+        xs.clear();
+        vs.clear();
+        size_t j = i;
+        for (; j < recs.size() && recs[j].q == q && recs[j].m == m; ++j)
+            for (int c = 0; c < 3; ++c) { xs.push_back(recs[j].x[c]); vs.push_back(recs[j].v[c]); }
         int64_t added = 0;
-        const int rc = pg_add_particles(sim, xs[k].data(), vs[k].data(), (int64_t)(xs[k].size() / 3), keys[k].first,
-                                        keys[k].second, &added);
+        const int rc = pg_add_particles(sim, xs.data(), vs.data(), (int64_t)(j - i), q, m, &added);
         if (rc) return rc;
         total += added;
+        i = j;
     }
     if (n_added) *n_added = total;
     return PG_OK;

@@ -196,6 +196,12 @@ int upload(pg_sim *s, T **p, const std::vector<T> &h) {
     return PG_OK;
 }
 
+static std::string mixed_capacity_message(int64_t slots) {
+    return "the mixed form holds at most " + std::to_string(kMaxMixedSlots) + " particle slots (int64 deposit sums in "
+           "units of 2^-" + std::to_string(kFixedBits) + " q_max cannot overflow below that); " +
+           std::to_string(slots) + " requested";
+}
+
 void free_particles(DevParticles &p) {
     void *ptrs[] = {p.x, p.y, p.z, p.vx, p.vy, p.vz, p.xf, p.yf, p.zf, p.vxf, p.vyf, p.vzf, p.cell, p.sp, p.pid};
     for (void *q : ptrs)
@@ -205,6 +211,8 @@ void free_particles(DevParticles &p) {
 
 int alloc_particles(pg_sim *s, DevParticles &p, int64_t cap) {
     p = DevParticles{};
+    if (s->cfg.precision == PG_MIXED && cap > kMaxMixedSlots)
+        return fail(PG_ERR_CAPACITY, mixed_capacity_message(cap));
     p.capacity = cap;
     auto al = [&](void **q, size_t bytes) -> bool { return cudaMalloc(q, bytes) == cudaSuccess; };
     bool ok = true;
@@ -246,6 +254,10 @@ int copy_particles(pg_sim *s, const DevParticles &src, const DevParticles &dst, 
 int ensure_capacity(pg_sim *s, int64_t need) {
     if (need <= s->P[0].capacity) return PG_OK;
     int64_t cap = std::max<int64_t>(need + need / 2, std::max<int64_t>(2 * s->P[0].capacity, 1 << 16));
+    if (s->cfg.precision == PG_MIXED) {
+        if (need > kMaxMixedSlots) return fail(PG_ERR_CAPACITY, mixed_capacity_message(need));
+        cap = std::min(cap, kMaxMixedSlots);
+    }
     for (int k = 0; k < 2; ++k) {
         DevParticles np;
         int rc = alloc_particles(s, np, cap);
@@ -732,12 +744,13 @@ static int image_charges(pg_sim *s, std::vector<double> &out, const double *phi 
 
 static bool is_mixed(const pg_sim *s) { return s->cfg.precision == PG_MIXED; }
 
-// Fixed-point unit of the mixed deposit: 2^-40 of the largest |q|.
+// Fixed-point unit of the mixed deposit: 2^-kFixedBits of the largest |q|
+// (the store limit kMaxMixedSlots keeps every dof's int64 sum below 2^62).
 static double fixed_unit(const pg_sim *s) {
     double qmax = 0.0;
     for (int k = 0; k < s->n_species; ++k) qmax = std::max(qmax, std::fabs(s->q[k]));
     if (qmax == 0.0) qmax = 1.0;
-    return std::ldexp(qmax, -40);
+    return std::ldexp(qmax, -kFixedBits);
 }
 
 static void fill_mixed(const pg_sim *s, MixedParams &mp, double dt_push, const double *B, bool accel, double dt_move,
@@ -1013,6 +1026,8 @@ int pg_create(const pg_mesh *mesh, const pg_config *cfg_in, pg_sim **out) {
     *out = nullptr;
     const HostMesh &h = mesh->h;
     if (h.n_objects >= kMaxTags - 2) return fail(PG_ERR_ARG, "pg_create: too many object tags");
+    if (cfg_in && cfg_in->precision == PG_MIXED && cfg_in->particle_capacity > kMaxMixedSlots)
+        return fail(PG_ERR_CAPACITY, "pg_create: " + mixed_capacity_message(cfg_in->particle_capacity));
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(PG_ERR_CUDA, "pg_create: no CUDA device");
     pg_sim *s = new pg_sim;
@@ -1443,11 +1458,21 @@ int pg_get_particles(pg_sim *s, int64_t capacity, double *x, double *v, double *
     if (!s || !n_out) return fail(PG_ERR_ARG, "pg_get_particles: NULL argument");
     const int64_t n = s->n_slots;
     const DevParticles &P = s->P[s->cur];
-    std::vector<double> hx(n), hy(n), hz(n), hvx(n), hvy(n), hvz(n);
+    const bool want = x || v || q || m || cell || pid;
     std::vector<int32_t> hc(n);
-    std::vector<uint8_t> hs(n);
-    std::vector<int64_t> hp(n);
     PG_CUDA(cudaStreamSynchronize(s->stream));
+    if (n > 0) PG_CUDA(cudaMemcpy(hc.data(), P.cell, 4 * n, cudaMemcpyDeviceToHost));
+    if (!want) {
+        // count only
+        int64_t k = 0;
+        for (int64_t i = 0; i < n; ++i) k += hc[i] >= 0;
+        *n_out = k;
+        return PG_OK;
+    }
+    // only the requested arrays cross to the host; ids always (sort key)
+    std::vector<double> hx(x ? n : 0), hy(x ? n : 0), hz(x ? n : 0), hvx(v ? n : 0), hvy(v ? n : 0), hvz(v ? n : 0);
+    std::vector<uint8_t> hs((q || m) ? n : 0);
+    std::vector<int64_t> hp(n);
     if (n > 0 && is_mixed(s)) {
         std::vector<float> f(n);
         auto dn = [&](std::vector<double> &dst, const float *src) {
@@ -1455,29 +1480,32 @@ int pg_get_particles(pg_sim *s, int64_t capacity, double *x, double *v, double *
             for (int64_t i = 0; i < n; ++i) dst[i] = f[i];
             return e;
         };
-        PG_CUDA(dn(hx, P.xf)); PG_CUDA(dn(hy, P.yf)); PG_CUDA(dn(hz, P.zf));
-        PG_CUDA(dn(hvx, P.vxf)); PG_CUDA(dn(hvy, P.vyf)); PG_CUDA(dn(hvz, P.vzf));
+        if (x) { PG_CUDA(dn(hx, P.xf)); PG_CUDA(dn(hy, P.yf)); PG_CUDA(dn(hz, P.zf)); }
+        if (v) { PG_CUDA(dn(hvx, P.vxf)); PG_CUDA(dn(hvy, P.vyf)); PG_CUDA(dn(hvz, P.vzf)); }
     } else if (n > 0) {
-        PG_CUDA(cudaMemcpy(hx.data(), P.x, 8 * n, cudaMemcpyDeviceToHost));
-        PG_CUDA(cudaMemcpy(hy.data(), P.y, 8 * n, cudaMemcpyDeviceToHost));
-        PG_CUDA(cudaMemcpy(hz.data(), P.z, 8 * n, cudaMemcpyDeviceToHost));
-        PG_CUDA(cudaMemcpy(hvx.data(), P.vx, 8 * n, cudaMemcpyDeviceToHost));
-        PG_CUDA(cudaMemcpy(hvy.data(), P.vy, 8 * n, cudaMemcpyDeviceToHost));
-        PG_CUDA(cudaMemcpy(hvz.data(), P.vz, 8 * n, cudaMemcpyDeviceToHost));
+        if (x) {
+            PG_CUDA(cudaMemcpy(hx.data(), P.x, 8 * n, cudaMemcpyDeviceToHost));
+            PG_CUDA(cudaMemcpy(hy.data(), P.y, 8 * n, cudaMemcpyDeviceToHost));
+            PG_CUDA(cudaMemcpy(hz.data(), P.z, 8 * n, cudaMemcpyDeviceToHost));
+        }
+        if (v) {
+            PG_CUDA(cudaMemcpy(hvx.data(), P.vx, 8 * n, cudaMemcpyDeviceToHost));
+            PG_CUDA(cudaMemcpy(hvy.data(), P.vy, 8 * n, cudaMemcpyDeviceToHost));
+            PG_CUDA(cudaMemcpy(hvz.data(), P.vz, 8 * n, cudaMemcpyDeviceToHost));
+        }
     }
     if (n > 0) {
-        PG_CUDA(cudaMemcpy(hc.data(), P.cell, 4 * n, cudaMemcpyDeviceToHost));
-        PG_CUDA(cudaMemcpy(hs.data(), P.sp, n, cudaMemcpyDeviceToHost));
+        if (q || m) PG_CUDA(cudaMemcpy(hs.data(), P.sp, n, cudaMemcpyDeviceToHost));
         PG_CUDA(cudaMemcpy(hp.data(), P.pid, 8 * n, cudaMemcpyDeviceToHost));
     }
     std::vector<int64_t> idx;
     idx.reserve(n);
     for (int64_t i = 0; i < n; ++i)
         if (hc[i] >= 0) idx.push_back(i);
-    std::sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) { return hc[a] != hc[b] ? hc[a] < hc[b] : hp[a] < hp[b]; });
     const int64_t k = (int64_t)idx.size();
     *n_out = k;
-    if (k > capacity && (x || v || q || m || cell || pid)) return fail(PG_ERR_ARG, "pg_get_particles: capacity too small");
+    if (k > capacity) return fail(PG_ERR_ARG, "pg_get_particles: capacity too small");
+    std::sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) { return hc[a] != hc[b] ? hc[a] < hc[b] : hp[a] < hp[b]; });
     for (int64_t t = 0; t < k; ++t) {
         const int64_t i = idx[t];
         if (x) { x[3 * t] = hx[i]; x[3 * t + 1] = hy[i]; x[3 * t + 2] = hz[i]; }
@@ -2237,6 +2265,8 @@ static int upload_circuit(pg_sim *s) {
 int pg_run_steps(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_objects, int32_t n_steps,
                  int32_t use_graph, pg_step_result *results) {
     if (!s || !a || n_steps < 0 || (n_objects > 0 && !objects)) return fail(PG_ERR_ARG, "pg_run_steps: bad arguments");
+    if (a->potential_energy)
+        return fail(PG_ERR_ARG, "pg_run_steps: the potential energy is computed per step by pg_step only");
     if (n_steps == 0) return PG_OK;
     const int n = s->n_obj;
     std::vector<int> map(n, -1);
@@ -2786,6 +2816,14 @@ int pg_step(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_obje
     } else if (!is_mixed(s)) {
         StageScope t(s, "efield");
         step_field_f64(s, a->E0);
+    }
+    if (a->potential_energy) {
+        // particle_potential_energy_cg1 at the time loop's place: particles at
+        // the step's start, the step's potential (interaction.cpp:367-372)
+        StageScope t(s, "PE");
+        if ((rc = diag_scratch(s))) return rc;
+        launch_potential_energy(s->dm, s->P[s->cur], s->n_slots, is_mixed(s), s->d_q, s->phi, s->diag_acc, s->stream);
+        PG_CUDA(cudaMemcpyAsync(&out.PE, s->diag_acc, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     }
     // accelerator + move + update, depositing the next step's charge
     {

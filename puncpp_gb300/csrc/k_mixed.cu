@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(kThreads) k_kinetic_mixed(DevParticles p, int6
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
-// rho = (sum in units of 2^-40 q_max) * q_max 2^-40 * dv_inv
+// rho = (sum in units of 2^-kFixedBits q_max) * q_max 2^-kFixedBits * dv_inv
 __global__ void k_fixed_to_rho(const unsigned long long *__restrict__ fixed, const double *__restrict__ dv_inv,
                                double unit, int32_t n, double *__restrict__ rho_acc, double *__restrict__ rho) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;

@@ -81,6 +81,8 @@ __device__ __forceinline__ void na_block_sum2(double a, double b, double *sh, do
 }
 
 // Sum of per-block partials (same order in every block), valid in thread 0.
+// Ends with a block barrier, so that the next call's warp sums cannot
+// overwrite the shared slots before thread 0 has read them.
 __device__ __forceinline__ void na_grid_sum2(const double *pa, const double *pb, int nb, double *sh, double &ra,
                                              double &rb) {
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
@@ -99,6 +101,7 @@ __device__ __forceinline__ void na_grid_sum2(const double *pa, const double *pb,
         ra = (r[0] + r[1]) + (r[2] + r[3]);
         rb = (r[4] + r[5]) + (r[6] + r[7]);
     }
+    __syncthreads();
 }
 
 __global__ void __launch_bounds__(kNaThreads, 2) k_pcg_csr_noalloc(NoAllocArgs a) {

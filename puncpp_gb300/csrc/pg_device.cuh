@@ -19,6 +19,13 @@ namespace pg {
 
 constexpr int kMaxSpecies = 8;
 constexpr int kMaxTags = 64;
+// Mixed form: the CG1 deposit sums q lambda in int64 units of 2^-kFixedBits
+// q_max.  One particle adds at most 2^kFixedBits units to a dof, so a dof's
+// sum stays below 2^62 (int64 without overflow, with margin) as long as the
+// particle store holds at most kMaxMixedSlots = 2^(62 - kFixedBits) slots,
+// whatever the distribution of the particles over the cells.
+constexpr int kFixedBits = 30;
+constexpr int64_t kMaxMixedSlots = int64_t(1) << (62 - kFixedBits);
 constexpr int kDead = -1;                 // cell id of a free particle slot
 constexpr int kWalkFail = -2147483647;    // walk step limit reached
 
@@ -144,7 +151,7 @@ struct InjectParams {
     // v2.xy), (v2.z, inward normal), (cell as int bits, 0, 0, 0); null in the
     // FP64 form
     const float4 *facets_f;
-    // mixed form: fixed-point deposit target and q * 2^40 / q_max per species
+    // mixed form: fixed-point deposit target and q * 2^kFixedBits / q_max per species
     unsigned long long *rho_fixed;
     float q_scaled[kMaxSpecies];
 };
@@ -155,7 +162,7 @@ struct MixedParams {
     float half_m[kMaxSpecies];
     float t[kMaxSpecies][3];
     float s[kMaxSpecies][3];
-    float q_scaled[kMaxSpecies];  // q * 2^40 / q_max
+    float q_scaled[kMaxSpecies];  // q * 2^kFixedBits / q_max
     int32_t has_B;
     int32_t accel;
     float dt;

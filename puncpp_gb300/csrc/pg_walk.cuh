@@ -126,7 +126,7 @@ __device__ __forceinline__ void barycentric_fp64(const DevMesh &m, int c, double
 }
 
 // Fixed-point CG1 deposit of the mixed form: q*lambda_i in units of
-// 2^-40 q_max (q_scaled = q * 2^40 / q_max in FP32), added with int64
+// 2^-kFixedBits q_max (q_scaled = q * 2^kFixedBits / q_max in FP32), added with int64
 // atomics, so the sum is the same in any order.
 __device__ __forceinline__ void deposit_fixed(const DevMesh &m, int c, float x, float y, float z, float q_scaled,
                                               unsigned long long *rho_fixed) {

@@ -6,16 +6,22 @@ interior facets) becomes 0, the next (the exterior boundary) 1, the rest
 objects 2, 3, ...  `read_mesh` does the same and returns the flat arrays the
 engine's mesh builder takes.
 
-Facet tags are accepted in the cell-relative form of a mesh value collection
-(`<value cell_index=.. local_entity=.. value=../>`, local facet i opposite local
-vertex i), which identifies each facet without DOLFIN's global facet
-numbering.  The global-index form (`<entity index=.. value=../>`) indexes
-facets by DOLFIN's own facet enumeration, which is not restated here; such
-files are refused with a message (convert them to the cell-relative form, or
-pass the boundary facets as vertex triples).
+Facet tags are read in either form DOLFIN 2019.1 writes:
 
-`write_mesh` writes the same two files from a mesh (tags in the cell-relative
-form), e.g. to hand a generated mesh to the reference.
+* a mesh value collection, cell-relative (`<value cell_index=..
+  local_entity=.. value=../>`, local facet i opposite local vertex i);
+* a mesh function indexed by DOLFIN's global facet numbering (`<mesh_function
+  dim="2"><entity index=.. value=../>`), the form dolfin-convert writes for
+  gmsh meshes.  In a serial mesh DOLFIN numbers the facets by key matching
+  (TopologyComputation::compute_entities_by_key_matching): each facet's
+  global vertex ids are sorted into a key, the keys of all cells' facets are
+  sorted lexicographically, and facet k is the k-th distinct key.
+  `dolfin_facet_numbering` restates that.
+
+HDF5 meshes (mesh.cpp:75-84) are refused: no HDF5 library is present.
+
+`write_mesh` writes the same two files from a mesh, tags in either form, e.g.
+to hand a generated mesh to the reference.
 """
 from __future__ import annotations
 
@@ -79,9 +85,21 @@ def _read_cells_vertices(path: str):
     return coords, cells
 
 
+def dolfin_facet_numbering(cells: np.ndarray) -> np.ndarray:
+    """The facets of a tetrahedral mesh in DOLFIN's serial numbering
+    (TopologyComputation::compute_entities_by_key_matching, DOLFIN 2019.1):
+    row k holds the ascending global vertex ids of facet k; the rows are the
+    distinct sorted vertex triples of all cells' facets in lexicographic
+    order."""
+    sc = np.sort(np.asarray(cells, np.int64), axis=1)
+    tri = np.concatenate([sc[:, [1, 2, 3]], sc[:, [0, 2, 3]], sc[:, [0, 1, 3]], sc[:, [0, 1, 2]]], axis=0)
+    return np.unique(tri, axis=0)
+
+
 def _read_facet_tags(path: str, cells: np.ndarray):
     """(sorted vertex triples, tag values) of the listed facets."""
     tri, vals = [], []
+    glob_idx, glob_vals = [], []
     for _, el in ET.iterparse(path, events=("end",)):
         t = _local(el.tag)
         if t == "value":
@@ -91,10 +109,18 @@ def _read_facet_tags(path: str, cells: np.ndarray):
             vals.append(v)
             el.clear()
         elif t == "entity":
-            raise ValueError(f"{path}: facet function indexed by DOLFIN's global facet numbering; convert it to "
-                             "the cell_index/local_entity form (mesh value collection)")
+            glob_idx.append(int(el.get("index")))
+            glob_vals.append(int(el.get("value")))
+            el.clear()
         elif t in ("mesh_function", "mesh_value_collection") and el.get("dim") not in (None, "2"):
             raise ValueError(f"{path}: facet tags must have dim 2")
+    if glob_idx:
+        facets = dolfin_facet_numbering(cells)
+        idx = np.asarray(glob_idx, np.int64)
+        if idx.min() < 0 or idx.max() >= len(facets):
+            raise ValueError(f"{path}: facet index out of range (the mesh has {len(facets)} facets)")
+        tri += facets[idx].tolist()
+        vals += glob_vals
     return np.array(tri, dtype=np.int64).reshape(-1, 3), np.array(vals, dtype=np.int64)
 
 
@@ -136,10 +162,14 @@ def read_mesh(fname: str, periodic_box=None) -> MeshArrays:
                       Ld=Ld, origin=origin, n_objects=len(labels) - 2)
 
 
-def write_mesh(fname: str, ma: MeshArrays, tag_values=None):
-    """Write name.xml and name_facet_region.xml (boundary tags in the
-    cell-relative form; tag_values maps the mesh's tags 1, 2, .. to the values
-    written, e.g. gmsh physical ids)."""
+def write_mesh(fname: str, ma: MeshArrays, tag_values=None, facet_form: str = "cell"):
+    """Write name.xml and name_facet_region.xml.  facet_form "cell": boundary
+    tags as a cell-relative mesh value collection; "global": a mesh function
+    over every facet in DOLFIN's numbering (interior facets 0), the layout
+    dolfin-convert writes.  tag_values maps the mesh's tags 1, 2, .. to the
+    values written, e.g. gmsh physical ids."""
+    if facet_form not in ("cell", "global"):
+        raise ValueError("facet_form is 'cell' or 'global'")
     stem = _stem(fname)
     with open(stem + ".xml", "w") as f:
         f.write('<?xml version="1.0"?>\n<dolfin xmlns:dolfin="http://fenicsproject.org">\n')
@@ -168,6 +198,19 @@ def write_mesh(fname: str, ma: MeshArrays, tag_values=None):
     if np.any(keys[np.minimum(pos, len(keys) - 1)] != bkeys):
         raise ValueError("a boundary facet is not a facet of any cell")
     cell_local = owner[pos]
+    if facet_form == "global":
+        facets = dolfin_facet_numbering(ma.cells)
+        fkeys = (facets[:, 0] * nv + facets[:, 1]) * nv + facets[:, 2]
+        values = np.zeros(len(facets), np.int64)
+        at = np.searchsorted(fkeys, bkeys)
+        values[at] = [tag_values[t] if tag_values is not None else t for t in ma.btags.tolist()]
+        with open(stem + "_facet_region.xml", "w") as f:
+            f.write('<?xml version="1.0"?>\n<dolfin xmlns:dolfin="http://fenicsproject.org">\n')
+            f.write(f'  <mesh_function type="uint" dim="2" size="{len(facets)}">\n')
+            for k, v in enumerate(values.tolist()):
+                f.write(f'    <entity index="{k}" value="{v}" />\n')
+            f.write("  </mesh_function>\n</dolfin>\n")
+        return
     with open(stem + "_facet_region.xml", "w") as f:
         f.write('<?xml version="1.0"?>\n<dolfin xmlns:dolfin="http://fenicsproject.org">\n')
         f.write(f'  <mesh_value_collection type="uint" dim="2" size="{len(bkeys)}">\n')

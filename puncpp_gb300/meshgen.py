@@ -200,6 +200,77 @@ def mapped_sphere_shell(n: int, k_inner: int, r_inner: float, r_outer: float) ->
                       Ld=(L, L, L), origin=(-r_outer,) * 3, n_objects=1)
 
 
+def icosphere(level: int):
+    """Unit-sphere triangulation: the icosahedron, each triangle split into 4
+    level times, vertices projected onto the sphere.  Returns (vertices
+    (10*4^level + 2, 3), triangles (20*4^level, 3))."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
+         (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
+         (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(p, float) / np.linalg.norm(p) for p in v]
+    tris = [tuple(x) for x in f]
+    for _ in range(level):
+        mid = {}
+
+        def midpoint(a, b):
+            key = (a, b) if a < b else (b, a)
+            if key not in mid:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                mid[key] = len(verts) - 1
+            return mid[key]
+
+        nxt = []
+        for a, b, c in tris:
+            ab, bc, ca = midpoint(a, b), midpoint(b, c), midpoint(c, a)
+            nxt += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        tris = nxt
+    return np.array(verts), np.array(tris, dtype=np.int64)
+
+
+def sphere_shell(r_inner: float, r_outer: float, level: int = 3) -> MeshArrays:
+    """Body-fitted tetrahedral shell between the spheres r_inner (the object,
+    tag 2) and r_outer (the exterior boundary, tag 1): the geometry of the
+    reference's test/sphere.geo.
+
+    The icosphere of the given level is extruded radially through layers
+    whose radii grow geometrically, so that a layer's thickness matches the
+    triangles' edge length at its radius (resolution proportional to r, as the
+    .geo file's 0.2 at r = 1 growing to 6 at r = 20).  Every triangle x layer
+    prism splits into 3 tetrahedra by the order of its vertices' ids (sorted
+    a < b < c below, a' < b' < c' above: (a,b,c,a'), (b,c,a',b'), (c,a',b',c')),
+    which cuts every quadrilateral side face along the diagonal from its
+    larger bottom vertex to its smaller top vertex; the neighbouring prism
+    cuts the shared face the same way, so the mesh is conforming.  Radial
+    extrusion keeps those side faces planar."""
+    if not 0.0 < r_inner < r_outer:
+        raise ValueError("need 0 < r_inner < r_outer")
+    u, tri = icosphere(level)
+    nu = u.shape[0]
+    e = u[tri]
+    edge = np.mean(np.linalg.norm(e[:, 0] - e[:, 1], axis=1))
+    layers = max(1, int(np.ceil(np.log(r_outer / r_inner) / np.log1p(edge))))
+    radii = r_inner * (r_outer / r_inner) ** (np.arange(layers + 1) / layers)
+    coords = (radii[:, None, None] * u[None, :, :]).reshape(-1, 3)
+    a, b, c = np.sort(tri, axis=1).T
+    cells = []
+    for k in range(layers):
+        lo, hi = k * nu, (k + 1) * nu
+        cells.append(np.stack([a + lo, b + lo, c + lo, a + hi], axis=1))
+        cells.append(np.stack([b + lo, c + lo, a + hi, b + hi], axis=1))
+        cells.append(np.stack([c + lo, a + hi, b + hi, c + hi], axis=1))
+    cells = np.concatenate(cells)
+    bf = np.concatenate([tri, tri + layers * nu])
+    btags = np.concatenate([np.full(len(tri), 2, np.int32), np.full(len(tri), 1, np.int32)])
+    L = 2 * r_outer
+    return MeshArrays(coords=np.ascontiguousarray(coords), cells=np.ascontiguousarray(cells),
+                      bfacets=np.ascontiguousarray(bf), btags=btags, n_dofs=int(coords.shape[0]),
+                      Ld=(L, L, L), origin=(-r_outer,) * 3, n_objects=1)
+
+
 def langmuir_cube(n: int = 16) -> MeshArrays:
     """Periodic unit cube, n^3 x 6 cells (n=16: 24,576 cells, 4,096 dofs)."""
     return kuhn_box(n, 0.0, 1.0, periodic=True)

@@ -250,17 +250,19 @@ class Population:
         L.check(L.load().pg_statistics(self.handle, L.dptr(out)))
         return out
 
-    def particles(self) -> dict:
-        """Live particles ordered by (cell, id): x, v, q, m, cell, id."""
+    def particles(self, fields=("x", "v", "q", "m", "cell", "id")) -> dict:
+        """Live particles ordered by (cell, id): x, v, q, m, cell, id (only
+        the named fields cross to the host)."""
         lib = L.load()
         n = C.c_int64()
         L.check(lib.pg_get_particles(self.handle, 0, None, None, None, None, None, None, C.byref(n)))
         k = n.value
-        x = np.zeros((k, 3)); v = np.zeros((k, 3)); q = np.zeros(k); m = np.zeros(k)
-        cell = np.zeros(k, np.int64); pid = np.zeros(k, np.int64)
-        L.check(lib.pg_get_particles(self.handle, k, L.dptr(x), L.dptr(v), L.dptr(q), L.dptr(m), L.i64ptr(cell),
-                                     L.i64ptr(pid), C.byref(n)))
-        return dict(x=x, v=v, q=q, m=m, cell=cell, id=pid)
+        shapes = {"x": (k, 3), "v": (k, 3), "q": (k,), "m": (k,), "cell": (k,), "id": (k,)}
+        out = {f: np.zeros(shapes[f], np.int64 if f in ("cell", "id") else np.float64) for f in fields}
+        ptr = {f: (L.i64ptr(a) if f in ("cell", "id") else L.dptr(a)) for f, a in out.items()}
+        L.check(lib.pg_get_particles(self.handle, k, ptr.get("x"), ptr.get("v"), ptr.get("q"), ptr.get("m"),
+                                     ptr.get("cell"), ptr.get("id"), C.byref(n)))
+        return out
 
     def update(self, objects, dt: float):
         arr = _objects_in(objects)
@@ -536,6 +538,32 @@ def create_flux(pop: Population, species):
     L.check(L.load().pg_create_flux(pop.handle, arr, len(species)))
 
 
+def load_particles(pop: Population, species, seed: int = 0, batch: int = 1 << 20) -> list:
+    """load_particles (punc/include/punc/injector.h:244-278): for each
+    species its num particles at positions uniform over the mesh (rejection
+    sampling in the cube [min coordinate, max coordinate]^3 of UniformPosition,
+    punc/include/punc/distributions.h:186-230, a point kept when it lies in a
+    cell) with Maxwellian velocities (vd + vth N(0, 1) per component).  The
+    reference's generator is unseeded; this one is numpy's, seeded.  Returns
+    the number added per species."""
+    rng = np.random.default_rng(seed)
+    co = pop.mesh.arrays.coords
+    lo, hi = float(co.min()), float(co.max())
+    added = []
+    for s in species:
+        need, xs = int(s.num), []
+        got = 0
+        while got < need:
+            pts = lo + (hi - lo) * rng.random((max(batch, 2 * (need - got)), 3))
+            pts = pts[pop.locate(pts) >= 0][: need - got]
+            xs.append(pts)
+            got += len(pts)
+        x = np.concatenate(xs) if xs else np.zeros((0, 3))
+        v = np.asarray(s.vd, float) + s.vth * rng.standard_normal((need, 3))
+        added.append(pop.add_particles(x, v, s.q, s.m))
+    return added
+
+
 def inject_particles(pop: Population, species, facets, dt: float, seed: int = 0, step: int = 0) -> int:
     """inject_particles (punc/include/punc/injector.h:157-232); create_flux must
     have been called for these species."""
@@ -545,12 +573,17 @@ def inject_particles(pop: Population, species, facets, dt: float, seed: int = 0,
 
 
 def step(pop: Population, objects, dt: float, B=(0.0, 0.0, 0.0), first_step=False, use_accel=False, Ld=None,
-         inject=False, seed=0, step_no=0, E0=(0.0, 0.0, 0.0), efield_cg1=False) -> L.StepResult:
+         inject=False, seed=0, step_no=0, E0=(0.0, 0.0, 0.0), efield_cg1=False,
+         potential_energy=False) -> L.StepResult:
     """One fused timestep in the order of interaction.cpp:342-480 (efield_cg1:
-    ESolver + accel_cg1/boris_cg1, else EFieldDG0 + accel/boris)."""
+    ESolver + accel_cg1/boris_cg1, else EFieldDG0 + accel/boris);
+    potential_energy: also particle_potential_energy_cg1 of the particles at
+    the step's start in the step's potential (res.PE), as the time loop
+    records it."""
     a = L.StepArgs(dt, (C.c_double * 3)(*B), 1 if first_step else 0, 1 if use_accel else 0,
                    0 if Ld is None else 1, (C.c_double * 3)(*(Ld if Ld is not None else (0.0, 0.0, 0.0))),
-                   1 if inject else 0, seed, step_no, (C.c_double * 3)(*E0), 1 if efield_cg1 else 0)
+                   1 if inject else 0, seed, step_no, (C.c_double * 3)(*E0), 1 if efield_cg1 else 0,
+                   1 if potential_energy else 0)
     arr = _objects_in(objects)
     res = L.StepResult()
     L.check(L.load().pg_step(pop.handle, C.byref(a), arr, len(objects), C.byref(res)))

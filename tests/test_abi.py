@@ -31,7 +31,7 @@ def test_bindings_cover_the_header():
 
 def test_abi_version(lib):
     from puncpp_gb300 import _lib
-    assert lib.pg_abi_version() == _lib.ABI_VERSION == 2
+    assert lib.pg_abi_version() == _lib.ABI_VERSION == 3
 
 
 def test_philox_known_answers(lib, oracle_mod):
@@ -193,3 +193,24 @@ def test_binding_structures_match_the_header_layout(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     got = [int(x) for x in out.stdout.split()]
     assert got == expect
+
+
+def test_mixed_store_is_bounded_so_deposit_sums_cannot_overflow(lib):
+    """The mixed form's deposit adds q lambda in int64 units of 2^-30 q_max:
+    one particle adds at most 2^30 units to a dof, so a store of at most 2^32
+    slots keeps every dof's sum below 2^62 whatever the particle distribution.
+    A larger store is refused with PG_ERR_CAPACITY before the device is
+    touched (no GPU needed)."""
+    from puncpp_gb300 import _lib as L
+    from puncpp_gb300 import meshgen, punc
+    fixed_bits, max_slots = 30, 1 << 32
+    assert max_slots * (1 << fixed_bits) <= 1 << 62
+    mesh = punc.Mesh(meshgen.kuhn_box(2))
+    cfg = L.Config()
+    cfg.precision = L.PG_MIXED
+    cfg.particle_capacity = max_slots + 1
+    h = C.c_void_p()
+    rc = lib.pg_create(mesh.handle, C.byref(cfg), C.byref(h))
+    assert L.STATUS_NAMES[rc] == "PG_ERR_CAPACITY" and not h.value
+    msg = lib.pg_last_error()
+    assert b"at most 4294967296 particle slots" in msg and b"2^-30" in msg

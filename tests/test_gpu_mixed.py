@@ -82,6 +82,29 @@ def test_mixed_deposit_is_deterministic_and_close_to_fp64(lib, oracle_mod):
     assert rel(r1, o.distribute_cg1()) < 1e-5
 
 
+def test_mixed_deposit_with_millions_of_particles_on_one_dof(lib, oracle_mod):
+    """10M particles of one sign packed next to one vertex of a single
+    sub-cube: that dof collects more than 2^23 units of q_max.  In units of
+    2^-40 q_max its int64 sum would pass 2^63; the engine's 2^-30 units (store
+    bounded to 2^32 slots) keep it exact, and the charge equals the oracle's
+    FP64 deposit of the same FP32 positions to 1e-7."""
+    ma = meshgen.kuhn_box(1)
+    mesh = punc.Mesh(ma)
+    pop = punc.Population(mesh, precision=L.PG_MIXED, capacity=10_000_000)
+    o = oracle_mod.Oracle(ma)
+    rng = np.random.default_rng(11)
+    xs = f32(0.001 + 0.049 * rng.random((10_000_000, 3)))
+    vs = np.zeros_like(xs)
+    assert pop.add_particles(xs, vs, -1.0, 1.0) == len(xs)
+    assert o.add_particles(xs, vs, -1.0, 1.0) == len(xs)
+    rho = punc.distribute_cg1(pop)
+    ref = o.distribute_cg1()
+    charge = ref / mesh.table(L.T_DV_INV)
+    assert np.abs(charge).max() > 2 ** 23
+    assert rel(rho, ref) < 1e-7
+    pop.close()
+
+
 def test_mixed_push_close_to_fp64(lib, oracle_mod):
     ma, mesh, pop, o, rng = mixed_setup(oracle_mod)
     phi = rng.normal(size=mesh.n_dofs)
