@@ -239,6 +239,16 @@ int pg_move_periodic(pg_sim *sim, double dt, const double Ld[3]);
  * particle by the facet walk of relocate_fast (539-569), absorb at boundaries,
  * zero then tally object currents, charge += current, current /= dt. */
 int pg_update(pg_sim *sim, pg_object *objects, int32_t n_objects, double dt);
+/* The absorbed-particle tally of the last pg_update, pg_step or pg_run_steps
+ * step, per boundary tag and species: Population::update
+ * (punc/include/punc/population.h:641-699) sums the same tally over the
+ * species into each object's current.  counts[t * n_species + k] = particles
+ * of species k absorbed at tag t (t = 0 .. n_tags-1; 1 = exterior boundary,
+ * 2.. objects; n_tags <= 64), q[k] and m[k] the species' charge and mass, in
+ * the engine's species order (first use of each (q, m)), for k < n_species;
+ * *n_species_out = the number of species.  Any output may be NULL. */
+int pg_absorbed_counts(pg_sim *sim, int64_t *counts, int32_t n_tags, int32_t n_species, double *q, double *m,
+                       int32_t *n_species_out);
 /* kinetic_energy (punc/include/punc/diagnostics.h:248-265). */
 int pg_kinetic_energy(pg_sim *sim, double *KE);
 

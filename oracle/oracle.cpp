@@ -1009,6 +1009,364 @@ int32_t or_pcg(void *h, const double *b_in, const int64_t *kind, const double *g
     return std::sqrt(rr) <= tol ? it : -1;
 }
 
+// ---- AMG-preconditioned CG for the timed CPU baseline ---------------------
+// The reference solves the Poisson system with PETSc's GMRES preconditioned by
+// hypre's algebraic multigrid (punc/src/poisson.cpp:297-304).  The CPU
+// baseline keeps that solver class with a textbook smoothed-aggregation AMG
+// (Vanek, Mandel, Brezina 1996) under CG on the symmetric Dirichlet-eliminated
+// system: aggregates of strongly coupled neighbourhoods (|a_ij| >= theta
+// sqrt(a_ii a_jj), theta = 0.08 halved per level), tentative prolongator P0
+// (one per aggregate), smoothed
+// P = (I - w D^-1 A) P0 with w = 4 / (3 lambda_max(D^-1 A)), Galerkin coarse
+// operators P^T A P down to at most 400 rows, a dense Cholesky solve on the
+// coarsest level (a periodic system's constant null space regularised away),
+// and one weighted-Jacobi sweep (weight w of the level) before and after each
+// coarse correction (a symmetric V-cycle).  Products run on nthreads threads.
+
+struct Csr {
+    int64_t n = 0, m = 0;                 // rows, columns
+    std::vector<int64_t> ptr, col;
+    std::vector<double> val;
+};
+
+static void csr_matvec(const Csr &A, const double *x, double *y, int nt) {
+    for_cells(A.n, nt, [&](int64_t rb, int64_t re, int) {
+        for (int64_t i = rb; i < re; ++i) {
+            double s = 0.0;
+            for (int64_t k = A.ptr[i]; k < A.ptr[i + 1]; ++k) s += A.val[k] * x[A.col[k]];
+            y[i] = s;
+        }
+    });
+}
+
+static Csr csr_transpose(const Csr &A) {
+    Csr T;
+    T.n = A.m; T.m = A.n;
+    T.ptr.assign(T.n + 1, 0);
+    for (int64_t c : A.col) ++T.ptr[c + 1];
+    for (int64_t i = 0; i < T.n; ++i) T.ptr[i + 1] += T.ptr[i];
+    T.col.resize(A.col.size());
+    T.val.resize(A.val.size());
+    std::vector<int64_t> pos(T.ptr.begin(), T.ptr.end() - 1);
+    for (int64_t i = 0; i < A.n; ++i)
+        for (int64_t k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
+            const int64_t q = pos[A.col[k]]++;
+            T.col[q] = i;
+            T.val[q] = A.val[k];
+        }
+    return T;
+}
+
+// C = A B (Gustavson's row-by-row product with a dense accumulator per thread).
+static Csr csr_matmul(const Csr &A, const Csr &B, int nt) {
+    Csr C;
+    C.n = A.n; C.m = B.m;
+    const int T = std::max(1, nt);
+    std::vector<std::vector<int64_t>> rcol(A.n);
+    std::vector<std::vector<double>> rval(A.n);
+    for_cells(A.n, T, [&](int64_t rb, int64_t re, int) {
+        std::vector<double> acc(B.m, 0.0);
+        std::vector<int64_t> mark(B.m, -1), used;
+        for (int64_t i = rb; i < re; ++i) {
+            used.clear();
+            for (int64_t k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
+                const int64_t j = A.col[k];
+                const double a = A.val[k];
+                for (int64_t q = B.ptr[j]; q < B.ptr[j + 1]; ++q) {
+                    const int64_t c = B.col[q];
+                    if (mark[c] != i) { mark[c] = i; acc[c] = 0.0; used.push_back(c); }
+                    acc[c] += a * B.val[q];
+                }
+            }
+            std::sort(used.begin(), used.end());
+            rcol[i] = used;
+            rval[i].resize(used.size());
+            for (size_t t = 0; t < used.size(); ++t) rval[i][t] = acc[used[t]];
+        }
+    });
+    C.ptr.assign(C.n + 1, 0);
+    for (int64_t i = 0; i < C.n; ++i) C.ptr[i + 1] = C.ptr[i] + (int64_t)rcol[i].size();
+    C.col.resize(C.ptr[C.n]);
+    C.val.resize(C.ptr[C.n]);
+    for (int64_t i = 0; i < C.n; ++i) {
+        std::copy(rcol[i].begin(), rcol[i].end(), C.col.begin() + C.ptr[i]);
+        std::copy(rval[i].begin(), rval[i].end(), C.val.begin() + C.ptr[i]);
+    }
+    return C;
+}
+
+struct AmgLevel {
+    Csr A, P, R;                 // operator, prolongator to this level from the next, R = P^T
+    std::vector<double> dinv;
+    double omega = 2.0 / 3.0;    // smoother weight 4 / (3 lambda_max(D^-1 A))
+    std::vector<double> x, b, r; // work vectors
+};
+
+struct OracleAmg {
+    std::vector<AmgLevel> lev;
+    std::vector<double> chol;    // dense Cholesky factor of the coarsest operator (row-major, lower)
+    int64_t nc = 0;
+    std::vector<int64_t> free_of; // reduced index -> dof
+    std::vector<int64_t> red_of;  // dof -> reduced index or -1
+    int periodic = 0;
+};
+
+static std::vector<int64_t> aggregate(const Csr &A, const std::vector<double> &diag, double theta, int64_t &n_agg) {
+    const int64_t n = A.n;
+    std::vector<int64_t> agg(n, -1);
+    auto strong = [&](int64_t i, int64_t k) {
+        const int64_t j = A.col[k];
+        return j != i && std::fabs(A.val[k]) >= theta * std::sqrt(std::fabs(diag[i] * diag[j]));
+    };
+    n_agg = 0;
+    // pass 1: nodes whose strong neighbourhood is still free seed an aggregate
+    for (int64_t i = 0; i < n; ++i) {
+        if (agg[i] >= 0) continue;
+        bool ok = true;
+        for (int64_t k = A.ptr[i]; k < A.ptr[i + 1] && ok; ++k)
+            if (strong(i, k) && agg[A.col[k]] >= 0) ok = false;
+        if (!ok) continue;
+        agg[i] = n_agg;
+        for (int64_t k = A.ptr[i]; k < A.ptr[i + 1]; ++k)
+            if (strong(i, k)) agg[A.col[k]] = n_agg;
+        ++n_agg;
+    }
+    // pass 2: the rest join the aggregate they couple to most strongly
+    std::vector<int64_t> first(agg);
+    for (int64_t i = 0; i < n; ++i) {
+        if (first[i] >= 0) continue;
+        double best = -1.0;
+        for (int64_t k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
+            const int64_t j = A.col[k];
+            if (strong(i, k) && first[j] >= 0 && std::fabs(A.val[k]) > best) { best = std::fabs(A.val[k]); agg[i] = first[j]; }
+        }
+    }
+    // pass 3: leftovers (no strongly coupled aggregate) form their own
+    for (int64_t i = 0; i < n; ++i) {
+        if (agg[i] >= 0) continue;
+        agg[i] = n_agg;
+        for (int64_t k = A.ptr[i]; k < A.ptr[i + 1]; ++k)
+            if (strong(i, k) && agg[A.col[k]] < 0) agg[A.col[k]] = n_agg;
+        ++n_agg;
+    }
+    return agg;
+}
+
+static void amg_vcycle(const OracleAmg &M, std::vector<AmgLevel> &lev, size_t l, int nt) {
+    AmgLevel &L = lev[l];
+    const int64_t n = L.A.n;
+    if (l + 1 == lev.size()) {
+        // dense Cholesky solve of the coarsest system
+        std::vector<double> y(L.b);
+        for (int64_t i = 0; i < n; ++i) {
+            double s = y[i];
+            for (int64_t k = 0; k < i; ++k) s -= M.chol[i * n + k] * y[k];
+            y[i] = s / M.chol[i * n + i];
+        }
+        for (int64_t i = n - 1; i >= 0; --i) {
+            double s = y[i];
+            for (int64_t k = i + 1; k < n; ++k) s -= M.chol[k * n + i] * y[k];
+            y[i] = s / M.chol[i * n + i];
+        }
+        L.x = y;
+        return;
+    }
+    const double w = L.omega;
+    for (int64_t i = 0; i < n; ++i) L.x[i] = w * L.dinv[i] * L.b[i];
+    csr_matvec(L.A, L.x.data(), L.r.data(), nt);
+    for (int64_t i = 0; i < n; ++i) L.r[i] = L.b[i] - L.r[i];
+    AmgLevel &C = lev[l + 1];
+    csr_matvec(L.R, L.r.data(), C.b.data(), nt);
+    amg_vcycle(M, lev, l + 1, nt);
+    csr_matvec(L.P, C.x.data(), L.r.data(), nt);
+    for (int64_t i = 0; i < n; ++i) L.x[i] += L.r[i];
+    csr_matvec(L.A, L.x.data(), L.r.data(), nt);
+    for (int64_t i = 0; i < n; ++i) L.x[i] += w * L.dinv[i] * (L.b[i] - L.r[i]);
+}
+
+// AMG hierarchy of the Dirichlet-eliminated stiffness matrix (free dofs,
+// kind < 0); periodic: all dofs, constant null space.  Returns a handle.
+void *or_amg_setup(void *h, const int64_t *kind, int32_t periodic, int32_t nthreads) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    const int nt = std::max(1, nthreads);
+    OracleAmg *M = new OracleAmg;
+    M->periodic = periodic;
+    M->red_of.assign(o.ndof, -1);
+    for (int64_t i = 0; i < o.ndof; ++i)
+        if (periodic || kind[i] < 0) { M->red_of[i] = (int64_t)M->free_of.size(); M->free_of.push_back(i); }
+    Csr A;
+    A.n = A.m = (int64_t)M->free_of.size();
+    A.ptr.assign(A.n + 1, 0);
+    for (int64_t r = 0; r < A.n; ++r) {
+        const int64_t i = M->free_of[r];
+        for (int64_t k = o.rowptr[i]; k < o.rowptr[i + 1]; ++k) {
+            const int64_t c = M->red_of[o.col[k]];
+            if (c >= 0 && o.K[k] != 0.0) { A.col.push_back(c); A.val.push_back(o.K[k]); }
+        }
+        A.ptr[r + 1] = (int64_t)A.col.size();
+    }
+    for (;;) {
+        AmgLevel L;
+        L.A = std::move(A);
+        const int64_t n = L.A.n;
+        std::vector<double> diag(n, 0.0);
+        for (int64_t i = 0; i < n; ++i)
+            for (int64_t k = L.A.ptr[i]; k < L.A.ptr[i + 1]; ++k)
+                if (L.A.col[k] == i) diag[i] = L.A.val[k];
+        L.dinv.resize(n);
+        for (int64_t i = 0; i < n; ++i) L.dinv[i] = diag[i] != 0.0 ? 1.0 / diag[i] : 1.0;
+        L.x.assign(n, 0.0); L.b.assign(n, 0.0); L.r.assign(n, 0.0);
+        if (n <= 400 || M->lev.size() >= 12) { M->lev.push_back(std::move(L)); break; }
+        int64_t na = 0;
+        const double theta = 0.08 * std::pow(0.5, (double)M->lev.size());
+        const std::vector<int64_t> agg = aggregate(L.A, diag, theta, na);
+        if (na >= n) { M->lev.push_back(std::move(L)); break; }
+        // lambda_max(D^-1 A) by power iteration
+        std::vector<double> v(n), t(n);
+        for (int64_t i = 0; i < n; ++i) v[i] = 1.0 + 0.5 * std::sin(0.7 * (double)i);
+        double lam = 1.0;
+        for (int it = 0; it < 20; ++it) {
+            csr_matvec(L.A, v.data(), t.data(), nt);
+            double num = 0.0, den = 0.0;
+            for (int64_t i = 0; i < n; ++i) { t[i] *= L.dinv[i]; num += t[i] * t[i]; den += v[i] * v[i]; }
+            lam = std::sqrt(num / den);
+            const double s = 1.0 / std::sqrt(num);
+            for (int64_t i = 0; i < n; ++i) v[i] = t[i] * s;
+        }
+        const double omega = 4.0 / (3.0 * lam);
+        L.omega = omega;
+        // P = (I - omega D^-1 A) P0
+        Csr P0;
+        P0.n = n; P0.m = na;
+        P0.ptr.resize(n + 1);
+        P0.col.resize(n);
+        P0.val.assign(n, 1.0);
+        for (int64_t i = 0; i < n; ++i) { P0.ptr[i] = i; P0.col[i] = agg[i]; }
+        P0.ptr[n] = n;
+        Csr S = L.A;
+        for (int64_t i = 0; i < n; ++i)
+            for (int64_t k = S.ptr[i]; k < S.ptr[i + 1]; ++k) {
+                S.val[k] *= -omega * L.dinv[i];
+                if (S.col[k] == i) S.val[k] += 1.0;
+            }
+        L.P = csr_matmul(S, P0, nt);
+        L.R = csr_transpose(L.P);
+        Csr AP = csr_matmul(L.A, L.P, nt);
+        A = csr_matmul(L.R, AP, nt);
+        M->lev.push_back(std::move(L));
+    }
+    // dense Cholesky of the coarsest operator (periodic: + mean(diag)/n 11^T)
+    const Csr &C = M->lev.back().A;
+    const int64_t n = C.n;
+    M->nc = n;
+    std::vector<double> D(n * n, 0.0);
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t k = C.ptr[i]; k < C.ptr[i + 1]; ++k) D[i * n + C.col[k]] += C.val[k];
+    if (periodic) {
+        double tr = 0.0;
+        for (int64_t i = 0; i < n; ++i) tr += D[i * n + i];
+        const double d = tr / ((double)n * (double)n);
+        for (double &x : D) x += d;
+    }
+    for (int64_t j = 0; j < n; ++j) {
+        double s = D[j * n + j];
+        for (int64_t k = 0; k < j; ++k) s -= D[j * n + k] * D[j * n + k];
+        if (!(s > 0.0)) { delete M; return nullptr; }
+        D[j * n + j] = std::sqrt(s);
+        for (int64_t i = j + 1; i < n; ++i) {
+            double t = D[i * n + j];
+            for (int64_t k = 0; k < j; ++k) t -= D[i * n + k] * D[j * n + k];
+            D[i * n + j] = t / D[j * n + j];
+        }
+    }
+    M->chol = std::move(D);
+    return M;
+}
+
+int32_t or_amg_levels(void *amg, int64_t *rows, int32_t cap) {
+    const OracleAmg &M = *static_cast<OracleAmg *>(amg);
+    for (int32_t l = 0; l < (int32_t)M.lev.size() && l < cap; ++l) rows[l] = M.lev[l].A.n;
+    return (int32_t)M.lev.size();
+}
+
+void or_amg_free(void *amg) { delete static_cast<OracleAmg *>(amg); }
+
+// CG preconditioned by one V-cycle of the hierarchy, with the stopping test
+// and conventions of or_pcg.  Returns the iteration count, or -1.
+int32_t or_amg_pcg(void *h, void *amg, const double *b_in, const int64_t *kind, const double *gval, double *x,
+                   double rtol, double atol, int32_t max_iter, int32_t remove_mean, int32_t nthreads) {
+    const Oracle &o = *static_cast<Oracle *>(h);
+    OracleAmg &M = *static_cast<OracleAmg *>(amg);
+    const int nt = std::max(1, nthreads);
+    const int64_t n = o.ndof;
+    std::vector<double> b(b_in, b_in + n), r(n), z(n), p(n, 0.0), Ap(n);
+    std::vector<AmgLevel> &lev = M.lev;
+    auto matvec = [&](const std::vector<double> &v, std::vector<double> &out) {
+        for_cells(n, nt, [&](int64_t rb, int64_t re, int) {
+            for (int64_t i = rb; i < re; ++i) {
+                if (M.red_of[i] < 0) { out[i] = v[i]; continue; }
+                double s = 0.0;
+                for (int64_t k = o.rowptr[i]; k < o.rowptr[i + 1]; ++k)
+                    if (M.red_of[o.col[k]] >= 0) s += o.K[k] * v[o.col[k]];
+                out[i] = s;
+            }
+        });
+    };
+    auto precond = [&]() {
+        const int64_t nf = (int64_t)M.free_of.size();
+        for (int64_t q = 0; q < nf; ++q) lev[0].b[q] = r[M.free_of[q]];
+        amg_vcycle(M, lev, 0, nt);
+        for (int64_t i = 0; i < n; ++i) z[i] = M.red_of[i] < 0 ? r[i] : lev[0].x[M.red_of[i]];
+        if (M.periodic) {
+            double s = 0.0;
+            for (double v : z) s += v;
+            for (double &v : z) v -= s / n;
+        }
+    };
+    for (int64_t i = 0; i < n; ++i)
+        if (M.red_of[i] < 0) x[i] = gval[i];
+    if (remove_mean) {
+        double s = 0.0;
+        for (double v : b) s += v;
+        for (double &v : b) v -= s / n;
+    }
+    std::vector<double> xv(x, x + n);
+    matvec(xv, Ap);
+    double rr = 0, bb = 0;
+    for (int64_t i = 0; i < n; ++i) { r[i] = M.red_of[i] < 0 ? 0.0 : b[i] - Ap[i]; rr += r[i] * r[i]; bb += b[i] * b[i]; }
+    const double tol = std::max(rtol * std::sqrt(bb), atol);
+    int it = 0;
+    double rz = 0.0, beta = 0.0;
+    while (std::sqrt(rr) > tol && it < max_iter) {
+        precond();
+        double rzn = 0.0;
+        for (int64_t i = 0; i < n; ++i) rzn += r[i] * z[i];
+        beta = it == 0 ? 0.0 : rzn / rz;
+        rz = rzn;
+        ++it;
+        for (int64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+        matvec(p, Ap);
+        double pap = 0;
+        for (int64_t i = 0; i < n; ++i) if (M.red_of[i] >= 0) pap += p[i] * Ap[i];
+        if (!(pap > 0)) return -1;
+        const double alpha = rz / pap;
+        rr = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            if (M.red_of[i] < 0) continue;
+            xv[i] += alpha * p[i];
+            r[i] -= alpha * Ap[i];
+            rr += r[i] * r[i];
+        }
+    }
+    if (remove_mean) {
+        double s = 0.0;
+        for (double v : xv) s += v;
+        for (double &v : xv) v -= s / n;
+    }
+    std::copy(xv.begin(), xv.end(), x);
+    return std::sqrt(rr) <= tol ? it : -1;
+}
+
 // b = M rho (full mass matrix, no boundary conditions).
 void or_mass_matvec(void *h, const double *rho, double *b) {
     const Oracle &o = *static_cast<Oracle *>(h);

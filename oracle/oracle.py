@@ -51,6 +51,11 @@ _SIG = {
     "or_image_charges": ([C.c_void_p, _D, C.c_int32, _D], None),
     "or_pcg": ([C.c_void_p, _D, _I64, _D, _D, C.c_double, C.c_double, C.c_int32, C.c_int32, C.c_int32], C.c_int32),
     "or_mass_matvec": ([C.c_void_p, _D, _D], None),
+    "or_amg_setup": ([C.c_void_p, _I64, C.c_int32, C.c_int32], C.c_void_p),
+    "or_amg_levels": ([C.c_void_p, _I64, C.c_int32], C.c_int32),
+    "or_amg_free": ([C.c_void_p], None),
+    "or_amg_pcg": ([C.c_void_p, C.c_void_p, _D, _I64, _D, _D, C.c_double, C.c_double, C.c_int32, C.c_int32,
+                    C.c_int32], C.c_int32),
     "or_create_flux": ([C.c_void_p, _D, C.c_int32], None),
     "or_inject": ([C.c_void_p, C.c_double, C.c_uint64, C.c_uint64, _I64], C.c_int64),
     "or_n_ext_facets": ([C.c_void_p], C.c_int64),
@@ -118,6 +123,9 @@ class Oracle:
         self.species = []   # (q, m) in first-use order, like the engine
 
     def __del__(self):
+        for h in getattr(self, "_amg", {}).values():
+            lib().or_amg_free(h)
+        self._amg = {}
         if getattr(self, "h", None):
             lib().or_free(self.h)
             self.h = None
@@ -314,6 +322,42 @@ class Oracle:
         if it < 0:
             raise RuntimeError("oracle PCG did not converge")
         return x, int(it)
+
+    def poisson_amg(self, rho, potentials=None, periodic=False, x0=None, rtol=1e-12, atol=1e-14, max_iter=1000,
+                    nthreads=1):
+        """CG preconditioned by a smoothed-aggregation AMG V-cycle (the
+        reference's solver class: PETSc + hypre AMG, punc/src/poisson.cpp:297-304)
+        on the system of poisson_pcg.  The hierarchy is built on the first
+        call (per periodic flag) and kept.  Returns (x, iterations)."""
+        kind, g = self.dirichlet(periodic)
+        if potentials is not None:
+            for k, p in enumerate(potentials):
+                g[kind == k + 1] = p
+        key = bool(periodic)
+        if not hasattr(self, "_amg"):
+            self._amg = {}
+        if key not in self._amg:
+            h = lib().or_amg_setup(self.h, _l(kind), 1 if periodic else 0, nthreads)
+            if not h:
+                raise RuntimeError("oracle AMG set-up failed")
+            self._amg[key] = h
+        K, M = self.matrices()
+        b = np.zeros(self.ndof)
+        lib().or_mass_matvec(self.h, _d(np.asarray(rho, float)), _d(b))
+        free = (kind < 0) | bool(periodic)
+        bcv = np.where(free, 0.0, g)
+        b = np.where(free, b - K @ bcv, g)
+        x = np.zeros(self.ndof) if x0 is None else np.array(x0, float)
+        it = lib().or_amg_pcg(self.h, self._amg[key], _d(b), _l(kind), _d(g), _d(x), rtol, atol, max_iter,
+                              1 if periodic else 0, nthreads)
+        if it < 0:
+            raise RuntimeError("oracle AMG-PCG did not converge")
+        return x, int(it)
+
+    def amg_levels(self, periodic=False):
+        rows = np.zeros(16, np.int64)
+        n = lib().or_amg_levels(self._amg[bool(periodic)], _l(rows), 16)
+        return rows[:n].tolist()
 
     # ---- injection ------------------------------------------------------------
     def create_flux(self, species):

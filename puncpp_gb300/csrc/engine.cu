@@ -1820,6 +1820,25 @@ int pg_update(pg_sim *s, pg_object *objects, int32_t n_objects, double dt) {
     return PG_OK;
 }
 
+int pg_absorbed_counts(pg_sim *s, int64_t *counts, int32_t n_tags, int32_t n_species, double *q, double *m,
+                       int32_t *n_species_out) {
+    if (!s || n_tags < 0 || n_tags > kMaxTags || n_species < 0)
+        return fail(PG_ERR_ARG, "pg_absorbed_counts: bad arguments");
+    if (n_species_out) *n_species_out = s->n_species;
+    if (counts && n_tags > 0 && n_species > 0) {
+        int64_t tally[kMaxTags][kMaxSpecies];
+        PG_CUDA(cudaStreamSynchronize(s->stream));
+        PG_CUDA(cudaMemcpy(tally, s->state->absorbed, sizeof(tally), cudaMemcpyDeviceToHost));
+        for (int t = 0; t < n_tags; ++t)
+            for (int k = 0; k < n_species; ++k) counts[(size_t)t * n_species + k] = k < kMaxSpecies ? tally[t][k] : 0;
+    }
+    for (int k = 0; k < n_species; ++k) {
+        if (q) q[k] = k < s->n_species ? s->q[k] : 0.0;
+        if (m) m[k] = k < s->n_species ? s->m[k] : 0.0;
+    }
+    return PG_OK;
+}
+
 int pg_kinetic_energy(pg_sim *s, double *KE) {
     if (!s || !KE) return fail(PG_ERR_ARG, "pg_kinetic_energy: NULL argument");
     double hm[kMaxSpecies] = {0};

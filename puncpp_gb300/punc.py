@@ -368,6 +368,22 @@ def distribute_cg1(pop: Population, rho: Function | None = None, dv_inv=None) ->
     return out
 
 
+def absorbed_counts(pop: Population, n_tags: int = 0):
+    """The last update's absorbed particles per boundary tag and species
+    (pg_absorbed_counts; Population::update sums them over the species into
+    each object's current): (counts [n_tags][n_species], q [n_species],
+    m [n_species]); n_tags 0: exterior and every object tag."""
+    lib = L.load()
+    ns = C.c_int32()
+    L.check(lib.pg_absorbed_counts(pop.handle, None, 0, 0, None, None, C.byref(ns)))
+    k = ns.value
+    t = n_tags or pop.mesh.num_objects + 2
+    counts = np.zeros((t, k), np.int64)
+    q, m = np.zeros(k), np.zeros(k)
+    L.check(lib.pg_absorbed_counts(pop.handle, L.i64ptr(counts), t, k, L.dptr(q), L.dptr(m), C.byref(ns)))
+    return counts, q, m
+
+
 def kinetic_energy(pop: Population) -> float:
     ke = C.c_double()
     L.check(L.load().pg_kinetic_energy(pop.handle, C.byref(ke)))

@@ -122,15 +122,26 @@ def test_probe_80_fused_steps_in_lockstep(lib, oracle_mod, capsys):
         absorbed = o.update(oobjs, bench.DT, nth)
         assert res.n_absorbed == absorbed.sum() > 0
         assert oobjs[0]["current"] != 0.0 and rel(objs[0].current, oobjs[0]["current"]) < RTOL, n
+        # the tally per boundary tag and species: its sums over the species are
+        # the oracle's per-tag counts, and the object's share per species adds
+        # up to the object current
+        counts, qs, _ = punc.absorbed_counts(pop)
+        assert np.array_equal(counts.sum(axis=1), absorbed[:counts.shape[0]]), n
+        per_species = counts[2] * qs / bench.DT
+        assert rel(per_species.sum(), objs[0].current) < RTOL, n
+        collected = per_species if n == 0 else collected + per_species
         ko, _ = o.inject(bench.DT, seed, n)
         assert res.n_injected == ko > 0
         a = pop.particles()
         b = o.particles()
         compare_particles(a, b)
         assert res.n_particles == len(b["id"])
-        rows.append((n, res.n_particles, res.n_absorbed, res.n_injected, objs[0].current, err_phi, err_q))
+        rows.append((n, res.n_particles, res.n_absorbed, res.n_injected, per_species[0], per_species[1], err_phi,
+                     err_q))
+    assert np.all(collected != 0.0)      # both species reach the object
     with capsys.disabled():
-        print("\nprobe-80, FP64 engine vs oracle (step, N, absorbed, injected, object current, phi err, charge err):")
+        print("\nprobe-80, FP64 engine vs oracle (step, N, absorbed, injected, object current of electrons, of ions, "
+              "phi err, charge err):")
         for r in rows:
-            print("  %d  %d  %d  %d  %.12e  %.1e  %.1e" % r)
+            print("  %d  %d  %d  %d  %.12e  %.12e  %.1e  %.1e" % r)
     pop.close()
