@@ -1,12 +1,17 @@
 #!/usr/bin/env python3
 """Benchmark of the PUNC++ per-timestep particle path on one GB300.
 
-Workload (the spherical-probe configuration): cube [-10,10]^3 of 80^3 sub-cubes
-x 6 Kuhn tetrahedra, cells with centroid inside r = 1 removed (the object),
-2M electrons (m = 1) and 2M ions (m = 1836), Maxwellian with T_e = T_i,
-lambda_D = omega_pe = 1, the object held at -2 kT/e by a CircuitCM voltage
-source, shifted-Maxwellian flux injection on the outer faces, absorption at the
-object and the outer boundary, dt = 0.05.  Inputs are seeded synthetic data.
+Headline workload (the mixed-precision configuration): the spherical probe,
+cube [-10,10]^3 of 120^3 sub-cubes x 6 Kuhn tetrahedra (10.4M cells, 1.77M
+dofs), cells with centroid inside r = 1 removed (the object), 10M electrons
+(m = 1) and 10M ions (m = 1836), Maxwellian with T_e = T_i, lambda_D = omega_pe
+= 1, the object held at -2 kT/e by a CircuitCM voltage source,
+shifted-Maxwellian flux injection on the outer faces, absorption at the object
+and the outer boundary, dt = 0.05; mixed form, with the FP64 form of the same
+workload beside it and the errors of the mixed form against the FP64 run from
+the same seed.  `--workload config3-40` is the same at 40^3; `probe-80` is the
+FP64 probe configuration (80^3, 2M + 2M particles).  Inputs are seeded
+synthetic data.
 
 A step is one full timestep (interaction/interaction.cpp:342-480): deposit,
 Poisson + circuit (one AMG-PCG solve; the object potential enters by
@@ -35,10 +40,14 @@ METRIC = "particle-steps/s on 1 GB300: mixed-precision vs FP64 form at ≤1e-5 r
 UNIT = "particle-steps/s"
 HALF, RADIUS = 10.0, 1.0
 N_SIDE, N_PER_SPECIES = 80, 2_000_000   # the probe configuration; --workload probe-N scales particles with N^3
+CONFIG3_PER_SPECIES = 10_000_000         # config3-N: the probe at N^3 with 20M particles
+LONG_STEPS = 500                          # the probe configuration's run length
+INJECT_SEED = 0x5EED0002
 
 
 def workload_name(n_side, n_per):
-    return (f"probe-{n_side}: [-10,10]^3, {n_side}^3x6 Kuhn tets minus centroid r<1 (object), "
+    label = f"config3-{n_side}" if n_per == CONFIG3_PER_SPECIES else f"probe-{n_side}"
+    return (f"{label}: [-10,10]^3, {n_side}^3x6 Kuhn tets minus centroid r<1 (object), "
             f"{n_per / 1e6:g}M e- + {n_per / 1e6:g}M ions (m_i=1836), Maxwellian T_e=T_i, CM bias -2 kT/e, "
             f"flux injection, dt=0.05, Poisson rtol 1e-10 atol 1e-12")
 
@@ -166,7 +175,7 @@ def run_ours(args):
 
     def one(first=False):
         nonlocal step_no, n_now
-        r = punc.step(pop, objs, DT, first_step=first, inject=True, seed=0x5EED0002, step_no=step_no,
+        r = punc.step(pop, objs, DT, first_step=first, inject=True, seed=INJECT_SEED, step_no=step_no,
                       efield_cg1=args.efield == "cg1")
         step_no += 1
         pushed = n_now
@@ -176,20 +185,18 @@ def run_ours(args):
     clk = ClockSampler().__enter__()
     for k in range(max(3, args.warmup)):
         one(first=(k == 0))
-        if k == 0:
-            rho_first = punc.Function(pop, "rho").vector()
     cg1 = args.efield == "cg1"
     graph = args.step_mode == "graph"
     tuning = None
     if args.autotune:
         # the autotuner's steps are part of the warm-up
-        tuning = punc.autotune(pop, objs, DT, steps_per_trial=2, inject=True, seed=0x5EED0002, step_no=step_no,
+        tuning = punc.autotune(pop, objs, DT, steps_per_trial=2, inject=True, seed=INJECT_SEED, step_no=step_no,
                                efield_cg1=cg1)
         step_no += (24 if prec == L.PG_MIXED else 12) * 2 + 41
         n_now = pop.num_of_particles()
     if args.step_mode != "staged":
         # capture the step graph (and run one more warm-up step) outside the timed region
-        rs = punc.run_steps(pop, objs, DT, 1, inject=True, seed=0x5EED0002, step_no=step_no, efield_cg1=cg1,
+        rs = punc.run_steps(pop, objs, DT, 1, inject=True, seed=INJECT_SEED, step_no=step_no, efield_cg1=cg1,
                             use_graph=graph)
         step_no += 1
         n_now = rs[-1].n_particles
@@ -197,6 +204,7 @@ def run_ours(args):
     launches0 = launch_count()
     pushed_total = 0
     iters = 0
+    first_timed = step_no
     L.check(lib.pg_event_record(pop.handle, 0))
     t_wall = time.perf_counter()
     t_start = t_wall
@@ -208,13 +216,14 @@ def run_ours(args):
             pushed_total += pushed
             iters += r.pcg_iterations
     else:
-        rs = punc.run_steps(pop, objs, DT, args.steps, inject=True, seed=0x5EED0002, step_no=step_no,
+        rs = punc.run_steps(pop, objs, DT, args.steps, inject=True, seed=INJECT_SEED, step_no=step_no,
                             efield_cg1=cg1, use_graph=graph)
         step_no += args.steps
         pushed_total = n_now + sum(r.n_particles for r in rs[:-1])
         n_now = rs[-1].n_particles
         iters = sum(r.pcg_iterations for r in rs)
     L.check(lib.pg_event_record(pop.handle, 1))
+    last_timed = step_no - 1
     ms = ctypes_ms(lib, pop, 0, 1)
     t_wall = time.perf_counter() - t_wall
     clk.window = (t_start, t_start + t_wall)
@@ -247,7 +256,7 @@ def run_ours(args):
         if args.step_mode == "staged":
             r, pushed = one()
         else:
-            r = punc.run_steps(pop, objs, DT, 1, inject=True, seed=0x5EED0002, step_no=step_no, efield_cg1=cg1,
+            r = punc.run_steps(pop, objs, DT, 1, inject=True, seed=INJECT_SEED, step_no=step_no, efield_cg1=cg1,
                                use_graph=graph)[0]
             step_no += 1
             pushed, n_now = n_now, r.n_particles
@@ -255,6 +264,25 @@ def run_ours(args):
         L.check(lib.pg_get_phi(pop.handle, L.dptr(phi_host)))
     L.check(lib.pg_synchronize(pop.handle))
     e2e_s = time.perf_counter() - t0
+
+    # long run: args.long_steps consecutive steps (the probe configuration's
+    # length), device-timed like the headline
+    long_run = None
+    if args.long_steps > 0 and args.step_mode != "staged":
+        n_first = n_now
+        L.check(lib.pg_event_record(pop.handle, 2))
+        rl = punc.run_steps(pop, objs, DT, args.long_steps, inject=True, seed=INJECT_SEED, step_no=step_no,
+                            efield_cg1=cg1, use_graph=graph)
+        L.check(lib.pg_event_record(pop.handle, 3))
+        ms_long = ctypes_ms(lib, pop, 2, 3)
+        pushed_long = n_now + sum(r.n_particles for r in rl[:-1])
+        long_run = {"steps": args.long_steps, "first_step": step_no, "value": round(pushed_long / (ms_long / 1e3), 1),
+                    "unit": UNIT, "ms_per_step": round(ms_long / args.long_steps, 4),
+                    "particles_first": n_first, "particles_last": rl[-1].n_particles,
+                    "pcg_iterations_per_step": round(sum(r.pcg_iterations for r in rl) / args.long_steps, 2),
+                    "timing": "CUDA events on the engine stream around one pg_run_steps call (captured step graph)"}
+        step_no += args.long_steps
+        n_now = rl[-1].n_particles
     import ctypes as C
     h2d = C.sizeof(L.StepArgs) + C.sizeof(L.Object) * len(objs)
     d2h = phi_host.nbytes + C.sizeof(L.StepResult) + C.sizeof(L.Object) * len(objs)
@@ -328,7 +356,9 @@ def run_ours(args):
                    "step_mode": args.step_mode, "tuning": tuning, "cells": nc, "dofs": nv, "nnz": nnz,
                    "amg_levels": [[v["rows"], v["nnz"]] for v in lay["levels"]], "particles_initial": n0,
                    "particles_mean_pushed": round(n_avg), "pcg_iterations_per_step": round(iters / args.steps, 1),
-                   "l2": "inputs larger than L2 (particle SoA ~250 MB, mesh tables ~0.9 GB)"},
+                   "first_timed_step": first_timed, "last_timed_step": last_timed,
+                   "l2": f"inputs larger than L2 (129 MB): particle records {(28 if mixed else 52) * n_avg / 1e6:.0f} MB, "
+                         f"cell tables {(80 if mixed else 288) * nc / 1e6:.0f} MB per pass"},
         "particle_stages": particle_stages,
         "stage_ms_per_step": {k: round(v, 4) for k, v in per_step.items()},
         "stage_share": stages_share, "stage_source": ("the timed steps" if args.step_mode == "staged"
@@ -341,9 +371,91 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "wall_s_timed": round(t_wall, 3),
+        "long_run": long_run,
     }
     pop.close()
-    return out, rho_first
+    return out
+
+
+def error_record(args, n_steps):
+    """The mixed form against the FP64 form from the same seeded start and
+    injection streams, in lockstep over n_steps fused steps (the steps the
+    timed runs went through, and at least the probe configuration's 500):
+    per step the charge density error in the L2 norm and the max-norm over
+    dofs, the potential error, and whether the step is a boundary event (the
+    forms' absorbed or injected counts, particle counts or object current
+    differ: a particle within rounding distance of a boundary absorbed by one
+    form and kept by the other).  The collected current per species (the
+    object's share of each species' absorbed tally, over dt) is averaged over
+    the run for both forms."""
+    import numpy as np
+
+    from puncpp_gb300 import _lib as L
+    from puncpp_gb300 import punc
+    ma, species, loads = make_workload(args.n_side, args.n_per)
+    mesh = punc.Mesh(ma)
+    runs = {}
+    for prec in (L.PG_FP64, L.PG_MIXED):
+        pop = punc.Population(mesh, precision=prec, capacity=int(2.6 * args.n_per * 2), pcg_rtol=RTOL, pcg_atol=ATOL,
+                              pcg_max_iter=4000, pcg_precond=PRECONDS[args.pcg_precond],
+                              warm_start=2 if args.warm_start == "extrapolate" else 1)
+        for s, (x, v) in zip(species, loads):
+            pop.add_particles(x, v, s["q"], s["m"])
+        punc.create_flux(pop, [punc.Species(s["q"], s["m"], n=s["n"], vth=s["vth"]) for s in species])
+        objs = [punc.Object(2)]
+        punc.CircuitCM(pop, objs, [(-1, 0, BIAS)], [], DT)
+        runs[prec] = (pop, objs)
+    l2, mx, phi_err, events = [], [], [], []
+    cur = {L.PG_FP64: [], L.PG_MIXED: []}
+    qs = None
+    for n in range(n_steps):
+        res = {}
+        for prec, (pop, objs) in runs.items():
+            res[prec] = punc.step(pop, objs, DT, first_step=(n == 0), inject=True, seed=INJECT_SEED, step_no=n,
+                                  efield_cg1=args.efield == "cg1")
+            counts, qs, _ = punc.absorbed_counts(pop)
+            cur[prec].append(counts[2] * qs / DT)
+        (p64, o64), (p32, o32) = runs[L.PG_FP64], runs[L.PG_MIXED]
+        r64, r32 = punc.Function(p64, "rho").vector(), punc.Function(p32, "rho").vector()
+        f64, f32 = punc.Function(p64, "phi").vector(), punc.Function(p32, "phi").vector()
+        d = r32 - r64
+        l2.append(float(np.linalg.norm(d) / np.linalg.norm(r64)))
+        mx.append(float(np.abs(d).max() / np.abs(r64).max()))
+        phi_err.append(float(np.abs(f32 - f64).max() / np.abs(f64).max()))
+        a, b = res[L.PG_FP64], res[L.PG_MIXED]
+        events.append(bool(a.n_absorbed != b.n_absorbed or a.n_injected != b.n_injected
+                           or a.n_particles != b.n_particles or not np.array_equal(cur[L.PG_FP64][-1], cur[L.PG_MIXED][-1])))
+    for pop, _ in runs.values():
+        pop.close()
+    l2, mx, ev = np.array(l2), np.array(mx), np.array(events)
+    quiet = ~ev
+
+    def first_over(a, bar=1e-5):
+        k = np.nonzero(quiet & (a > bar))[0]
+        return int(k[0]) if len(k) else None
+
+    names = ["electrons" if q < 0 else "ions" for q in qs]
+    cur_mean = {form: {nm: float(np.mean([c[k] for c in cur[prec]])) for k, nm in enumerate(names)}
+                for form, prec in (("fp64", L.PG_FP64), ("mixed", L.PG_MIXED))}
+    return {
+        "steps": n_steps, "bar": 1e-5, "event_steps": int(ev.sum()),
+        "step0": {"l2": float(l2[0]), "max": float(mx[0]),
+                  "what": "the first deposit: the same loaded particles, FP32 positions and fixed-point sums "
+                          "against FP64"},
+        "non_event_steps": {"l2_max": float(l2[quiet].max()), "max_max": float(mx[quiet].max()),
+                            "first_above_bar_l2": first_over(l2), "first_above_bar_max": first_over(mx),
+                            "l2_median": float(np.median(l2[quiet]))},
+        "event_step_l2_max": float(l2[ev].max()) if ev.any() else None,
+        "phi_max_err": float(max(phi_err)),
+        "per_step_l2": [float("%.3g" % v) for v in l2], "per_step_max": [float("%.3g" % v) for v in mx],
+        "event_step_indices": [int(k) for k in np.nonzero(ev)[0]],
+        "collected_current_per_species": cur_mean,
+        "collected_current_rel_diff": {nm: abs(cur_mean["mixed"][nm] - cur_mean["fp64"][nm]) /
+                                           max(abs(cur_mean["fp64"][nm]), 1e-300) for nm in names},
+        "how": "fresh FP64 and mixed engines, the workload's seeded particles and injection streams, pg_step per step "
+               "(the trajectories of the timed runs: the mixed form is deterministic, the FP64 form's atomics "
+               "reorder sums at 1e-16)",
+    }
 
 
 def pinned_host(n):
@@ -398,7 +510,15 @@ def launch_count():
 
 
 # ---------------------------------------------------------------------------
+CPU_STAGES = ("distributor", "poisson", "efield", "accelerator", "move", "update", "injector")
+PARTICLE_STAGES = ("distributor", "accelerator", "move", "update", "injector")
+
+
 def oracle_workload(nthreads, n_side=N_SIDE, n_per=N_PER_SPECIES):
+    """The workload on the oracle (the reference's algorithm restated in C++),
+    with the Poisson solve by AMG-preconditioned CG (the reference's solver
+    class: Krylov + hypre AMG, punc/src/poisson.cpp:297-304), warm-started
+    from the previous potential, to the bench's tolerances."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
     import oracle as O
@@ -408,66 +528,124 @@ def oracle_workload(nthreads, n_side=N_SIDE, n_per=N_PER_SPECIES):
     for s, (x, v) in zip(species, loads):
         o.add_particles(x, v, s["q"], s["m"])
     o.create_flux(species)
-    state = {"phi": None}
+    state = {"phi": None, "nthreads": nthreads, "iters": 0}
 
     def solve(rho, pots, laplace=False):
         r = np.zeros(o.ndof) if rho is None else rho
-        x, _ = o.poisson_pcg(r, potentials=list(pots), x0=None if laplace else state["phi"], rtol=RTOL, atol=ATOL,
-                             max_iter=4000, nthreads=nthreads)
+        x, it = o.poisson_amg(r, potentials=list(pots), x0=None if laplace else state["phi"], rtol=RTOL, atol=ATOL,
+                              max_iter=4000, nthreads=state["nthreads"])
         if not laplace:
             state["phi"] = x
+            state["iters"] += it
         return x
 
     circ = O.CircuitCM(o, [(-1, 0, BIAS)], [], DT, solve)
     objs = [dict(bnd_id=2, charge=0.0, current=0.0, potential=0.0)]
-    return o, circ, objs
+    return o, circ, objs, state
 
 
-def oracle_step(o, circ, objs, n, nthreads):
-    rho = o.distribute_cg1(nthreads)
-    phi, _ = circ.solve_circuit(rho, objs)
-    E = o.efield(phi)
+def oracle_step(o, circ, objs, n, nthreads, times=None):
+    """One full step on the oracle, stage by stage (the reference Timer's task
+    names, interaction/interaction.cpp:324-334); stage seconds add into times."""
+    T = times if times is not None else {}
+    clock = time.perf_counter
+
+    def tick(name, t0):
+        T[name] = T.get(name, 0.0) + clock() - t0
+
+    t = clock(); rho = o.distribute_cg1(nthreads); tick("distributor", t)
+    t = clock(); phi, _ = circ.solve_circuit(rho, objs); tick("poisson", t)
+    t = clock(); E = o.efield(phi); tick("efield", t)
     pushed = o.num_particles()
-    o.boris(E, (0.0, 0.0, 0.0), DT * (0.5 if n == 0 else 1.0), nthreads)
-    o.move(DT, None, nthreads)
-    o.update(objs, DT, nthreads)
-    o.inject(DT, 0x5EED0002, n)
+    t = clock(); o.boris(E, (0.0, 0.0, 0.0), DT * (0.5 if n == 0 else 1.0), nthreads); tick("accelerator", t)
+    t = clock(); o.move(DT, None, nthreads); tick("move", t)
+    t = clock(); o.update(objs, DT, nthreads); tick("update", t)
+    t = clock(); o.inject(DT, INJECT_SEED, n); tick("injector", t)
     return pushed
 
 
-def cpu_baseline(args, max_seconds=25.0):
+def _rates(pushed, elapsed, times, steps):
+    part = sum(times.get(k, 0.0) for k in PARTICLE_STAGES)
+    return {"value": round(pushed / elapsed, 1), "unit": UNIT,
+            "particle_stages_value": round(pushed / part, 1) if part > 0 else None,
+            "stage_s_per_step": {k: round(times.get(k, 0.0) / steps, 4) for k in CPU_STAGES}}
+
+
+def cpu_baseline(args, budget=30.0):
+    """The oracle on the machine's host cores: all threads on full steps of the
+    workload, then one thread.  A single-threaded full step of a large workload
+    would take minutes, so the single-thread leg times the Poisson solve and the
+    field in full and the particle stages on a subsample of the particles
+    (per-particle rates scaled to the full count)."""
+    import numpy as np
     nthreads = os.cpu_count() or 1
-    o, circ, objs = oracle_workload(nthreads, args.n_side, args.n_per)
-    oracle_step(o, circ, objs, 0, nthreads)         # first step (half push) untimed
-    pushed, t0, n = 0, time.perf_counter(), 1
+    o, circ, objs, state = oracle_workload(nthreads, args.n_side, args.n_per)
+    oracle_step(o, circ, objs, 0, nthreads)          # first step (half push, AMG set-up) untimed
+    times, pushed, steps, n = {}, 0, 0, 1
+    state["iters"] = 0
+    t0 = time.perf_counter()
     while True:
-        pushed += oracle_step(o, circ, objs, n, nthreads)
+        pushed += oracle_step(o, circ, objs, n, nthreads, times)
         n += 1
+        steps += 1
         el = time.perf_counter() - t0
-        if el > max_seconds or n > 6:
+        if el > 0.5 * budget or steps >= 5:
             break
-    return {"value": round(pushed / el, 1), "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{n - 1} full steps of the same probe-{args.n_side} workload on the oracle (C++ restatement, "
-                      f"{nthreads} threads, Jacobi PCG for Poisson), after one untimed step"}
+    allc = _rates(pushed, el, times, steps)
+    allc.update({"cores": nthreads, "steps": steps, "amg_pcg_iterations_per_step": round(state["iters"] / steps, 1)})
+    # one thread: Poisson and field in full, particle stages on a subsample
+    n_full = o.num_particles()
+    p = o.particles(sort=False)
+    k = max(1, int(np.ceil(n_full * sum(times.get(s, 0.0) for s in PARTICLE_STAGES) / steps * nthreads * 0.8
+                           / (0.25 * budget) / n_full))) if n_full else 1
+    t1 = {}
+    state["nthreads"] = 1
+    clock = time.perf_counter
+    rho = o.distribute_cg1(nthreads)
+    t = clock(); phi, _ = circ.solve_circuit(rho, objs); t1["poisson"] = clock() - t
+    t = clock(); E = o.efield(phi); t1["efield"] = clock() - t
+    if k > 1:
+        o.set_particles({key: val[::k] for key, val in p.items()})
+    n_sub = o.num_particles()
+    t = clock(); o.distribute_cg1(1); t1["distributor"] = clock() - t
+    t = clock(); o.boris(E, (0.0, 0.0, 0.0), DT, 1); t1["accelerator"] = clock() - t
+    t = clock(); o.move(DT, None, 1); t1["move"] = clock() - t
+    t = clock(); o.update(objs, DT, 1); t1["update"] = clock() - t
+    t = clock(); o.inject(DT, INJECT_SEED, n); t1["injector"] = clock() - t
+    scale = n_full / max(1, n_sub)
+    for key in ("distributor", "accelerator", "move", "update"):
+        t1[key] *= scale
+    one = _rates(n_full, sum(t1.values()), t1, 1)
+    one.update({"cores": 1, "particle_subsample": f"1/{k}" if k > 1 else "none",
+                "how": "Poisson and field timed on the full mesh; distributor, accelerator, move and update timed on "
+                       "every k-th particle and scaled by k; injector in full"})
+    return {"value": allc["value"], "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{steps} full steps of the same {args.workload} workload on the oracle (the reference's "
+                      f"algorithm restated in C++, {nthreads} threads; Poisson by AMG-preconditioned CG like the "
+                      f"reference's Krylov + hypre AMG) after one untimed step",
+            "all_cores": allc, "single_thread": one}
 
 
 def run_reference(args):
     nthreads = os.cpu_count() or 1
-    o, circ, objs = oracle_workload(nthreads, args.n_side, args.n_per)
+    o, circ, objs, state = oracle_workload(nthreads, args.n_side, args.n_per)
     n = 0
     for _ in range(max(1, args.warmup)):
         oracle_step(o, circ, objs, n, nthreads)
         n += 1
     pushed, t0, done = 0, time.perf_counter(), 0
     budget = 150.0
+    times = {}
+    state["iters"] = 0
     for _ in range(args.steps):
-        pushed += oracle_step(o, circ, objs, n, nthreads)
+        pushed += oracle_step(o, circ, objs, n, nthreads, times)
         n += 1
         done += 1
         if time.perf_counter() - t0 > budget:
             break
     el = time.perf_counter() - t0
-    v = round(pushed / el, 1)
+    rates = _rates(pushed, el, times, done)
+    v = rates["value"]
     return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(el / done * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
@@ -475,8 +653,12 @@ def run_reference(args):
             "config": {"workload": workload_name(args.n_side, args.n_per), "precision": "fp64"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
                              "sample": f"{done} of {args.steps} timed steps (bounded to {budget:.0f} s) of the full "
-                                       f"workload on the oracle, the reference's algorithm restated in C++ (the "
-                                       f"reference needs DOLFIN/PETSc/Boost, absent here)"},
+                                       f"workload on the oracle, the reference's algorithm restated in C++ with its "
+                                       f"solver class (AMG-preconditioned Krylov) for Poisson (the reference needs "
+                                       f"DOLFIN/PETSc/Boost, absent here)",
+                             "particle_stages_value": rates["particle_stages_value"],
+                             "stage_s_per_step": rates["stage_s_per_step"],
+                             "amg_pcg_iterations_per_step": round(state["iters"] / done, 1)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -561,65 +743,96 @@ def run_langmuir(args):
     return out
 
 
+def batch_plan(R, seed=0x5EED0004):
+    """The bias-sweep configuration's runs: per run r a probe box [-h, h]^3 of
+    n^3 sub-cubes x 6 tetrahedra (n uniform in 30..70) around a sphere of
+    radius 0.5, 1, 2 or 4 Debye lengths, a bias uniform in [-5, 5] kT/e and a
+    particle count uniform in 0.2M..4M (electrons + ions).  All runs share the
+    simulation density (250 particles per species per unit volume, the probe
+    configuration's), so the species are common to all runs and a run's count
+    fixes its box: (2h)^3 - 4/3 pi r^3 = count / 500, with h >= r + 2."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    sides = rng.integers(30, 71, R)
+    radii = rng.choice([0.5, 1.0, 2.0, 4.0], R)
+    biases = rng.uniform(-5.0, 5.0, R)
+    counts = rng.uniform(0.2e6, 4.0e6, R)
+    n_sim = 250.0
+    halves = 0.5 * np.cbrt(counts / (2 * n_sim) + 4.0 / 3.0 * math.pi * radii ** 3)
+    halves = np.maximum(halves, radii + 2.0)
+    return sides, halves, radii, biases, n_sim, rng
+
+
 def run_batch(args):
-    """A batch of independent probe runs in one engine (a scaled bias sweep):
-    run r is the box [-h_r, h_r]^3 (h_r uniform in [6, 10]) of 30..50
-    sub-cubes per side x 6 tetrahedra around a sphere of radius 0.5, 1, 2 or 4,
-    biased uniformly in [-5, 5], with its own injection seed; all runs share
-    the species (simulation density 125 per unit volume: 0.2M..1M particles per
-    species per run).  Every stage is one launch for all runs, each step a
-    captured graph, launch configuration from the autotuner."""
+    """Config: R independent probe runs in one engine (the bias sweep, R = 64
+    by default), each step one launch per stage for all runs, captured as a
+    CUDA graph, launch configuration from the autotuner."""
     import numpy as np
 
     from puncpp_gb300 import _lib as L
     from puncpp_gb300 import batch as B
     from puncpp_gb300 import meshgen, punc
     R = args.runs
-    rng = np.random.default_rng(0x5EED0004)
-    sides = rng.integers(30, 51, R)
-    halves = rng.uniform(6.0, 10.0, R)
-    radii = rng.choice([0.5, 1.0, 2.0, 4.0], R)
-    biases = rng.uniform(-5.0, 5.0, R)
-    n_sim, mi = 125.0, 1836.0
+    t_setup = time.perf_counter()
+    sides, halves, radii, biases, n_sim, rng = batch_plan(R)
+    mi = 1836.0
     w = 1.0 / n_sim
     meshes = [meshgen.probe_box(int(n), float(h), float(r)) for n, h, r in zip(sides, halves, radii)]
     nper = [int(n_sim * ((2 * h) ** 3 - 4.0 / 3.0 * math.pi * r ** 3)) for h, r in zip(halves, radii)]
+    t_mesh = time.perf_counter()
     bt = B.Batch(meshes, precision=L.PG_MIXED, capacity=int(2.6 * 2 * sum(nper)), pcg_rtol=RTOL, pcg_atol=ATOL,
                  pcg_max_iter=4000)
+    t_engine = time.perf_counter()
     species = ((-w, w, 1.0), (w, mi * w, 1.0 / math.sqrt(mi)))
+    loaded = []
     for r in range(R):
         h = halves[r]
+        box = (2 * h) ** 3
+        k = 0
         for q, m_, vth in species:
-            xs = -h + rng.random((int(nper[r] * (2 * h) ** 3 / ((2 * h) ** 3 - 4.0 / 3.0 * math.pi * radii[r] ** 3)) + 1,
-                                  3)) * (2 * h)
-            bt.add_particles(r, xs, rng.normal(0.0, vth, xs.shape), q, m_)
+            xs = -h + rng.random((int(nper[r] * box / (box - 4.0 / 3.0 * math.pi * radii[r] ** 3)) + 1, 3)) * (2 * h)
+            k += bt.add_particles(r, xs, rng.normal(0.0, vth, xs.shape), q, m_)
+        loaded.append(k)
     bt.create_flux([punc.Species(q, m_, n=n_sim, vth=vth) for q, m_, vth in species],
                    seeds=[0x5EED0004 + r for r in range(R)])
     objs = bt.objects()
     bt.circuit(objs, biases, DT)
     pop = bt.pop
     lib = L.load()
+    t_loaded = time.perf_counter()
     punc.run_steps(pop, objs, DT, args.warmup, first_step=True, inject=True, seed=0x5EED0004)
     tuning = punc.autotune(pop, objs, DT, steps_per_trial=2, inject=True, seed=0x5EED0004, step_no=args.warmup)
     step_no = args.warmup + (24 * 2 + 41)
     rs0 = punc.run_steps(pop, objs, DT, 1, inject=True, seed=0x5EED0004, step_no=step_no)
     n_now = rs0[-1].n_particles
+    clk = ClockSampler().__enter__()
+    t_w = time.perf_counter()
     ms, rs = _event_ms(lib, pop, lambda: punc.run_steps(pop, objs, DT, args.steps, inject=True, seed=0x5EED0004,
                                                          step_no=step_no + 1))
+    clk.window = (t_w, time.perf_counter())
+    clk.__exit__(None, None, None)
     pushed = n_now + sum(r.n_particles for r in rs[:-1])
     cells = sum(m.n_cells for m in meshes)
+    per_run = bt.particles_per_run()
+    lay = punc.poisson_layout(pop)
+    pop.close()
     return {"metric": "particle-steps/s on 1 GB300 (batched independent probe runs, mixed form)",
             "value": round(pushed / (ms / 1e3), 1), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64",
             "data": "synthetic: seeded Maxwellian loads on generated Kuhn probe meshes",
-            "config": {"workload": f"batch-{R}: {R} probe runs in one engine, boxes [-h,h]^3 (h in [6,10]) of "
-                                   f"30..50 sub-cubes per side x 6, radii in {{0.5,1,2,4}}, biases in [-5,5], "
-                                   f"0.2M..1M particles per species per run, flux injection, dt = 0.05, captured "
-                                   f"step graph",
-                       "runs": R, "cells": cells, "particles_mean_pushed": round(pushed / args.steps),
+            "config": {"workload": f"batch-{R}: {R} probe runs in one engine, boxes [-h,h]^3 of 30..70 sub-cubes per "
+                                   f"side x 6, radii in {{0.5,1,2,4}}, biases in [-5,5], 0.2M..4M particles per run "
+                                   f"(e- + ions, m_i = 1836), flux injection, dt = 0.05, captured step graph",
+                       "runs": R, "cells": cells, "dofs": lay["n_rows"], "particles_loaded": int(sum(loaded)),
+                       "particles_per_run_min_max": [int(per_run.min()), int(per_run.max())],
+                       "sides_min_max": [int(sides.min()), int(sides.max())],
+                       "particles_mean_pushed": round(pushed / args.steps),
                        "pcg_iterations_per_step": round(sum(r.pcg_iterations for r in rs) / args.steps, 1),
-                       "tuning": tuning}}
+                       "tuning": tuning,
+                       "setup_s": {"meshes": round(t_mesh - t_setup, 1), "engine": round(t_engine - t_mesh, 1),
+                                   "particles_flux_circuit": round(t_loaded - t_engine, 1)}},
+            "clocks": clk.summary()}
 
 
 def run_adjoint(args):
@@ -687,9 +900,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"],
                     help="ours: the engine; reference: the reference's algorithm on the host cores")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the timed CPU baseline sample")
-    ap.add_argument("--workload", default="probe-80",
-                    help="probe-N (the headline: N^3 sub-cubes, particles scaled by (N/80)^3), langmuir-N, "
-                         "batch-R (R independent probe runs), adjoint-N")
+    ap.add_argument("--workload", default="config3-120",
+                    help="config3-N (the headline: the probe at N^3 sub-cubes with 20M particles), probe-N (N^3 "
+                         "sub-cubes, 2M + 2M particles scaled by (N/80)^3), langmuir-N, batch-R (R independent "
+                         "probe runs), adjoint-N")
+    ap.add_argument("--long-steps", type=int, default=LONG_STEPS,
+                    help="probe workloads: a further device-timed run of this many consecutive steps (0: none)")
+    ap.add_argument("--error-steps", type=int, default=LONG_STEPS,
+                    help="mixed form: steps of the lockstep error record against the FP64 form (at least the "
+                         "steps the timed runs went through; 0: none)")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
                     help="mixed (the headline form: FP32 particles, fixed-point deposit, mixed PCG) or fp64")
     ap.add_argument("--no-fp64-form", dest="fp64_form", action="store_false",
@@ -705,14 +924,14 @@ def main():
                     help="field path: EFieldDG0 + accel/boris, or ESolver (CG1) + accel_cg1/boris_cg1")
     ap.add_argument("--pcg-precond", default="amg", choices=sorted(PRECONDS),
                     help="Poisson preconditioner: one AMG V-cycle or Jacobi per iteration")
-    ap.add_argument("--runs", type=int, default=16, help="batch-R: runs in the batch (from the workload name)")
+    ap.add_argument("--runs", type=int, default=64, help="batch-R: runs in the batch (from the workload name)")
     ap.add_argument("--adjoint-particles", type=int, default=2_000_000, help="adjoint-N: particles of the run")
     args = ap.parse_args()
     kind = args.workload.split("-")[0]
-    if kind not in ("probe", "langmuir", "batch", "adjoint"):
-        ap.error("--workload must be probe-N, langmuir-N, batch-R or adjoint-N")
+    if kind not in ("config3", "probe", "langmuir", "batch", "adjoint"):
+        ap.error("--workload must be config3-N, probe-N, langmuir-N, batch-R or adjoint-N")
     args.n_side = int(args.workload.split("-")[1])
-    if kind != "probe":
+    if kind not in ("probe", "config3"):
         if kind == "batch":
             args.runs = args.n_side
         if args.impl == "reference":
@@ -721,7 +940,10 @@ def main():
         fn = {"langmuir": run_langmuir, "batch": run_batch, "adjoint": run_adjoint}[kind]
         print(json.dumps(fn(args)))
         return
-    args.n_per = int(round(N_PER_SPECIES * (args.n_side / N_SIDE) ** 3))
+    if kind == "config3":
+        args.n_per = CONFIG3_PER_SPECIES
+    else:
+        args.n_per = int(round(N_PER_SPECIES * (args.n_side / N_SIDE) ** 3))
     if args.warmup < 3:
         args.warmup = 3
     rank = int(os.environ.get("RANK", "0"))
@@ -736,21 +958,21 @@ def main():
         if rank == 0:
             print(json.dumps(run_reference(args)))
         return
-    res, rho_first = run_ours(args)
+    res = run_ours(args)
     if args.precision == "mixed" and args.fp64_form:
-        # the same workload in the FP64 form: its throughput, and the charge
-        # density error of the mixed form after one step from identical particles
+        # the same workload in the FP64 form: its throughput
         import copy
-
-        import numpy as np
         a64 = copy.copy(args)
         a64.precision = "fp64"
-        r64, rho64 = run_ours(a64)
-        d = np.asarray(rho_first) - np.asarray(rho64)
+        r64 = run_ours(a64)
         res["fp64_form"] = {"value": r64["value"], "unit": UNIT, "ms_per_step": r64["ms_per_step"],
                             "pcg_iterations_per_step": r64["config"]["pcg_iterations_per_step"],
                             "e2e": r64["e2e"]["value"], "roofline_particles_frac": r64["roofline_particles"]["frac"],
-                            "particle_stages": r64["particle_stages"]}
+                            "particle_stages": r64["particle_stages"], "long_run": r64["long_run"],
+                            "stage_ms_per_step": r64["stage_ms_per_step"],
+                            "poisson": "the same AMG-preconditioned PCG as the mixed form (FP32 recurrence and "
+                                       "operators, FP64 solution, inner products and true-residual replacement, "
+                                       "FP64 stopping test); the particle arithmetic is FP64"}
         # the full step shares the Poisson solve between the forms; the
         # particle stages (push, move, walk, deposit, injection) are where
         # they differ
@@ -758,9 +980,11 @@ def main():
         if res["particle_stages"]["value"] and r64["particle_stages"]["value"]:
             res["mixed_vs_fp64_particle_stages"] = round(res["particle_stages"]["value"] /
                                                          r64["particle_stages"]["value"], 3)
-        res["rho_rel_err"] = {"l2": float(np.linalg.norm(d) / np.linalg.norm(rho64)),
-                              "max": float(np.abs(d).max() / np.abs(rho64).max()),
-                              "bar": 1e-5, "after": "one step from identical particles and injection streams"}
+        if args.error_steps > 0:
+            # the timed steps of both runs lie inside the first covered steps
+            covered = max(args.error_steps, res["config"]["last_timed_step"] + 1,
+                          r64["config"]["last_timed_step"] + 1)
+            res["rho_rel_err"] = error_record(args, covered)
     if world > 1:
         res = combine_replicas(res, world)
     if rank == 0:

@@ -1,5 +1,5 @@
-"""Batched runs (the bias-sweep configuration, here three runs of different
-mesh sizes, object radii, particle counts, biases and seeds): one engine over
+"""Batched runs (the bias-sweep configuration, here eight runs of different
+mesh sizes, box sizes, object radii, particle counts, biases and seeds): one engine over
 the union mesh against each run done alone.  Injection draws the standalone
 streams, so per run and per step the particle counts, absorbed counts and the
 object's current and charge agree, and the particles agree to the solver's
@@ -15,8 +15,13 @@ pytestmark = pytest.mark.gpu
 
 
 def test_batch_equals_standalone_runs(lib):
-    meshes = [meshgen.probe_box(6, 2.0, 0.6), meshgen.probe_box(5, 2.5, 0.7), meshgen.probe_box(7, 3.0, 0.9)]
-    biases, seeds, npart = [-1.0, -2.5, 0.5], [11, 22, 33], [3000, 5000, 8000]
+    geo = [(6, 2.0, 0.6), (5, 2.5, 0.7), (7, 3.0, 0.9), (4, 2.0, 0.8), (8, 3.5, 1.2), (6, 2.6, 1.0), (9, 4.0, 1.5),
+           (5, 1.8, 0.6)]
+    meshes = [meshgen.probe_box(n, h, r) for n, h, r in geo]
+    biases = [-1.0, -2.5, 0.5, 3.0, -4.0, 1.5, -0.5, 2.0]
+    seeds = [11, 22, 33, 44, 55, 66, 77, 88]
+    npart = [3000, 5000, 8000, 1500, 12000, 4000, 20000, 2500]
+    assert len({m.n_cells for m in meshes}) == len(meshes)
     sp = [punc.Species(-1.0, 1.0, n=20.0, vth=1.0), punc.Species(1.0, 100.0, n=20.0, vth=0.1)]
     dt, steps = 0.1, 5
     cfg = dict(precision=L.PG_MIXED, pcg_rtol=1e-13, pcg_atol=1e-30, pcg_max_iter=4000)
@@ -27,7 +32,7 @@ def test_batch_equals_standalone_runs(lib):
                       (uniform_points(ma, n, rng), maxwellian_velocities(n, 0.1, rng), 1.0, 100.0)])
     # the batch
     b = batch.Batch(meshes, **cfg)
-    added = [[b.add_particles(r, x, v, q, m) for x, v, q, m in loads[r]] for r in range(3)]
+    added = [[b.add_particles(r, x, v, q, m) for x, v, q, m in loads[r]] for r in range(len(meshes))]
     b.create_flux(sp, seeds)
     objs = b.objects()
     b.circuit(objs, biases, dt)

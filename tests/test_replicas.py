@@ -66,3 +66,23 @@ def test_reference_arm_under_torchrun_prints_one_line():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["value"] > 0 and d["cpu_baseline"]["kind"] == "port"
+    st = d["cpu_baseline"]["stage_s_per_step"]
+    assert set(st) == {"distributor", "poisson", "efield", "accelerator", "move", "update", "injector"}
+    assert d["cpu_baseline"]["particle_stages_value"] > d["value"] > 0
+
+
+def test_cpu_baseline_reports_all_cores_and_one_thread():
+    """The CPU baseline of the bench line: all host threads on full steps, and
+    one thread (Poisson in full, particle stages on a subsample), with the
+    stage times of each."""
+    sys.path.insert(0, ROOT)
+    import argparse
+
+    import bench
+    args = argparse.Namespace(n_side=20, n_per=20000, workload="probe-20")
+    cb = bench.cpu_baseline(args, budget=4.0)
+    assert cb["kind"] == "port" and cb["value"] == cb["all_cores"]["value"] > 0
+    for leg in (cb["all_cores"], cb["single_thread"]):
+        assert leg["particle_stages_value"] > leg["value"] > 0
+        assert set(leg["stage_s_per_step"]) == set(bench.CPU_STAGES)
+    assert cb["single_thread"]["cores"] == 1 and cb["all_cores"]["cores"] == (os.cpu_count() or 1)
