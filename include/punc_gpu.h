@@ -222,6 +222,17 @@ int pg_population_load(pg_sim *sim, const char *fname, int32_t binary, int64_t *
 /* Population::locate (punc/src/population.cpp:24-39), for n points. */
 int pg_locate(pg_sim *sim, const double *xs, int64_t n, int64_t *cells);
 
+/* Single-point walks of Population from given cells (no particles move):
+ * mode 0 = relocate_fast (punc/include/punc/population.h:539-569, the first
+ * facet with a positive plane value, the walk of update), mode 1 = relocate
+ * and relocate_stat (population.h:454-538, the facet of the largest plane
+ * value; the walk stays only when every value is negative).  cells_out[i] =
+ * the final cell or -tag of the boundary hit; crossings (optional) = facets
+ * crossed, relocate_stat's count.  A walk at the step limit gives
+ * PG_ERR_WALK_LIMIT. */
+int pg_relocate(pg_sim *sim, const double *xs, const int64_t *cells, int64_t n, int32_t mode, int64_t *cells_out,
+                int32_t *crossings);
+
 /* EFieldDG0::solve (punc/src/efield.cpp:95-99): E = -grad(phi) per cell.
  * phi may be NULL (use the device potential). */
 int pg_efield_dg0(pg_sim *sim, const double *phi);

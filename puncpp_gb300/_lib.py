@@ -131,6 +131,7 @@ SIGNATURES = {
     "pg_move_periodic": ([_P, C.c_double, _D], C.c_int),
     "pg_update": ([_P, C.POINTER(Object), C.c_int32, C.c_double], C.c_int),
     "pg_absorbed_counts": ([_P, _I64, C.c_int32, C.c_int32, _D, _D, _I32], C.c_int),
+    "pg_relocate": ([_P, _D, _I64, C.c_int64, C.c_int32, _I64, _I32], C.c_int),
     "pg_kinetic_energy": ([_P, _D], C.c_int),
     "pg_distribute_cg1": ([_P, _D], C.c_int),
     "pg_set_rho": ([_P, _D], C.c_int),

@@ -1537,6 +1537,42 @@ int pg_locate(pg_sim *s, const double *xs, int64_t n, int64_t *cells) {
     return PG_OK;
 }
 
+int pg_relocate(pg_sim *s, const double *xs, const int64_t *cells, int64_t n, int32_t mode, int64_t *cells_out,
+                int32_t *crossings) {
+    if (!s || (n > 0 && (!xs || !cells || !cells_out)) || n < 0 || (mode != 0 && mode != 1))
+        return fail(PG_ERR_ARG, "pg_relocate: bad arguments");
+    if (n == 0) return PG_OK;
+    std::vector<int32_t> start(n);
+    for (int64_t i = 0; i < n; ++i) {
+        if (cells[i] < 0 || cells[i] >= s->nc) return fail(PG_ERR_ARG, "pg_relocate: start cell out of range");
+        start[i] = (int32_t)cells[i];
+    }
+    double *d_xyz = nullptr;
+    int32_t *d_io = nullptr;
+    PG_CUDA(cudaMalloc(&d_xyz, sizeof(double) * 3 * n));
+    if (cudaMalloc(&d_io, sizeof(int32_t) * 3 * n) != cudaSuccess) {
+        cudaFree(d_xyz);
+        return fail(PG_ERR_CUDA, "pg_relocate: cudaMalloc failed");
+    }
+    std::vector<int32_t> out(2 * n);
+    cudaMemcpyAsync(d_xyz, xs, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->stream);
+    cudaMemcpyAsync(d_io, start.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s->stream);
+    launch_relocate(s->dm, d_xyz, d_io, n, mode, s->cfg.max_walk_steps, d_io + n, d_io + 2 * n, s->stream);
+    cudaMemcpyAsync(out.data(), d_io + n, sizeof(int32_t) * 2 * n, cudaMemcpyDeviceToHost, s->stream);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    cudaFree(d_xyz);
+    cudaFree(d_io);
+    if (e != cudaSuccess) return fail(PG_ERR_CUDA, std::string("pg_relocate: ") + cudaGetErrorString(e));
+    int64_t bad = -1;
+    for (int64_t i = 0; i < n; ++i) {
+        if (out[i] == kWalkFail && bad < 0) bad = i;
+        cells_out[i] = out[i];
+        if (crossings) crossings[i] = out[n + i];
+    }
+    if (bad >= 0) return fail(PG_ERR_WALK_LIMIT, "pg_relocate: walk step limit reached at point " + std::to_string(bad));
+    return PG_OK;
+}
+
 // ESolver::solve (punc/src/efield.cpp:70-75): E = L2 projection of -grad(phi)
 // onto CG1 vector fields, plus the uniform E0, into the packed vertex field.
 // FP64 form: FP64 CG to the reference's tolerances (rel 1e-12, abs 1e-14);

@@ -208,6 +208,45 @@ __global__ void k_locate(DevMesh m, const double *__restrict__ xyz, int64_t n, i
     out[i] = found;
 }
 
+// Single-point walks of Population (punc/include/punc/population.h:454-570)
+// from given cells: mode 0 relocate_fast (the first facet with a positive
+// plane value), mode 1 relocate and relocate_stat (the facet of the largest
+// plane value, the first of equal ones; the walk stays only when every value
+// is negative).  Plane values summed left to right as the reference.
+// out: the final cell or -tag; cross: facets crossed; a walk that reaches
+// max_steps reports kWalkFail.
+__global__ void k_relocate(DevMesh m, const double *__restrict__ xyz, const int32_t *__restrict__ start, int64_t n,
+                           int mode, int max_steps, int32_t *__restrict__ out, int32_t *__restrict__ cross) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+    int c = start[i], k = 0, end = kWalkFail;
+    for (int it = 0; it < max_steps; ++it) {
+        const double *P = m.planes + 16 * (size_t)c;
+        const int4 nb = __ldg(m.nbr + c);
+        const int nbv[4] = {nb.x, nb.y, nb.z, nb.w};
+        double d[4];
+#pragma unroll
+        for (int f = 0; f < 4; ++f) d[f] = plane64(P[4 * f], P[4 * f + 1], P[4 * f + 2], P[4 * f + 3], x, y, z);
+        int f = -1;
+        if (mode == 0) {
+            for (int q = 0; q < 4; ++q)
+                if (d[q] > 0) { f = q; break; }
+        } else {
+            int a = 0;
+            for (int q = 1; q < 4; ++q)
+                if (d[q] > d[a]) a = q;
+            f = d[a] < 0 ? -1 : a;
+        }
+        if (f < 0) { end = c; break; }
+        ++k;
+        if (nbv[f] < 0) { end = nbv[f]; break; }
+        c = nbv[f];
+    }
+    out[i] = end;
+    if (cross) cross[i] = k;
+}
+
 // x <- 2 x - x_prev, x_prev <- old x (linear extrapolation of the last two solutions).
 __global__ void k_extrapolate(double *__restrict__ x, double *__restrict__ x_prev, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -428,6 +467,14 @@ void launch_locate(const DevMesh &m, const double *xyz, int64_t n, int32_t *cell
     if (n <= 0) return;
     count_launches(1);
     k_locate<<<(unsigned)((n + kThreads - 1) / kThreads), kThreads, 0, st>>>(m, xyz, n, cells);
+}
+
+void launch_relocate(const DevMesh &m, const double *xyz, const int32_t *start, int64_t n, int mode, int max_steps,
+                     int32_t *out, int32_t *cross, cudaStream_t st) {
+    if (n <= 0) return;
+    count_launches(1);
+    k_relocate<<<(unsigned)((n + kThreads - 1) / kThreads), kThreads, 0, st>>>(m, xyz, start, n, mode, max_steps, out,
+                                                                            cross);
 }
 
 void launch_scale(const double *a, const double *b, double *out, int64_t n, cudaStream_t st) {

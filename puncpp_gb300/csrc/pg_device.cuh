@@ -312,6 +312,8 @@ void launch_fused_step(const DevMesh &m, const DevParticles &p, int64_t n_slots,
 void launch_kinetic(const DevParticles &p, int64_t n_slots, const double *half_m, double *partials,
                     int nblocks, double *ke_out, cudaStream_t st);
 void launch_locate(const DevMesh &m, const double *xyz, int64_t n, int32_t *cells, cudaStream_t st);
+void launch_relocate(const DevMesh &m, const double *xyz, const int32_t *start, int64_t n, int mode, int max_steps,
+                     int32_t *out, int32_t *cross, cudaStream_t st);
 void launch_scale(const double *a, const double *b, double *out, int64_t n, cudaStream_t st);
 void launch_extrapolate(double *x, double *x_prev, int64_t n, cudaStream_t st);
 

@@ -217,6 +217,18 @@ class Population:
         L.check(L.load().pg_locate(self.handle, L.dptr(xs), xs.shape[0], L.i64ptr(out)))
         return out
 
+    def relocate(self, xs, cells, fast: bool = True, with_crossings: bool = False):
+        """relocate_fast (fast) or relocate / relocate_stat
+        (punc/include/punc/population.h:454-569) of points xs from the given
+        cells: the final cell or -tag per point, and the facets crossed."""
+        xs = np.ascontiguousarray(xs, np.float64).reshape(-1, 3)
+        c0 = np.ascontiguousarray(cells, np.int64).reshape(-1)
+        out = np.zeros(len(c0), np.int64)
+        cr = np.zeros(len(c0), np.int32)
+        L.check(L.load().pg_relocate(self.handle, L.dptr(xs), L.i64ptr(c0), len(c0), 0 if fast else 1,
+                                     L.i64ptr(out), cr.ctypes.data_as(C.POINTER(C.c_int32))))
+        return (out, cr) if with_crossings else out
+
     def _counts(self):
         t, ng, ps = C.c_int64(), C.c_int64(), C.c_int64()
         L.check(L.load().pg_num_particles(self.handle, C.byref(t), C.byref(ng), C.byref(ps)))

@@ -512,3 +512,40 @@ def test_amg_pcg_reports_an_unattainable_tolerance(lib, oracle_mod):
     phi_o, _ = o.poisson_pcg(rho, potentials=[-2.0], rtol=1e-13, atol=1e-30, max_iter=20000, nthreads=8)
     assert rel(phi_g, phi_o) < 1e-9
     pop.close()
+
+
+def _walk_reference(planes, nbr, x, c, fast):
+    """relocate_fast / relocate (punc/include/punc/population.h:454-569) in
+    Python floats: plane value c0 + c1 x + c2 y + c3 z summed left to right."""
+    k = 0
+    while True:
+        P = planes[c]
+        d = [((P[4 * f] + P[4 * f + 1] * x[0]) + P[4 * f + 2] * x[1]) + P[4 * f + 3] * x[2] for f in range(4)]
+            f = next((q for q in range(4) if d[q] > 0), -1)
+        else:
+            a = max(range(4), key=lambda q: (d[q], -q))
+            f = -1 if d[a] < 0 else a
+        if f < 0:
+            return c, k
+        k += 1
+        if nbr[c][f] < 0:
+            return int(nbr[c][f]), k
+        c = int(nbr[c][f])
+
+
+@pytest.mark.parametrize("fast", [True, False])
+def test_single_point_relocate(fast, lib, oracle_mod):
+    """pg_relocate: the walk of one point from a given cell, both of the
+    reference's rules (first positive facet, largest projection) and the
+    crossing count of relocate_stat, bit for bit against a Python
+    restatement, for points inside and outside the mesh."""
+    ma, mesh, pop, o, rng = probe_setup(lib, oracle_mod)
+    planes = mesh.table(L.T_PLANES).reshape(-1, 16)
+    nbr = mesh.table(L.T_NEIGHBOURS).reshape(-1, 4)
+    n = 3000
+    start = rng.integers(0, ma.n_cells, n)
+    pts = np.asarray(ma.origin) + rng.random((n, 3)) * np.asarray(ma.Ld) * 1.1 - 0.05 * np.asarray(ma.Ld)
+    got, cr = pop.relocate(pts, start, fast=fast, with_crossings=True)
+    ref = [_walk_reference(planes, nbr, pts[i].tolist(), int(start[i]), fast) for i in range(n)]
+    assert np.array_equal(got, [r[0] for r in ref]) and np.array_equal(cr, [r[1] for r in ref])
+    assert (got < 0).any() and (got >= 0).any() and cr.max() >= 3
