@@ -2,25 +2,29 @@
 40^3-120^3 configuration, here at 40^3 with 4M particles): same seeded
 particles, same injection seed, 100 fused steps with the object biased through
 CircuitCM.  Every step records the charge density error in the L2 norm and the
-max-norm over dofs, the potential error, both forms' collected current, and
-whether the step is a boundary event: a step whose absorbed or injected counts,
-particle counts or object currents differ between the forms (one particle
-within rounding distance of a boundary absorbed by one form and kept by the
-other).  At event steps, and every 25 steps, the ids of the particles alive in
-one form only are recorded.  The table is printed for the record.
+max-norm over dofs, both over all dofs and over the interior dofs (those of no
+cell with a facet on the exterior boundary), the potential error, both forms'
+collected current, and whether the step is a boundary event: a step whose
+absorbed or injected counts, particle counts or object currents differ between
+the forms (a particle within rounding distance of a boundary absorbed by one
+form and kept by the other).  The ids of the particles alive in one form only
+are recorded at the first event steps.  The table is printed for the record.
+
+A boundary event changes the charge of the dofs of one boundary cell, which
+dominates the all-dof error of that step (about 1e-3 in L2); the interior
+error separates it from the drift of the FP32 trajectories away from the FP64
+ones (rounding of the position and velocity updates), which grows with the
+steps.
 
 Bars:
 * step 0 deposits the loaded particles, identical up to the FP32 rounding of
-  the inputs: 1e-5 relative in the max-norm;
-* steps without a boundary event: charge density within 1e-5 relative in the
-  L2 norm up to the drift horizon HORIZON (the FP32 trajectories leave the FP64
-  ones by rounding of the position and velocity updates, and particles that
-  cross a facet in one form a step before the other add up); the first such
-  step above 1e-5 is printed;
+  the inputs: 1e-5 relative in the max-norm over all dofs;
+* the interior charge density within 1e-5 relative in the L2 norm for the
+  first HORIZON steps (the drift horizon; the first step above it is printed);
 * every step: potential within 1e-3 relative in the max-norm, particle counts
-  within 1e-4, and the collected current non-zero in both forms;
-* the collected current averaged over the 100 steps within 1% between the
-  forms."""
+  within 1e-4;
+* the collected object current equal in both forms on at least 95% of the
+  steps, and its mean over the run within 1% and non-zero."""
 import numpy as np
 import pytest
 
@@ -31,6 +35,7 @@ pytestmark = pytest.mark.gpu
 
 STEPS = 100
 HORIZON = 10
+ID_RECORDS = 5
 
 
 def rel_max(a, b):
@@ -43,10 +48,21 @@ def rel_l2(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
 
 
+def interior_dofs(mesh):
+    """Dofs of no cell that has a facet on the exterior boundary (tag 1)."""
+    nbr = mesh.table(L.T_NEIGHBOURS).reshape(-1, 4)
+    dofs = mesh.table(L.T_CELL_DOFS).reshape(-1, 4)
+    keep = np.ones(mesh.n_dofs, bool)
+    keep[np.unique(dofs[(nbr == -1).any(axis=1)])] = False
+    return keep
+
+
 def test_mixed_form_errors_on_the_probe_at_40_cubed(capsys):
     import bench
     ma, species, loads = bench.make_workload(40, 2_000_000)
     mesh = punc.Mesh(ma)
+    inner = interior_dofs(mesh)
+    assert 0.5 * mesh.n_dofs < inner.sum() < mesh.n_dofs
     runs = {}
     for prec in (L.PG_FP64, L.PG_MIXED):
         pop = punc.Population(mesh, precision=prec, capacity=int(2.6 * 4_000_000), pcg_rtol=1e-10, pcg_atol=1e-12,
@@ -60,6 +76,7 @@ def test_mixed_form_errors_on_the_probe_at_40_cubed(capsys):
     p64, o64, _ = runs[L.PG_FP64]
     p32, o32, _ = runs[L.PG_MIXED]
     rows = []
+    id_records = 0
     for n in range(STEPS):
         a = punc.step(p64, o64, bench.DT, first_step=(n == 0), inject=True, seed=0x5EED0003, step_no=n)
         b = punc.step(p32, o32, bench.DT, first_step=(n == 0), inject=True, seed=0x5EED0003, step_no=n)
@@ -68,32 +85,34 @@ def test_mixed_form_errors_on_the_probe_at_40_cubed(capsys):
         event = (a.n_absorbed != b.n_absorbed or a.n_injected != b.n_injected or a.n_particles != b.n_particles
                  or o64[0].current != o32[0].current)
         ids = None
-        if event or n % 25 == 24:
+        if event and id_records < ID_RECORDS:
             ids = np.setxor1d(p64.particles(fields=("id",))["id"], p32.particles(fields=("id",))["id"])
-        rows.append(dict(n=n, l2=rel_l2(r32, r64), mx=rel_max(r32, r64), phi=rel_max(f32, f64),
+            id_records += 1
+        rows.append(dict(n=n, l2=rel_l2(r32, r64), mx=rel_max(r32, r64), l2i=rel_l2(r32[inner], r64[inner]),
+                         mxi=rel_max(r32[inner], r64[inner]), phi=rel_max(f32, f64),
                          c64=o64[0].current, c32=o32[0].current, N64=a.n_particles, N32=b.n_particles,
                          event=event, ids=ids))
-    over = [r["n"] for r in rows if not r["event"] and r["l2"] > 1e-5]
+    over = [r["n"] for r in rows if r["l2i"] > 1e-5]
     first_over = over[0] if over else None
     with capsys.disabled():
-        print("\nprobe-40, 4M particles, mixed vs FP64 over %d steps (step, rho L2, rho max, phi max, current FP64, "
-              "current mixed, N FP64, N mixed, event, ids alive in one form only):" % STEPS)
+        print("\nprobe-40, 4M particles, mixed vs FP64 over %d steps (step, rho L2, rho max, interior rho L2, "
+              "interior rho max, phi max, current FP64, current mixed, N FP64, N mixed, event, ids alive in one "
+              "form only):" % STEPS)
         for r in rows:
-            ids = "" if r["ids"] is None else "%d %s" % (len(r["ids"]), list(r["ids"][:4]))
-            print("  %3d  %.2e  %.2e  %.2e  %+.6e  %+.6e  %8d  %8d  %s  %s" % (
-                r["n"], r["l2"], r["mx"], r["phi"], r["c64"], r["c32"], r["N64"], r["N32"],
+            ids = "" if r["ids"] is None else "%d %s" % (len(r["ids"]), [int(k) for k in r["ids"][:4]])
+            print("  %3d  %.2e  %.2e  %.2e  %.2e  %.2e  %+.6e  %+.6e  %8d  %8d  %s  %s" % (
+                r["n"], r["l2"], r["mx"], r["l2i"], r["mxi"], r["phi"], r["c64"], r["c32"], r["N64"], r["N32"],
                 "event" if r["event"] else "-", ids))
-        print("  first step without a boundary event above 1e-5 (L2):", first_over,
+        print("  first step with the interior rho L2 error above 1e-5:", first_over,
               "; event steps:", sum(r["event"] for r in rows))
     assert rows[0]["mx"] < 1e-5, rows[0]
     for r in rows[:HORIZON]:
-        if not r["event"]:
-            assert r["l2"] < 1e-5, r
+        assert r["l2i"] < 1e-5, r
     for r in rows:
         assert r["phi"] < 1e-3 and abs(r["N64"] - r["N32"]) <= 1e-4 * r["N64"], r
-        assert r["c64"] != 0.0 and r["c32"] != 0.0, r
+    assert sum(r["c64"] == r["c32"] for r in rows) >= 0.95 * STEPS
     mean64 = np.mean([r["c64"] for r in rows])
     mean32 = np.mean([r["c32"] for r in rows])
-    assert abs(mean32 - mean64) < 1e-2 * abs(mean64), (mean32, mean64)
+    assert mean64 != 0.0 and abs(mean32 - mean64) < 1e-2 * abs(mean64), (mean32, mean64)
     for pop, _, _ in runs.values():
         pop.close()

@@ -112,8 +112,6 @@ def test_probe_80_fused_steps_in_lockstep(lib, oracle_mod, capsys):
         err_phi = rel(phi, phi_o)
         assert err_phi < PHI_TOL, (n, err_phi)
         assert objs[0].potential == oobjs[0]["potential"] == bench.BIAS
-        err_q = abs(objs[0].charge - oobjs[0]["charge"]) / abs(oobjs[0]["charge"])
-        assert err_q < PHI_TOL, (n, err_q)
         E = o.efield(phi)
         assert np.array_equal(punc.Function(pop, "E").vector(), E), n
         ke = o.boris(E, (0.0, 0.0, 0.0), bench.DT * (0.5 if n == 0 else 1.0), nth)
@@ -122,6 +120,10 @@ def test_probe_80_fused_steps_in_lockstep(lib, oracle_mod, capsys):
         absorbed = o.update(oobjs, bench.DT, nth)
         assert res.n_absorbed == absorbed.sum() > 0
         assert oobjs[0]["current"] != 0.0 and rel(objs[0].current, oobjs[0]["current"]) < RTOL, n
+        # the object charge: the circuit's charge of the solve plus the
+        # absorbed charge of the update (the solve's accuracy bounds it)
+        err_q = abs(objs[0].charge - oobjs[0]["charge"]) / abs(oobjs[0]["charge"])
+        assert err_q < PHI_TOL, (n, err_q)
         # the tally per boundary tag and species: its sums over the species are
         # the oracle's per-tag counts, and the object's share per species adds
         # up to the object current
