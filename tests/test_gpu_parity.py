@@ -521,6 +521,7 @@ def _walk_reference(planes, nbr, x, c, fast):
     while True:
         P = planes[c]
         d = [((P[4 * f] + P[4 * f + 1] * x[0]) + P[4 * f + 2] * x[1]) + P[4 * f + 3] * x[2] for f in range(4)]
+        if fast:
             f = next((q for q in range(4) if d[q] > 0), -1)
         else:
             a = max(range(4), key=lambda q: (d[q], -q))
