@@ -516,6 +516,7 @@ static int upload_op(pg_sim *s, const Csr &A, int g, SpOp &out, bool want_c16 = 
         int32_t *d_sw;
         if ((rc = upload(s, &d_sw, swidth))) return rc;
         out.swidth = d_sw;
+        out.wmax = swidth.empty() ? 0 : *std::max_element(swidth.begin(), swidth.end());
     }
     if (c16) {
         std::vector<uint16_t> c(col.size(), 0);

@@ -91,12 +91,60 @@ __device__ __forceinline__ float csr_lane_sum(const SpOp &S, int i, int lane, in
     return s0 + s1;
 }
 
+constexpr int kWide = 8;   // SELL operators whose slices hold at most this many entries a row
+
 template <bool C16, bool V16, class XV, class PRE, class EPI>
 __device__ __forceinline__ void apply_t(const SpOp &S, XV xv, PRE pre, EPI epi, int t0, int ts) {
     using P = decltype(pre(0));
     using E = Entry<C16, V16>;
     const float vs = V16 ? S.vscale : 1.0f;
-    if (S.g == 1) {
+    if (S.g == 1 && S.wmax <= kWide) {
+        // narrow SELL: every entry of two rows loaded at once, then every
+        // gather, so a round costs three dependent trips (offsets, entries,
+        // gathered values) instead of two per pair of entries; the sums run
+        // in the same entry order as the general path below
+        constexpr int R = 2;
+        for (int i = t0; i < S.n; i += R * ts) {
+            int off[R], wid[R], cb[R];
+            P pv[R];
+#pragma unroll
+            for (int q = 0; q < R; ++q) {
+                const int r = i + q * ts;
+                const bool ok = r < S.n;
+                off[q] = ok ? (int)__ldg(S.ptr + (r >> 5)) + (r & 31) : 0;
+                wid[q] = ok ? __ldg(S.swidth + (r >> 5)) : 0;
+                cb[q] = (ok && C16) ? __ldg(S.cbase + (r >> 5)) : 0;
+                pv[q] = ok ? pre(r) : P{};
+            }
+            int c[R][kWide];
+            float v[R][kWide];
+#pragma unroll
+            for (int q = 0; q < R; ++q)
+#pragma unroll
+                for (int k = 0; k < kWide; ++k) {
+                    const bool ok = k < wid[q];
+                    const int o = off[q] + 32 * k;
+                    c[q][k] = ok ? E::col(S, o, cb[q]) : -1;
+                    v[q][k] = ok ? E::val(S, o) : 0.0f;
+                }
+            float x[R][kWide];
+#pragma unroll
+            for (int q = 0; q < R; ++q)
+#pragma unroll
+                for (int k = 0; k < kWide; ++k) x[q][k] = c[q][k] >= 0 ? xv(c[q][k]) : 0.0f;
+#pragma unroll
+            for (int q = 0; q < R; ++q) {
+                // the general path adds entries in pairs (a zero pair member
+                // past an odd width included): the same operations here
+                const int wpair = (wid[q] + 1) & ~1;
+                float sum = 0.0f;
+#pragma unroll
+                for (int k = 0; k < kWide; ++k)
+                    if (k < wpair) sum = fmaf(v[q][k], x[q][k], sum);
+                if (i + q * ts < S.n) epi(i + q * ts, V16 ? sum * vs : sum, pv[q]);
+            }
+        }
+    } else if (S.g == 1) {
         for (int i = t0; i < S.n; i += kRows * ts) {
             int off[kRows];   // operators hold fewer than 2^31 entries (checked at upload)
             int wid[kRows], cb[kRows];

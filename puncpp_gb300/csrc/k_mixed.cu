@@ -61,11 +61,6 @@ __device__ __forceinline__ void deposit_lambdas(bool agg, int c, const float l[4
     atomicAdd(rho_fixed + d.w, (unsigned long long)v3);
 }
 
-// Prefetch the line holding ptr into L1 (no register holds the data).
-__device__ __forceinline__ void prefetch_l1(const void *ptr) {
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(ptr));
-}
-
 // Cell record of c: barycentric rows 0-2 and the neighbours (int bits).
 struct CellRec {
     float4 r0, r1, r2, nb;
@@ -83,25 +78,8 @@ __global__ void __launch_bounds__(512, 2) k_mixed(DevMesh m, DevParticles p, int
     int retests = 0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t n_use = slots_in_use(p, n_slots);
-    // Software pipeline over this thread's particles i, i + stride, ...: the
-    // cell of particle i + 2 stride is loaded one iteration ahead of the
-    // prefetch of its cell record and dofs into L1, which runs one iteration
-    // ahead of their use, so the record's latency overlaps the work on the
-    // current particle.
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int c_cur = i < n_use ? p.cell[i] : -1;
-    int c_n1 = i + stride < n_use ? p.cell[i + stride] : -1;
-    int c_n2 = -1;
-    for (; i < n_use; i += stride, c_cur = c_n1, c_n1 = c_n2) {
-        const int64_t i2 = i + 2 * stride;
-        c_n2 = i2 < n_use ? p.cell[i2] : -1;
-        if (c_n1 >= 0) {
-            const char *rec = reinterpret_cast<const char *>(m.cell_f + 4 * (size_t)c_n1);
-            prefetch_l1(rec);
-            prefetch_l1(rec + 32);
-            prefetch_l1(m.dofs + c_n1);
-        }
-        int c = c_cur;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_use; i += stride) {
+        int c = p.cell[i];
         if (c < 0) continue;
         const int s = p.sp[i];
         float x = p.xf[i], y = p.yf[i], z = p.zf[i];

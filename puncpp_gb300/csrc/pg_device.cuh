@@ -257,6 +257,7 @@ struct SpOp {
     int32_t g = 1;                       // lanes per row
     const int64_t *ptr = nullptr;        // SELL slice offsets [n_slices+1] or CSR row offsets [n+1]
     const int32_t *swidth = nullptr;     // SELL slice widths (g == 1 only)
+    int32_t wmax = 0;                    // widest SELL slice (g == 1 only)
     const int32_t *col = nullptr;        // column indices (when col16 is null)
     const float *val = nullptr;          // FP32 values (when val16 is null)
     // compressed forms: column = cbase[slice or row] + col16[k]; value =
