@@ -255,7 +255,7 @@ int pg_update(pg_sim *sim, pg_object *objects, int32_t n_objects, double dt);
  * (punc/include/punc/population.h:641-699) sums the same tally over the
  * species into each object's current.  counts[t * n_species + k] = particles
  * of species k absorbed at tag t (t = 0 .. n_tags-1; 1 = exterior boundary,
- * 2.. objects; n_tags <= 64), q[k] and m[k] the species' charge and mass, in
+ * 2.. objects; n_tags <= 256), q[k] and m[k] the species' charge and mass, in
  * the engine's species order (first use of each (q, m)), for k < n_species;
  * *n_species_out = the number of species.  Any output may be NULL. */
 int pg_absorbed_counts(pg_sim *sim, int64_t *counts, int32_t n_tags, int32_t n_species, double *q, double *m,

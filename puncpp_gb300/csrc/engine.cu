@@ -55,6 +55,8 @@ struct pg_sim {
     const double *x_prev_of = nullptr;         // the solution vector x_prev belongs to
     int x_prev_count = 0;                      // solutions seen for that vector (0, 1, 2+)
     double *lap = nullptr;                     // [n_obj][ndof] unit-potential Laplace solutions
+    int32_t *lap_rng = nullptr;                // [n_obj][2] dof range [lo, hi) holding L_k's entries
+                                               // above 1e-12 of its largest (a batch run's own dofs)
     int32_t *bc_kind = nullptr;
     double *bc_value = nullptr, *w_ext = nullptr, *w_obj = nullptr;
     double *r = nullptr, *z = nullptr, *p0 = nullptr, *p1 = nullptr, *Ap = nullptr, *pcg_part = nullptr;
@@ -873,7 +875,7 @@ static int solve_circuit_internal(pg_sim *s, pg_object *objects, int32_t n_objec
         Pots pv{};
         pv.n = n;
         for (int i = 0; i < n; ++i) pv.v[i] = pot[i];
-        launch_superpose(s->phi0, s->lap, pv, s->ndof, s->phi, s->stream);
+        launch_superpose(s->phi0, s->lap, pv, s->lap_rng, s->ndof, s->phi, s->stream);
         s->phi_valid = true;
         return PG_OK;
     }
@@ -1956,6 +1958,7 @@ int pg_circuit_cm_setup(pg_sim *s, const pg_source *vs, int32_t nvs, const pg_so
     // capacitance matrix: one Laplace solve per object (inv_capacitance,
     // punc/src/object_CM.cpp:62-106 and laplace_solver 401-437).
     std::vector<double> cap(n * n, 0.0);
+    std::vector<int32_t> rng(2 * (size_t)n, 0);
     if (!s->lap) {
         int rc = dalloc(s, &s->lap, (size_t)n * s->ndof);
         if (rc) return rc;
@@ -1973,7 +1976,24 @@ int pg_circuit_cm_setup(pg_sim *s, const pg_source *vs, int32_t nvs, const pg_so
         for (int i = 0; i < n; ++i) cap[i * n + j] = img[i];
         PG_CUDA(cudaMemcpyAsync(s->lap + (size_t)j * s->ndof, s->phi, sizeof(double) * s->ndof,
                                 cudaMemcpyDeviceToDevice, s->stream));
+        // the dof range of L_j's entries above 1e-12 of its largest: the
+        // superposition skips the rest (in batched runs L_j lives in its run)
+        std::vector<double> h((size_t)s->ndof);
+        PG_CUDA(cudaMemcpyAsync(h.data(), s->phi, sizeof(double) * s->ndof, cudaMemcpyDeviceToHost, s->stream));
+        PG_CUDA(cudaStreamSynchronize(s->stream));
+        double vmax = 0.0;
+        for (double v : h) vmax = std::max(vmax, std::fabs(v));
+        int32_t lo = s->ndof, hi = 0;
+        for (int32_t i = 0; i < s->ndof; ++i)
+            if (std::fabs(h[i]) > 1e-12 * vmax) { lo = std::min(lo, i); hi = i + 1; }
+        rng[2 * j] = lo < hi ? lo : 0;
+        rng[2 * j + 1] = hi;
     }
+    if (!s->lap_rng) {
+        int rc = dalloc(s, &s->lap_rng, 2 * (size_t)n);
+        if (rc) return rc;
+    }
+    PG_CUDA(cudaMemcpyAsync(s->lap_rng, rng.data(), sizeof(int32_t) * 2 * n, cudaMemcpyHostToDevice, s->stream));
     s->phi0_valid = false;
     s->phi_valid = false;
     s->inv_cap = cap;
@@ -2203,7 +2223,7 @@ static int enqueue_step(pg_sim *s, const pg_step_args *a, bool first) {
         launch_image_charge(s->dm, superpose ? s->phi0 : s->phi, s->d_ofacets, s->n_ofac, s->n_obj, s->cfg.eps0,
                             s->image, s->stream);
         launch_circuit_post(s->circ_dev, s->image, s->run_obj, s->obj_pot, s->stream);
-        if (superpose) launch_superpose_dev(s->phi0, s->lap, s->obj_pot, s->n_obj, s->ndof, s->phi, s->stream);
+        if (superpose) launch_superpose_dev(s->phi0, s->lap, s->obj_pot, s->lap_rng, s->n_obj, s->ndof, s->phi, s->stream);
         else if ((rc = pcg_enqueue(s, s->phi))) return rc;
     } else {
         if ((rc = pcg_enqueue(s, s->phi))) return rc;

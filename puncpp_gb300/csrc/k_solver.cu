@@ -435,20 +435,21 @@ __global__ void k_image_charge(DevMesh m, const double *__restrict__ phi, const 
 // phi = phi0 + sum_k V_k L_k: the solution with object potentials V from the
 // one with zero potentials and the unit-potential Laplace solutions L_k.
 __global__ void k_superpose(const double *__restrict__ phi0, const double *__restrict__ lap, Pots pots,
-                            int32_t n, double *__restrict__ out) {
+                            const int32_t *__restrict__ rng, int32_t n, double *__restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double v = phi0[i];
-    for (int k = 0; k < pots.n; ++k) v = v + pots.v[k] * lap[(size_t)k * n + i];
+    for (int k = 0; k < pots.n; ++k)
+        if (!rng || (i >= rng[2 * k] && i < rng[2 * k + 1])) v = v + pots.v[k] * lap[(size_t)k * n + i];
     out[i] = v;
 }
 
 }  // namespace
 
-void launch_superpose(const double *phi0, const double *lap, const Pots &pots, int32_t n, double *out,
-                      cudaStream_t st) {
+void launch_superpose(const double *phi0, const double *lap, const Pots &pots, const int32_t *rng, int32_t n,
+                      double *out, cudaStream_t st) {
     count_launches(1);
-    k_superpose<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(phi0, lap, pots, n, out);
+    k_superpose<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(phi0, lap, pots, rng, n, out);
 }
 
 void launch_efield(const DevMesh &m, const double *phi, const double E0[3], cudaStream_t st) {

@@ -93,11 +93,13 @@ __global__ void k_circuit_post(const CircuitDev c, const double *img, double *ob
 }
 
 __global__ void k_superpose_dev(const double *__restrict__ phi0, const double *__restrict__ lap,
-                                const double *__restrict__ pot, int n_obj, int32_t n, double *__restrict__ out) {
+                                const double *__restrict__ pot, const int32_t *__restrict__ rng, int n_obj, int32_t n,
+                                double *__restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double v = phi0[i];
-    for (int k = 0; k < n_obj; ++k) v = v + pot[k] * lap[(size_t)k * n + i];
+    for (int k = 0; k < n_obj; ++k)
+        if (!rng || (i >= rng[2 * k] && i < rng[2 * k + 1])) v = v + pot[k] * lap[(size_t)k * n + i];
     out[i] = v;
 }
 
@@ -154,10 +156,10 @@ void launch_circuit_post(const CircuitDev &c, const double *img, double *obj, do
     count_launches(1);
     k_circuit_post<<<1, 1, 0, s>>>(c, img, obj, obj_pot);
 }
-void launch_superpose_dev(const double *phi0, const double *lap, const double *pot, int n_obj, int32_t n, double *out,
-                          cudaStream_t s) {
+void launch_superpose_dev(const double *phi0, const double *lap, const double *pot, const int32_t *rng, int n_obj,
+                         int32_t n, double *out, cudaStream_t s) {
     count_launches(1);
-    k_superpose_dev<<<(n + 255) / 256, 256, 0, s>>>(phi0, lap, pot, n_obj, n, out);
+    k_superpose_dev<<<(n + 255) / 256, 256, 0, s>>>(phi0, lap, pot, rng, n_obj, n, out);
 }
 void launch_step_record(double *rows, int row_len, int64_t *counts, const double *ke, const DevState *st,
                         int n_species, const int32_t *pcg_i, const double *pcg_d, const double *obj, int n_obj,

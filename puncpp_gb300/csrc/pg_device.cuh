@@ -18,7 +18,7 @@
 namespace pg {
 
 constexpr int kMaxSpecies = 8;
-constexpr int kMaxTags = 64;
+constexpr int kMaxTags = 256;   // boundary tags: 1 = exterior, 2.. objects (batched runs: one per run)
 // Mixed form: the CG1 deposit sums q lambda in int64 units of 2^-kFixedBits
 // q_max.  One particle adds at most 2^kFixedBits units to a dof, so a dof's
 // sum stays below 2^62 (int64 without overflow, with margin) as long as the
@@ -358,8 +358,9 @@ struct Pots {
     int32_t n;
     double v[kMaxTags];
 };
-void launch_superpose(const double *phi0, const double *lap, const Pots &pots, int32_t n, double *out,
-                      cudaStream_t st);
+// rng (optional): [2 n_obj] dof range [lo, hi) outside which L_k is dropped
+void launch_superpose(const double *phi0, const double *lap, const Pots &pots, const int32_t *rng, int32_t n,
+                      double *out, cudaStream_t st);
 
 // CircuitCM matrices and groups on the device (k_step.cu)
 struct CircuitDev {
@@ -377,8 +378,8 @@ void launch_objects_update(const DevState *st, const double *q, int n_species, c
 void launch_circuit_pre(const double *isrc, int n_isrc, double circ_dt, int n_obj, double *obj, double *obj_pot,
                         cudaStream_t s);
 void launch_circuit_post(const CircuitDev &c, const double *img, double *obj, double *obj_pot, cudaStream_t s);
-void launch_superpose_dev(const double *phi0, const double *lap, const double *pot, int n_obj, int32_t n, double *out,
-                          cudaStream_t s);
+void launch_superpose_dev(const double *phi0, const double *lap, const double *pot, const int32_t *rng, int n_obj,
+                         int32_t n, double *out, cudaStream_t s);
 void launch_step_record(double *rows, int row_len, int64_t *counts, const double *ke, const DevState *st,
                         int n_species, const int32_t *pcg_i, const double *pcg_d, const double *obj, int n_obj,
                         cudaStream_t s);
