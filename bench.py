@@ -158,8 +158,8 @@ def run_ours(args):
     ma, species, loads = make_workload(args.n_side, args.n_per)
     mesh = punc.Mesh(ma)
     prec = L.PG_MIXED if args.precision == "mixed" else L.PG_FP64
-    pop = punc.Population(mesh, precision=prec, capacity=int(2.6 * args.n_per * 2), pcg_rtol=RTOL, pcg_atol=ATOL,
-                          pcg_max_iter=4000, pcg_precond=PRECONDS[args.pcg_precond],
+    pop = punc.Population(mesh, precision=prec, capacity=int(args.capacity_factor * args.n_per * 2), pcg_rtol=RTOL,
+                          pcg_atol=ATOL, pcg_max_iter=4000, pcg_precond=PRECONDS[args.pcg_precond],
                           warm_start=2 if args.warm_start == "extrapolate" else 1)
     for s, (x, v) in zip(species, loads):
         pop.add_particles(x, v, s["q"], s["m"])
@@ -944,6 +944,8 @@ def main():
                     help="field path: EFieldDG0 + accel/boris, or ESolver (CG1) + accel_cg1/boris_cg1")
     ap.add_argument("--pcg-precond", default="amg", choices=sorted(PRECONDS),
                     help="Poisson preconditioner: one AMG V-cycle or Jacobi per iteration")
+    ap.add_argument("--capacity-factor", type=float, default=2.6,
+                    help="probe workloads: particle store slots per initial particle (the store grows if needed)")
     ap.add_argument("--runs", type=int, default=64, help="batch-R: runs in the batch (from the workload name)")
     ap.add_argument("--adjoint-particles", type=int, default=2_000_000, help="adjoint-N: particles of the run")
     args = ap.parse_args()
