@@ -55,8 +55,12 @@ def workload_name(n_side, n_per):
 # dominant kernels on probe-80 in the mixed form, from one ncu capture each
 # of this bench's command (the summaries under profiles/ give the commands)
 PROFILED_TRAFFIC = {
-    "k_pcg_amg": (1.204e9, "profiles/k_pcg_amg_probe80_mixed.md: 987 MB read + 217 MB written per solve"),
-    "k_mixed": (0.562e9, "profiles/k_mixed_probe80.md: 455 MB read + 106 MB written per launch"),
+    ("probe-80", "k_pcg_amg"): (1.204e9, "profiles/k_pcg_amg_probe80_mixed.md: 987 MB read + 217 MB written per solve"),
+    ("probe-80", "k_mixed"): (0.562e9, "profiles/k_mixed_probe80.md: 455 MB read + 106 MB written per launch"),
+    ("config3-120", "k_pcg_amg"): (10.99e9, "profiles/k_pcg_amg_config3_120.md: 9.73 GB read + 1.27 GB written per "
+                                            "solve (20 iterations)"),
+    ("config3-120", "k_mixed"): (2.89e9, "profiles/k_mixed_config3_120.md: 2.30 GB read + 0.59 GB written per launch "
+                                         "(untuned 256 x 4 launch configuration)"),
 }
 
 DT = 0.05
@@ -324,8 +328,8 @@ def run_ours(args):
         out = {"bound": "hbm", "kernel": name, "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
                "frac": round(ach / hbm, 4), "peak_source": peak_src, "traffic": None,
                "algorithmic_bytes": model}
-        key = name.split(" ")[0]
-        if mixed and args.n_side == N_SIDE and key in PROFILED_TRAFFIC and args.pcg_precond == "amg":
+        key = (args.workload, name.split(" ")[0])
+        if mixed and key in PROFILED_TRAFFIC and args.pcg_precond == "amg":
             out["traffic"], out["traffic_source"] = PROFILED_TRAFFIC[key]
             out["traffic_unit"] = "bytes per launch"
         return out

@@ -56,13 +56,33 @@ constexpr int kRows = 4;   // rows per thread (SELL) or per lane group (CSR) at 
 
 // Column and value of stored entry o (b: the entry's slice or row base) in
 // the operator's storage form.
+// Read-only loads of operator entries that ask the L2 for the 256-byte
+// segment around the address: the entries of the next step of a row (32 rows
+// further in a SELL slice, the next lanes' share in CSR) arrive with this
+// step's, so the next step's loads hit L2.
+__device__ __forceinline__ uint16_t ld_nc_u16(const uint16_t *p) {
+    uint16_t v;
+    asm("ld.global.nc.L2::256B.u16 %0, [%1];" : "=h"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ int ld_nc_s32(const int32_t *p) {
+    int v;
+    asm("ld.global.nc.L2::256B.s32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ float ld_nc_f32(const float *p) {
+    float v;
+    asm("ld.global.nc.L2::256B.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+
 template <bool C16, bool V16>
 struct Entry {
     __device__ static __forceinline__ int col(const SpOp &S, int o, int b) {
-        return C16 ? b + (int)__ldg(S.col16 + o) : __ldg(S.col + o);
+        return C16 ? b + (int)ld_nc_u16(S.col16 + o) : ld_nc_s32(S.col + o);
     }
     __device__ static __forceinline__ float val(const SpOp &S, int o) {
-        return V16 ? __half2float(__ushort_as_half(__ldg(S.val16 + o))) : __ldg(S.val + o);
+        return V16 ? __half2float(__ushort_as_half(ld_nc_u16(S.val16 + o))) : ld_nc_f32(S.val + o);
     }
 };
 
