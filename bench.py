@@ -54,13 +54,17 @@ def workload_name(n_side, n_per):
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # dominant kernels on probe-80 in the mixed form, from one ncu capture each
 # of this bench's command (the summaries under profiles/ give the commands)
+# DRAM traffic of the dominant kernels from one ncu capture each: the
+# particle pass per launch, the PCG per iteration at the AMG strength threshold
+# of the capture (scaled by this run's iterations per solve)
 PROFILED_TRAFFIC = {
-    ("probe-80", "k_pcg_amg"): (1.204e9, "profiles/k_pcg_amg_probe80_mixed.md: 987 MB read + 217 MB written per solve"),
-    ("probe-80", "k_mixed"): (0.562e9, "profiles/k_mixed_probe80.md: 455 MB read + 106 MB written per launch"),
-    ("config3-120", "k_pcg_amg"): (10.99e9, "profiles/k_pcg_amg_config3_120.md: 9.73 GB read + 1.27 GB written per "
-                                            "solve (20 iterations)"),
-    ("config3-120", "k_mixed"): (2.89e9, "profiles/k_mixed_config3_120.md: 2.30 GB read + 0.59 GB written per launch "
-                                         "(untuned 256 x 4 launch configuration)"),
+    ("probe-80", "k_pcg_amg", 0.0): (1.204e9 / 17, "profiles/k_pcg_amg_probe80_mixed.md: 987 MB read + 217 MB "
+                                                   "written per solve of 17 iterations"),
+    ("probe-80", "k_mixed", None): (0.562e9, "profiles/k_mixed_probe80.md: 455 MB read + 106 MB written per launch"),
+    ("config3-120", "k_pcg_amg", 0.0): (10.99e9 / 20, "profiles/k_pcg_amg_config3_120.md (threshold 0): 9.73 GB "
+                                                      "read + 1.27 GB written per solve of 20 iterations"),
+    ("config3-120", "k_mixed", None): (2.89e9, "profiles/k_mixed_config3_120.md: 2.30 GB read + 0.59 GB written per "
+                                               "launch (untuned 256 x 4 launch configuration)"),
 }
 
 DT = 0.05
@@ -165,6 +169,8 @@ def run_ours(args):
     pop = punc.Population(mesh, precision=prec, capacity=int(args.capacity_factor * args.n_per * 2), pcg_rtol=RTOL,
                           pcg_atol=ATOL, pcg_max_iter=4000, pcg_precond=PRECONDS[args.pcg_precond],
                           warm_start=2 if args.warm_start == "extrapolate" else 1)
+    if args.amg_theta is not None and args.pcg_precond == "amg":
+        punc.set_amg_strength(pop, args.amg_theta)
     for s, (x, v) in zip(species, loads):
         pop.add_particles(x, v, s["q"], s["m"])
     sp = [punc.Species(s["q"], s["m"], n=s["n"], vth=s["vth"]) for s in species]
@@ -197,6 +203,12 @@ def run_ours(args):
         tuning = punc.autotune(pop, objs, DT, steps_per_trial=2, inject=True, seed=INJECT_SEED, step_no=step_no,
                                efield_cg1=cg1)
         step_no += (24 if prec == L.PG_MIXED else 12) * 2 + 41
+        if args.pcg_precond == "amg" and args.amg_theta is None:
+            # the AMG aggregation threshold of least PCG time, three candidates
+            at = punc.autotune_amg(pop, objs, DT, steps_per_trial=6, inject=True, seed=INJECT_SEED, step_no=step_no,
+                                   efield_cg1=cg1)
+            tuning.update({"amg_theta": at["amg_theta"], "amg_pcg_ms": at["pcg_ms"]})
+            step_no += 3 * 6
         n_now = pop.num_of_particles()
     if args.step_mode != "staged":
         # capture the step graph (and run one more warm-up step) outside the timed region
@@ -328,10 +340,17 @@ def run_ours(args):
         out = {"bound": "hbm", "kernel": name, "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
                "frac": round(ach / hbm, 4), "peak_source": peak_src, "traffic": None,
                "algorithmic_bytes": model}
-        key = (args.workload, name.split(" ")[0])
+        kern = name.split(" ")[0]
+        if kern == "k_pcg_amg":
+            key = (args.workload, kern, punc.amg_strength(pop))
+            per = iters / max(1, args.steps)          # iterations per solve (one solve a step)
+        else:
+            key, per = (args.workload, kern, None), 1.0
         if mixed and key in PROFILED_TRAFFIC and args.pcg_precond == "amg":
-            out["traffic"], out["traffic_source"] = PROFILED_TRAFFIC[key]
-            out["traffic_unit"] = "bytes per launch"
+            t, srcs = PROFILED_TRAFFIC[key]
+            out["traffic"], out["traffic_source"] = round(t * per), srcs
+            out["traffic_unit"] = "bytes per launch" + (" (per iteration x %.2f iterations per solve)" % per
+                                                        if kern == "k_pcg_amg" else "")
         return out
 
     r_part = roof_of("k_mixed (fused FP32 DG0 field+push+move+walk, fixed-point deposit)" if mixed
@@ -358,7 +377,8 @@ def run_ours(args):
         "config": {"workload": workload_name(args.n_side, args.n_per), "precision": args.precision,
                    "pcg_precond": args.pcg_precond, "warm_start": args.warm_start, "efield": args.efield,
                    "step_mode": args.step_mode, "tuning": tuning, "cells": nc, "dofs": nv, "nnz": nnz,
-                   "amg_levels": [[v["rows"], v["nnz"]] for v in lay["levels"]], "particles_initial": n0,
+                   "amg_levels": [[v["rows"], v["nnz"]] for v in lay["levels"]],
+                   "amg_theta": punc.amg_strength(pop) if lay["levels"] else None, "particles_initial": n0,
                    "particles_mean_pushed": round(n_avg), "pcg_iterations_per_step": round(iters / args.steps, 1),
                    "first_timed_step": first_timed, "last_timed_step": last_timed,
                    "l2": f"inputs larger than L2 (129 MB): particle records {(28 if mixed else 52) * n_avg / 1e6:.0f} MB, "
@@ -419,6 +439,8 @@ def error_record(args, n_steps):
         pop = punc.Population(mesh, precision=prec, capacity=int(2.6 * args.n_per * 2), pcg_rtol=RTOL, pcg_atol=ATOL,
                               pcg_max_iter=4000, pcg_precond=PRECONDS[args.pcg_precond],
                               warm_start=2 if args.warm_start == "extrapolate" else 1)
+        if args.amg_theta is not None and args.pcg_precond == "amg":
+            punc.set_amg_strength(pop, args.amg_theta)
         for s, (x, v) in zip(species, loads):
             pop.add_particles(x, v, s["q"], s["m"])
         punc.create_flux(pop, [punc.Species(s["q"], s["m"], n=s["n"], vth=s["vth"]) for s in species])
@@ -827,6 +849,9 @@ def run_batch(args):
     punc.run_steps(pop, objs, DT, args.warmup, first_step=True, inject=True, seed=0x5EED0004)
     tuning = punc.autotune(pop, objs, DT, steps_per_trial=2, inject=True, seed=0x5EED0004, step_no=args.warmup)
     step_no = args.warmup + (24 * 2 + 41)
+    at = punc.autotune_amg(pop, objs, DT, steps_per_trial=6, inject=True, seed=0x5EED0004, step_no=step_no)
+    tuning.update({"amg_theta": at["amg_theta"], "amg_pcg_ms": at["pcg_ms"]})
+    step_no += 3 * 6
     rs0 = punc.run_steps(pop, objs, DT, 1, inject=True, seed=0x5EED0004, step_no=step_no)
     n_now = rs0[-1].n_particles
     clk = ClockSampler().__enter__()
@@ -938,7 +963,7 @@ def main():
     ap.add_argument("--no-fp64-form", dest="fp64_form", action="store_false",
                     help="skip the FP64-form run that the mixed form is compared with")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
-                    help="skip the engine's autotuner (launch configuration, sort interval) in the warm-up")
+                    help="skip the engine's autotuners (launch configuration, sort interval, AMG strength threshold) in the warm-up")
     ap.add_argument("--step-mode", default="graph", choices=["graph", "stream", "staged"],
                     help="graph: pg_run_steps replaying a captured CUDA graph; stream: pg_run_steps without the "
                          "graph; staged: pg_step per step with stage timing")
@@ -948,6 +973,9 @@ def main():
                     help="field path: EFieldDG0 + accel/boris, or ESolver (CG1) + accel_cg1/boris_cg1")
     ap.add_argument("--pcg-precond", default="amg", choices=sorted(PRECONDS),
                     help="Poisson preconditioner: one AMG V-cycle or Jacobi per iteration")
+    ap.add_argument("--amg-theta", type=float, default=None,
+                    help="AMG aggregation strength threshold (default: chosen by pg_autotune_amg in the warm-up, "
+                         "0 with --no-autotune)")
     ap.add_argument("--capacity-factor", type=float, default=2.6,
                     help="probe workloads: particle store slots per initial particle (the store grows if needed)")
     ap.add_argument("--runs", type=int, default=64, help="batch-R: runs in the batch (from the workload name)")
@@ -995,7 +1023,8 @@ def main():
                             "pcg_iterations_per_step": r64["config"]["pcg_iterations_per_step"],
                             "e2e": r64["e2e"]["value"], "roofline_particles_frac": r64["roofline_particles"]["frac"],
                             "particle_stages": r64["particle_stages"], "long_run": r64["long_run"],
-                            "stage_ms_per_step": r64["stage_ms_per_step"],
+                            "stage_ms_per_step": r64["stage_ms_per_step"], "tuning": r64["config"]["tuning"],
+                            "amg_theta": r64["config"]["amg_theta"],
                             "poisson": "the same AMG-preconditioned PCG as the mixed form (FP32 recurrence and "
                                        "operators, FP64 solution, inner products and true-residual replacement, "
                                        "FP64 stopping test); the particle arithmetic is FP64"}

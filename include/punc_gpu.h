@@ -324,6 +324,22 @@ int pg_get_tuning(pg_sim *sim, pg_tuning *tuning);
  * Applies and returns the choice; about 24 steps_per_trial + 41 steps. */
 int pg_autotune(pg_sim *sim, const pg_step_args *args, pg_object *objects, int32_t n_objects,
                 int32_t steps_per_trial, pg_tuning *out);
+/* Strength threshold theta of the AMG preconditioner's aggregation (the
+ * couplings |a_ij| >= theta sqrt(a_ii a_jj) count as strong; 0, the default:
+ * every coupling): rebuilds the hierarchy from the matrix kept at pg_create.
+ * The solves still stop on the same FP64 residual test; the threshold changes
+ * the iteration count and the cost of an iteration.  PG_ERR_ARG without an
+ * AMG preconditioner (pcg_precond 1); on failure the previous hierarchy is
+ * kept. */
+int pg_amg_set_strength(pg_sim *sim, double theta);
+int pg_amg_get_strength(pg_sim *sim, double *theta);
+/* The threshold chosen by timing: for each candidate (NULL, 0: {0, 0.01,
+ * 0.02}) the hierarchy is rebuilt and steps_per_trial real steps of this
+ * simulation run (pg_step with args, the RNG step advancing); the candidate
+ * of least mean PCG time per step is applied and returned with that time. */
+int pg_autotune_amg(pg_sim *sim, const pg_step_args *args, pg_object *objects, int32_t n_objects,
+                    int32_t steps_per_trial, const double *thetas, int32_t n_thetas, double *best_theta,
+                    double *best_pcg_ms);
 /* Adjoint of n_steps fused steps (FP64 form; DG0 field with B = 0, no
  * injection, no absorption, objects at fixed potentials): the forward runs the
  * steps from the current state (args as pg_step; args->step the first step's

@@ -21,7 +21,8 @@ STATUS_NAMES = {
     5: "PG_ERR_WALK_LIMIT", 6: "PG_ERR_NOT_CONVERGED", 7: "PG_ERR_STATE", 8: "PG_ERR_SINGULAR",
 }
 PG_FP64, PG_MIXED = 0, 1
-PG_ERR_NOT_CONVERGED = 6
+(PG_ERR_ARG, PG_ERR_CUDA, PG_ERR_MESH, PG_ERR_CAPACITY, PG_ERR_WALK_LIMIT, PG_ERR_NOT_CONVERGED, PG_ERR_STATE,
+ PG_ERR_SINGULAR) = range(1, 9)
 
 (T_CELL_VERTICES, T_BARYCENTRIC, T_PLANES, T_NEIGHBOURS, T_CELL_DOFS, T_VOLUME, T_DV_INV,
  T_CSR_ROWPTR, T_CSR_COL, T_STIFFNESS, T_MASS, T_EXT_FACETS, T_BC_KIND, T_OBJ_FACETS) = range(14)
@@ -153,6 +154,10 @@ SIGNATURES = {
     "pg_set_tuning": ([_P, C.POINTER(Tuning)], C.c_int),
     "pg_get_tuning": ([_P, C.POINTER(Tuning)], C.c_int),
     "pg_autotune": ([_P, C.POINTER(StepArgs), C.POINTER(Object), C.c_int32, C.c_int32, C.POINTER(Tuning)], C.c_int),
+    "pg_amg_set_strength": ([_P, C.c_double], C.c_int),
+    "pg_amg_get_strength": ([_P, _D], C.c_int),
+    "pg_autotune_amg": ([_P, C.POINTER(StepArgs), C.POINTER(Object), C.c_int32, C.c_int32, _D, C.c_int32, _D, _D],
+                        C.c_int),
     "pg_run_steps": ([_P, C.POINTER(StepArgs), C.POINTER(Object), C.c_int32, C.c_int32, C.c_int32,
                       C.POINTER(StepResult)], C.c_int),
     "pg_stage_times": ([_P, _D, C.c_int32, _I32], C.c_int),

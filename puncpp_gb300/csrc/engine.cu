@@ -68,6 +68,10 @@ struct pg_sim {
     bool has_dirichlet = false;
     bool use_amg = false;                      // AMG-preconditioned mixed PCG
     AmgDev amg{};
+    Csr amg_A0;                                // the reduced matrix the hierarchy is built from
+    double amg_theta = 0.0;                    // strength threshold of the aggregation
+    std::vector<void *> amg_mem;               // device allocations of the hierarchy
+    std::vector<void *> *alloc_to = nullptr;   // where dalloc records (null: allocs)
     std::vector<int64_t> amg_rows, amg_nnz, amg_nnz_p;   // per level (pg_poisson_layout_get)
     int64_t a_nnz = 0, a_sell = 0;                       // stored nonzeros and SELL-32 entries of A
     int64_t amg_nnz_g = 0, amg_nnz_u1 = 0;               // cycle operators G and U1
@@ -185,7 +189,7 @@ int dalloc(pg_sim *s, T **p, size_t count) {
     void *q = nullptr;
     cudaError_t e = cudaMalloc(&q, count * sizeof(T));
     if (e != cudaSuccess) return fail(PG_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    s->allocs.push_back(q);
+    (s->alloc_to ? *s->alloc_to : s->allocs).push_back(q);
     *p = reinterpret_cast<T *>(q);
     return PG_OK;
 }
@@ -554,18 +558,16 @@ static int upload_op(pg_sim *s, const Csr &A, int g, SpOp &out, bool want_c16 = 
     return PG_OK;
 }
 
-// Smoothed-aggregation hierarchy of the reduced Poisson matrix, on the
-// device, with the operators of the collapsed cycle.  Level 0 shares the
-// solver's FP32 SELL-32 matrix and D^-1.
-static int setup_amg(pg_sim *s, const std::vector<int32_t> &arow, const std::vector<int32_t> &acol,
-                     const std::vector<double> &aval) {
-    Csr A0;
-    A0.n = A0.m = (int64_t)arow.size() - 1;
-    A0.rp.assign(arow.begin(), arow.end());
-    A0.ci = acol;
-    A0.v = aval;
+// Smoothed-aggregation hierarchy of the reduced Poisson matrix s->amg_A0
+// with strength threshold s->amg_theta, on the device, with the operators of
+// the collapsed cycle.  Level 0 shares the solver's D^-1.  Device memory goes
+// to s->amg_mem (freed by a rebuild).
+static int build_amg(pg_sim *s) {
+    const Csr &A0 = s->amg_A0;
     AmgHierarchy h;
-    const int arc = amg_setup(A0, h, s->cfg.periodic != 0);
+    AmgParams prm;
+    prm.theta = s->amg_theta;
+    const int arc = amg_setup(A0, h, s->cfg.periodic != 0, prm);
     if (arc == 9) return fail(PG_ERR_ARG, "AMG: coarsening stalls above 4096 rows (use pcg_precond = 1)");
     if (arc != 0) return fail(PG_ERR_SINGULAR, "AMG: coarsest operator is singular");
     if ((int)h.levels.size() > kAmgMaxLevels) return fail(PG_ERR_ARG, "AMG: too many levels");
@@ -662,6 +664,31 @@ static int setup_amg(pg_sim *s, const std::vector<int32_t> &arow, const std::vec
     s->amg_cycle_bytes = cb;
     s->use_amg = true;
     return PG_OK;
+}
+
+static void free_amg(pg_sim *s) {
+    for (void *p : s->amg_mem) cudaFree(p);
+    s->amg_mem.clear();
+    s->amg = AmgDev{};
+    s->use_amg = false;
+}
+
+static int rebuild_amg(pg_sim *s) {
+    free_amg(s);
+    s->alloc_to = &s->amg_mem;
+    const int rc = build_amg(s);
+    s->alloc_to = nullptr;
+    return rc;
+}
+
+static int setup_amg(pg_sim *s, const std::vector<int32_t> &arow, const std::vector<int32_t> &acol,
+                     const std::vector<double> &aval) {
+    Csr &A0 = s->amg_A0;
+    A0.n = A0.m = (int64_t)arow.size() - 1;
+    A0.rp.assign(arow.begin(), arow.end());
+    A0.ci = acol;
+    A0.v = aval;
+    return rebuild_amg(s);
 }
 
 static int object_index(const pg_sim *s, int64_t bnd_id) {
@@ -1307,6 +1334,7 @@ int pg_destroy(pg_sim *s) {
     for (auto &g : s->graph_exec)
         if (g) cudaGraphExecDestroy(g);
     for (void *p : s->adj.mem) cudaFree(p);
+    for (void *p : s->amg_mem) cudaFree(p);
     for (void *p : s->allocs) cudaFree(p);
     free_particles(s->P[0]);
     free_particles(s->P[1]);
@@ -2598,6 +2626,74 @@ done:
     if (rc) return rc;
     if (out) *out = best;
     return do_sort(s);
+}
+
+// Device time of a named stage over the steps since the last reset.
+static double stage_ms_named(pg_sim *s, const char *name) {
+    for (size_t k = 0; k < s->stage_names.size(); ++k)
+        if (s->stage_names[k] == name) return s->stage_ms[k];
+    return 0.0;
+}
+
+int pg_amg_set_strength(pg_sim *s, double theta) {
+    if (!s) return fail(PG_ERR_ARG, "pg_amg_set_strength: NULL handle");
+    if (!(theta >= 0.0 && theta < 1.0)) return fail(PG_ERR_ARG, "pg_amg_set_strength: theta must lie in [0, 1)");
+    if (s->amg_A0.n == 0) return fail(PG_ERR_ARG, "pg_amg_set_strength: the solver has no AMG preconditioner");
+    if (theta == s->amg_theta && s->use_amg) return PG_OK;
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+    drop_graphs(s);
+    const double old = s->amg_theta;
+    s->amg_theta = theta;
+    int rc = rebuild_amg(s);
+    if (rc) {
+        // keep the handle usable: back to the previous hierarchy
+        const std::string msg = pg_last_error();
+        s->amg_theta = old;
+        if (rebuild_amg(s) == PG_OK) return fail(rc, msg);
+    }
+    return rc;
+}
+
+int pg_amg_get_strength(pg_sim *s, double *theta) {
+    if (!s || !theta) return fail(PG_ERR_ARG, "pg_amg_get_strength: NULL argument");
+    *theta = s->amg_theta;
+    return PG_OK;
+}
+
+int pg_autotune_amg(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_t n_objects, int32_t steps_per_trial,
+                    const double *thetas, int32_t n_thetas, double *best_theta, double *best_ms) {
+    if (!s || !a) return fail(PG_ERR_ARG, "pg_autotune_amg: NULL argument");
+    if (n_thetas < 0 || (n_thetas > 0 && !thetas)) return fail(PG_ERR_ARG, "pg_autotune_amg: bad candidates");
+    if (s->amg_A0.n == 0) return fail(PG_ERR_ARG, "pg_autotune_amg: the solver has no AMG preconditioner");
+    static const double kDefault[] = {0.0, 0.01, 0.02};
+    const double *cand = n_thetas > 0 ? thetas : kDefault;
+    const int nc = n_thetas > 0 ? n_thetas : 3;
+    const int k = std::max(1, steps_per_trial);
+    const bool profiling = s->profiling;
+    s->profiling = true;
+    pg_step_args st = *a;
+    int rc = PG_OK;
+    double bt = s->amg_theta, bms = 1e300;
+    for (int c = 0; c < nc && rc == PG_OK; ++c) {
+        if ((rc = pg_amg_set_strength(s, cand[c]))) break;
+        collect_stages(s);
+        for (auto &v : s->stage_ms) v = 0.0;
+        for (int i = 0; i < k && rc == PG_OK; ++i) {
+            rc = pg_step(s, &st, objects, n_objects, nullptr);
+            st.first_step = 0;
+            st.step += 1;
+        }
+        if (rc) break;
+        collect_stages(s);
+        const double ms = stage_ms_named(s, "pcg") / k;
+        if (ms < bms) { bms = ms; bt = cand[c]; }
+    }
+    s->profiling = profiling;
+    if (rc) return rc;
+    if ((rc = pg_amg_set_strength(s, bt))) return rc;
+    if (best_theta) *best_theta = bt;
+    if (best_ms) *best_ms = bms;
+    return PG_OK;
 }
 
 // ---- adjoint of K fused steps (FP64 form) ---------------------------------

@@ -663,6 +663,34 @@ def autotune(pop: Population, objects, dt: float, steps_per_trial: int = 2, B=(0
     return _tuning_dict(t)
 
 
+def set_amg_strength(pop: Population, theta: float):
+    """Rebuild the AMG preconditioner with aggregation strength threshold theta
+    (pg_amg_set_strength; 0, the default, counts every coupling as strong)."""
+    L.check(L.load().pg_amg_set_strength(pop.handle, float(theta)))
+
+
+def amg_strength(pop: Population) -> float:
+    t = C.c_double()
+    L.check(L.load().pg_amg_get_strength(pop.handle, C.byref(t)))
+    return t.value
+
+
+def autotune_amg(pop: Population, objects, dt: float, steps_per_trial: int = 6, thetas=None, B=(0.0, 0.0, 0.0),
+                 first_step=False, inject=False, seed=0, step_no=0, E0=(0.0, 0.0, 0.0), efield_cg1=False) -> dict:
+    """The AMG strength threshold of least PCG time over real steps of the
+    simulation (pg_autotune_amg; candidates {0, 0.01, 0.02} by default);
+    applies it and returns {"amg_theta", "pcg_ms"}."""
+    a = L.StepArgs(dt, (C.c_double * 3)(*B), 1 if first_step else 0, 0, 0, (C.c_double * 3)(0.0, 0.0, 0.0),
+                   1 if inject else 0, seed, step_no, (C.c_double * 3)(*E0), 1 if efield_cg1 else 0)
+    arr = _objects_in(objects)
+    cand = np.ascontiguousarray(thetas if thetas is not None else [], np.float64)
+    best, ms = C.c_double(), C.c_double()
+    L.check(L.load().pg_autotune_amg(pop.handle, C.byref(a), arr, len(objects), steps_per_trial,
+                                     L.dptr(cand) if len(cand) else None, len(cand), C.byref(best), C.byref(ms)))
+    _objects_out(arr, objects)
+    return {"amg_theta": best.value, "pcg_ms": ms.value}
+
+
 def adjoint_forward(pop: Population, objects, dt: float, n_steps: int, ckpt_every: int, rho_target,
                     first_step=True, use_accel=False, E0=(0.0, 0.0, 0.0), Ld=None, step_no=0) -> float:
     """K fused steps keeping checkpoints; returns ||rho_K - rho_target||^2."""

@@ -514,6 +514,57 @@ def test_amg_pcg_reports_an_unattainable_tolerance(lib, oracle_mod):
     pop.close()
 
 
+def test_amg_strength_threshold_rebuild_and_selection(lib, oracle_mod):
+    """pg_amg_set_strength rebuilds the hierarchy: level 0 and 1 stay, the
+    coarsest level grows (48 rows at theta 0, 281 at 0.05 on this mesh), the
+    solve still matches a direct solve; a threshold outside [0, 1) is refused
+    with the hierarchy kept; steps replayed from a graph captured before a
+    rebuild use the new hierarchy (bitwise the same particles as a handle
+    built with that threshold from the start); pg_autotune_amg applies the
+    candidate it returns; a Jacobi-preconditioned handle has no threshold.
+    Mixed form: its deposit and solve are deterministic, so two handles agree
+    bit for bit."""
+    kw = dict(n=24, half=4.0, radius=0.8, n_particles=20000, pcg_rtol=1e-13, pcg_atol=1e-30, pcg_max_iter=5000,
+              precision=L.PG_MIXED)
+    ma, mesh, pop, o, rng = probe_setup(lib, oracle_mod, **kw)
+    rows0 = [v["rows"] for v in punc.poisson_layout(pop)["levels"]]
+    assert punc.amg_strength(pop) == 0.0 and rows0[-1] == 48
+    punc.set_amg_strength(pop, 0.05)
+    rows1 = [v["rows"] for v in punc.poisson_layout(pop)["levels"]]
+    assert punc.amg_strength(pop) == 0.05 and rows1[:2] == rows0[:2] and rows1[-1] == 281
+    rho = punc.distribute_cg1(pop)
+    objs = [punc.Object(2, potential=-2.0)]
+    phi_g = punc.PoissonSolver(pop, objs).solve(punc.Function(pop, "phi"), punc.Function(pop, "rho"), objs)
+    assert rel(phi_g, o.poisson_direct(rho, potentials=[-2.0])) < 1e-9
+    with pytest.raises(L.PgError) as err:
+        punc.set_amg_strength(pop, 1.5)
+    assert err.value.code == L.PG_ERR_ARG
+    assert punc.amg_strength(pop) == 0.05 and [v["rows"] for v in punc.poisson_layout(pop)["levels"]] == rows1
+    # a graph captured at theta 0.05, then a rebuild at theta 0
+    dt = 0.05
+    punc.run_steps(pop, objs, dt, 2, first_step=True, use_graph=True)
+    punc.set_amg_strength(pop, 0.0)
+    punc.run_steps(pop, objs, dt, 2, step_no=2, use_graph=True)
+    _, _, ref, _, _ = probe_setup(lib, oracle_mod, **kw)
+    punc.set_amg_strength(ref, 0.05)
+    robjs = [punc.Object(2, potential=-2.0)]
+    punc.run_steps(ref, robjs, dt, 2, first_step=True, use_graph=True)
+    punc.set_amg_strength(ref, 0.0)
+    punc.run_steps(ref, robjs, dt, 2, step_no=2, use_graph=False)
+    compare_particles(pop.particles(), ref.particles())
+    np.testing.assert_array_equal(punc.Function(pop, "phi").vector(), punc.Function(ref, "phi").vector())
+    res = punc.autotune_amg(pop, objs, dt, steps_per_trial=2, thetas=[0.0, 0.05], step_no=4)
+    assert res["amg_theta"] in (0.0, 0.05) and res["pcg_ms"] > 0.0
+    assert punc.amg_strength(pop) == res["amg_theta"]
+    pop.close()
+    ref.close()
+    _, _, jac, _, _ = probe_setup(lib, oracle_mod, pcg_precond=1)
+    with pytest.raises(L.PgError) as err:
+        punc.set_amg_strength(jac, 0.01)
+    assert err.value.code == L.PG_ERR_ARG
+    jac.close()
+
+
 def _walk_reference(planes, nbr, x, c, fast):
     """relocate_fast / relocate (punc/include/punc/population.h:454-569) in
     Python floats: plane value c0 + c1 x + c2 y + c3 z summed left to right."""
