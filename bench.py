@@ -63,6 +63,8 @@ PROFILED_TRAFFIC = {
     ("probe-80", "k_mixed", None): (0.562e9, "profiles/k_mixed_probe80.md: 455 MB read + 106 MB written per launch"),
     ("config3-120", "k_pcg_amg", 0.0): (10.99e9 / 20, "profiles/k_pcg_amg_config3_120.md (threshold 0): 9.73 GB "
                                                       "read + 1.27 GB written per solve of 20 iterations"),
+    ("config3-120", "k_pcg_amg", 0.01): (10.463e9 / 17, "profiles/k_pcg_amg_config3_120.md (threshold 0.01): 9.30 GB "
+                                                        "read + 1.16 GB written per solve of 17 iterations"),
     ("config3-120", "k_mixed", None): (2.89e9, "profiles/k_mixed_config3_120.md: 2.30 GB read + 0.59 GB written per "
                                                "launch (untuned 256 x 4 launch configuration)"),
 }
