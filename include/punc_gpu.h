@@ -439,10 +439,9 @@ int pg_poisson_layout_get(pg_sim *sim, pg_poisson_layout *out);
  * receives the solution; stops when ||b - A x|| <= max(rtol ||b||, atol).
  * At most 524,288 rows (larger n: PG_ERR_ARG); the array (about 20 MB) stays
  * on every GPU that loads the library.  All calls share it, so calls that
- * overlap on the GPU race.  The first call on a device sets the device up
- * (looks up the array's address): make it before any stream capture.
- * stream: a cudaStream_t, or NULL for the default stream; the call waits for
- * the solve to finish. */
+ * overlap on the GPU race.  The first call on a device also looks up the
+ * array's device address.  stream: a cudaStream_t, or NULL for the default
+ * stream; the call waits for the solve to finish. */
 int pg_pcg_solve_noalloc(int32_t n, const int32_t *rowptr, const int32_t *col, const double *val,
                          const double *b, double *x, double rtol, double atol, int32_t max_iter,
                          void *stream, int32_t *iterations, double *residual);

@@ -18,7 +18,7 @@
 //     and each call initialises every value it reads before reading it;
 //   * the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress, which may load the module) and the kernel's
-//     occupancy; make that first call before any stream capture.
+//     occupancy.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
