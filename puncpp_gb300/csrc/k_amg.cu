@@ -412,14 +412,43 @@ __device__ double vcycle_phase0(const AmgDev &M, const PcgArgs &a, const float *
     return rz;
 }
 
+// The FP64 true residual b - A x of this thread's rows (A the solver's FP64
+// SELL matrix; x read through L2, it is written inside the kernel) into r in
+// FP32; returns this thread's share of ||b - A x||^2 and, with want_bb, adds
+// its share of ||b||^2 to bb.
+__device__ __forceinline__ double true_residual(const PcgArgs &a, float *r, bool want_bb, double &bb, int t0,
+                                                int ts) {
+    double rr = 0.0;
+    for (int i = t0; i < a.n; i += ts) {
+        double s = 0.0;
+        const int64_t base = a.slice_ptr[i >> 5] + (i & 31);
+        const int w = a.slice_width[i >> 5];
+#pragma unroll 4
+        for (int k = 0; k < w; ++k) s = fma(__ldg(a.val + base + 32 * k), __ldcg(a.x + __ldg(a.col + base + 32 * k)), s);
+        const double bi = a.b[i];
+        const double ri = bi - s;
+        r[i] = (float)ri;
+        rr = fma(ri, ri, rr);
+        if (want_bb) bb = fma(bi, bi, bb);
+    }
+    return rr;
+}
+
 // Phases 1 .. of z = B r after phase 0 (L >= 1, r the current residual,
 // complete): down-sweep phases l = 1 .. L-1 (restriction or, at l = L-1,
 // G; smoothing t_l of levels l >= 2 into the stack; t_0 = W_0 r in phase 1
 // and t_1 = W_1 b_1 in phase L-1, where the restrictions leave the grid
 // idle), the collapsed up-sweep y_1 = t_1 + U1 [t_2 .. t_{L-1}, y_L]
 // (L >= 2), then z = t_0 + S_0 y_1; returns this thread's share of r.z.
+//
+// With rt (L >= 2): a residual replacement that keeps this cycle.  The FP64
+// true residual of the current x goes to rt (FP32) in the coarse phase l =
+// L-1, where the products are small, with its block partials of ||b - A x||^2
+// in part_rt; the returned r.z is taken against rt.  z = B r of the recurrence
+// residual r then stands for B rt: they differ by the recurrence's drift.
 __device__ __forceinline__ double vcycle_rest(const AmgDev &M, const float *r, float *z, cg::grid_group &grid,
-                                              int t0, int ts) {
+                                              int t0, int ts, const PcgArgs &a, float *rt, double *part_rt,
+                                              double *sh) {
     const int L = M.nlev - 1;
     for (int l = 1; l < L; ++l) {
         const float *b = M.lev[l].b;
@@ -461,6 +490,12 @@ __device__ __forceinline__ double vcycle_rest(const AmgDev &M, const float *r, f
             const float *b1 = M.lev[1].b;
             smooth<true>(M.lev[1], [=](int j) { return b1[j]; }, M.lev[1].t, pt0, pts);
         }
+        if (rt && l == L - 1) {
+            double unused = 0.0, ra, rb;
+            const double rr = true_residual(a, rt, false, unused, t0, ts);
+            block_sum2(rr, 0.0, sh, ra, rb);
+            if (threadIdx.x == 0) part_rt[blockIdx.x] = ra;
+        }
         grid.sync();
     }
     const float *yup = M.yL;
@@ -473,8 +508,9 @@ __device__ __forceinline__ double vcycle_rest(const AmgDev &M, const float *r, f
         yup = M.y1;
     }
     const float *tz = M.lev[0].t;
+    const float *rzv = rt ? rt : r;
     double rz = 0.0;
-    apply<true>(M.S0, [=](int j) { return yup[j]; }, [=](int i) { return make_float2(tz[i], r[i]); },
+    apply<true>(M.S0, [=](int j) { return yup[j]; }, [=](int i) { return make_float2(tz[i], rzv[i]); },
           [&](int i, float s, float2 tr) {
               const float zi = tr.x + s;
               z[i] = zi;
@@ -490,7 +526,7 @@ __device__ __forceinline__ double vcycle_rest(const AmgDev &M, const float *r, f
 __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M) {
     cg::grid_group grid = cg::this_grid();
     __shared__ double sh[2 * kPcgThreads + 16];
-    __shared__ double scal[4];
+    __shared__ double scal[5];
     const int nb = gridDim.x;
     const int n = a.n;
     const int L = M.nlev - 1;
@@ -528,19 +564,8 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M)
     float *r = a.r32, *rn = M.r_alt;
     for (int pass = 0;; ++pass) {
         // true residual in FP64 into the FP32 recurrence
-        double rr = 0.0, bb = 0.0;
-        for (int i = gtid; i < n; i += gstride) {
-            double s = 0.0;
-            const int64_t base = a.slice_ptr[i >> 5] + (i & 31);
-            const int w = a.slice_width[i >> 5];
-#pragma unroll 4
-            for (int k = 0; k < w; ++k) s = fma(__ldg(a.val + base + 32 * k), __ldcg(a.x + __ldg(a.col + base + 32 * k)), s);
-            const double bi = a.b[i];
-            const double ri = bi - s;
-            r[i] = (float)ri;
-            rr = fma(ri, ri, rr);
-            if (pass == 0) bb = fma(bi, bi, bb);
-        }
+        double bb = 0.0;
+        const double rr = true_residual(a, r, pass == 0, bb, gtid, gstride);
         block_sum2(rr, bb, sh, ra, rb);
         if (threadIdx.x == 0) { partB[blockIdx.x] = ra; partD[blockIdx.x] = rb; }
         grid.sync();
@@ -579,7 +604,7 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M)
             }
             grid.sync();
             if (L >= 1) {
-                const double rzp = vcycle_rest(M, r, a.z32, grid, gtid, gstride);
+                const double rzp = vcycle_rest(M, r, a.z32, grid, gtid, gstride, a, nullptr, nullptr, sh);
                 block_sum2(rzp, 0.0, sh, ra, rb);
                 if (threadIdx.x == 0) partC[blockIdx.x] = ra;
                 grid.sync();
@@ -632,23 +657,47 @@ __global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_amg(PcgArgs a, AmgDev M)
             }
             grid_sum2(partB, L == 0 ? partC : nullptr, nb, sh, ra, rb);
             if (threadIdx.x == 0) {
+                // replacement: at the end (tolerance or cap) by a new pass;
+                // between (the recurrence fell by 1e6 in ||r||^2) inside this
+                // cycle when L >= 2
                 const double rr_rec = ra;
-                scal[2] = (rr_rec <= 1e-6 * t_rmax || rr_rec <= t_tol2 || t_it >= a.max_iter) ? 1.0 : 0.0;
+                const bool last = rr_rec <= t_tol2 || t_it >= a.max_iter;
+                scal[2] = (last || (rr_rec <= 1e-6 * t_rmax && L < 2)) ? 1.0 : 0.0;
+                scal[4] = (!last && rr_rec <= 1e-6 * t_rmax && L >= 2) ? 1.0 : 0.0;
                 scal[3] = rb;
             }
             __syncthreads();
             if (scal[2] != 0.0) break;   // replace the residual (next pass)
+            const bool keep = scal[4] != 0.0;
             double rz = scal[3];
             if (L >= 1) {
-                const double rzp = vcycle_rest(M, r, a.z32, grid, gtid, gstride);
+                const double rzp = vcycle_rest(M, r, a.z32, grid, gtid, gstride, a, keep ? rn : nullptr, partD, sh);
                 block_sum2(rzp, 0.0, sh, ra, rb);
                 if (threadIdx.x == 0) partC[blockIdx.x] = ra;
                 grid.sync();
-                grid_sum2(partC, nullptr, nb, sh, ra, rb);
+                grid_sum2(partC, keep ? partD : nullptr, nb, sh, ra, rb);
                 rz = ra;
             }
-            if (threadIdx.x == 0) { scal[0] = rz / t_rz; t_rz = rz; }
+            if (threadIdx.x == 0) {
+                scal[1] = 1.0;
+                if (keep) {
+                    // the true residual replaces the recurrence's (as at a
+                    // pass start, with the same stall test)
+                    const bool stalled = rb > 1e-2 * t_rr;
+                    t_rr = rb;
+                    t_rmax = rb;
+                    ++t_updates;
+                    if (t_rr <= t_tol2) { t_status = 0; scal[1] = 0.0; }
+                    else if (stalled) { t_status = 3; scal[1] = 0.0; }
+                }
+                scal[0] = rz / t_rz;
+                t_rz = rz;
+            }
             __syncthreads();
+            if (keep) {
+                float *t = r; r = rn; rn = t;
+            }
+            if (scal[1] == 0.0) break;
         }
         if (scal[1] == 0.0) break;
         grid.sync();

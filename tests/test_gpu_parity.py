@@ -514,6 +514,25 @@ def test_amg_pcg_reports_an_unattainable_tolerance(lib, oracle_mod):
     pop.close()
 
 
+@pytest.mark.parametrize("rtol", [1e-10, 1e-13])
+def test_amg_pcg_residual_replacement_inside_the_cycle(rtol, lib, oracle_mod):
+    """A hierarchy of three or more levels: the replacements between the
+    start and the end of a solve take the FP64 true residual inside the
+    iteration's own V-cycle; the solve still meets the FP64 stopping test
+    (several replacements at rtol 1e-13) and matches a direct solve."""
+    ma, mesh, pop, o, rng = probe_setup(lib, oracle_mod, n=24, half=4.0, radius=0.8, n_particles=20000,
+                                        pcg_rtol=rtol, pcg_atol=1e-30, pcg_max_iter=5000)
+    assert len(punc.poisson_layout(pop)["levels"]) >= 3
+    rho = punc.distribute_cg1(pop)
+    objs = [punc.Object(2, potential=-2.0)]
+    solver = punc.PoissonSolver(pop, objs)
+    phi_g = solver.solve(punc.Function(pop, "phi"), punc.Function(pop, "rho"), objs)
+    info = solver.last_info
+    assert info.residual <= rtol * info.rhs_norm and info.iterations < 60
+    assert rel(phi_g, o.poisson_direct(rho, potentials=[-2.0])) < 1e4 * rtol
+    pop.close()
+
+
 def test_amg_strength_threshold_rebuild_and_selection(lib, oracle_mod):
     """pg_amg_set_strength rebuilds the hierarchy: level 0 and 1 stay, the
     coarsest level grows (48 rows at theta 0, 281 at 0.05 on this mesh), the
