@@ -281,6 +281,11 @@ int pg_circuit_cm_setup(pg_sim *sim, const pg_source *vsources, int32_t n_vsourc
 int pg_solve_circuit(pg_sim *sim, pg_object *objects, int32_t n_objects,
                      double *phi, pg_solve_info *info);
 int pg_get_phi(pg_sim *sim, double *phi);
+/* The potential after the work queued so far, read back without waiting:
+ * phi (ndof doubles; page-locked host memory lets the copy overlap the next
+ * steps) holds it once pg_synchronize returns.  Keep phi untouched until
+ * then; alternate buffers to keep several steps' potentials. */
+int pg_get_phi_async(pg_sim *sim, double *phi);
 int pg_get_rho(pg_sim *sim, double *rho);
 int pg_get_capacitance(pg_sim *sim, double *inv_capacitance);  /* [n_obj][n_obj] */
 
@@ -377,7 +382,8 @@ int pg_set_profiling(pg_sim *sim, int32_t on);
  * (waits for the later one). */
 int pg_event_record(pg_sim *sim, int32_t slot);
 int pg_event_elapsed(pg_sim *sim, int32_t from_slot, int32_t to_slot, double *ms);
-/* Wait until all work queued on the engine stream has finished. */
+/* Wait until all work queued on the engine stream, and every read-back of
+ * pg_get_phi_async, has finished. */
 int pg_synchronize(pg_sim *sim);
 /* ESolver::solve (punc/src/efield.cpp:70-75, punc/ufl/EField3D.ufl): the CG1
  * field E = L2 projection of -grad(phi) (phi: the current potential), solved

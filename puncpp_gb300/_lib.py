@@ -140,6 +140,7 @@ SIGNATURES = {
     "pg_circuit_cm_setup": ([_P, C.POINTER(Source), C.c_int32, C.POINTER(Source), C.c_int32, C.c_double], C.c_int),
     "pg_solve_circuit": ([_P, C.POINTER(Object), C.c_int32, _D, C.POINTER(SolveInfo)], C.c_int),
     "pg_get_phi": ([_P, _D], C.c_int),
+    "pg_get_phi_async": ([_P, _D], C.c_int),
     "pg_get_rho": ([_P, _D], C.c_int),
     "pg_get_capacitance": ([_P, _D], C.c_int),
     "pg_create_flux": ([_P, C.POINTER(Species), C.c_int32], C.c_int),

@@ -19,6 +19,11 @@ using namespace pg;
 struct pg_sim {
     pg_config cfg{};
     cudaStream_t stream = nullptr;
+    // pg_get_phi_async: a snapshot of phi read back on a copy stream
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t phi_ready = nullptr, phi_copied = nullptr;
+    double *phi_snap = nullptr;
+    bool phi_copy_pending = false;
     int device = 0;
     std::vector<void *> allocs;  // mesh and solver buffers (freed at destroy)
 
@@ -1347,6 +1352,12 @@ int pg_destroy(pg_sim *s) {
     for (auto &e : s->ev_pending) { cudaEventDestroy(e.second.first); cudaEventDestroy(e.second.second); }
     for (auto &e : s->user_ev)
         if (e) cudaEventDestroy(e);
+    if (s->copy_stream) {
+        cudaStreamSynchronize(s->copy_stream);
+        cudaStreamDestroy(s->copy_stream);
+        cudaEventDestroy(s->phi_ready);
+        cudaEventDestroy(s->phi_copied);
+    }
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return PG_OK;
@@ -1951,6 +1962,29 @@ int pg_get_phi(pg_sim *s, double *phi) {
     if (!s || !phi) return fail(PG_ERR_ARG, "pg_get_phi: NULL argument");
     PG_CUDA(cudaStreamSynchronize(s->stream));
     PG_CUDA(cudaMemcpy(phi, s->phi, sizeof(double) * s->ndof, cudaMemcpyDeviceToHost));
+    return PG_OK;
+}
+
+// The potential as it stands after the work queued so far: copied to a
+// device snapshot on the engine stream, then read back to phi on a copy
+// stream, so the next steps run while the copy is in flight.  The snapshot is
+// written again only after the previous read-back has finished.
+int pg_get_phi_async(pg_sim *s, double *phi) {
+    if (!s || !phi) return fail(PG_ERR_ARG, "pg_get_phi_async: NULL argument");
+    if (!s->copy_stream) {
+        PG_CUDA(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+        PG_CUDA(cudaEventCreateWithFlags(&s->phi_ready, cudaEventDisableTiming));
+        PG_CUDA(cudaEventCreateWithFlags(&s->phi_copied, cudaEventDisableTiming));
+        const int rc = dalloc(s, &s->phi_snap, s->ndof);
+        if (rc) return rc;
+    }
+    if (s->phi_copy_pending) PG_CUDA(cudaStreamWaitEvent(s->stream, s->phi_copied, 0));
+    PG_CUDA(cudaMemcpyAsync(s->phi_snap, s->phi, sizeof(double) * s->ndof, cudaMemcpyDeviceToDevice, s->stream));
+    PG_CUDA(cudaEventRecord(s->phi_ready, s->stream));
+    PG_CUDA(cudaStreamWaitEvent(s->copy_stream, s->phi_ready, 0));
+    PG_CUDA(cudaMemcpyAsync(phi, s->phi_snap, sizeof(double) * s->ndof, cudaMemcpyDeviceToHost, s->copy_stream));
+    PG_CUDA(cudaEventRecord(s->phi_copied, s->copy_stream));
+    s->phi_copy_pending = true;
     return PG_OK;
 }
 
@@ -3098,6 +3132,10 @@ int pg_launch_count(int64_t *n) {
 int pg_synchronize(pg_sim *s) {
     if (!s) return fail(PG_ERR_ARG, "NULL handle");
     PG_CUDA(cudaStreamSynchronize(s->stream));
+    if (s->copy_stream) {
+        PG_CUDA(cudaStreamSynchronize(s->copy_stream));
+        s->phi_copy_pending = false;
+    }
     return PG_OK;
 }
 

@@ -241,6 +241,51 @@ def test_run_steps_equals_step_by_step(use_graph, lib, oracle_mod):
     assert np.array_equal(p1.particles()["x"], p2.particles()["x"])
 
 
+@pytest.mark.parametrize("pinned", [True, False])
+def test_async_potential_read_back(pinned, lib, oracle_mod):
+    """pg_get_phi_async after each of six graph-replayed steps, into
+    alternating host buffers (page-locked or not), read after one
+    pg_synchronize: each buffer holds the potential of its step (bit for bit
+    that of a second handle read with pg_get_phi after every step), and the
+    steps' particles are unchanged by the read-backs in flight."""
+    torch = pytest.importorskip("torch")
+    ma = meshgen.probe_box(8, 3.0, 0.8)
+    mesh = punc.Mesh(ma)
+    rng = np.random.default_rng(37)
+    xe, ve = f32(uniform_points(ma, 20000, rng)), f32(maxwellian_velocities(20000, 1.0, rng))
+    sp = [punc.Species(-1.0, 1.0, n=20.0, vth=1.0)]
+    runs = []
+    for k in range(2):
+        pop = punc.Population(mesh, precision=L.PG_MIXED, pcg_rtol=1e-10)
+        pop.add_particles(xe, ve, -1.0, 1.0)
+        punc.create_flux(pop, sp)
+        objs = [punc.Object(2)]
+        punc.CircuitCM(pop, objs, [(-1, 0, -1.5)], [], 0.1)
+        runs.append((pop, objs))
+    (p1, o1), (p2, o2) = runs
+    ref = []
+    for n in range(6):
+        punc.run_steps(p1, o1, 0.1, 1, first_step=(n == 0), inject=True, seed=5, step_no=n)
+        ref.append(punc.Function(p1, "phi").vector().copy())
+    if pinned:
+        bufs = [torch.zeros(mesh.n_dofs, dtype=torch.float64, pin_memory=True) for _ in range(6)]
+        arrs = [b.numpy() for b in bufs]
+    else:
+        arrs = [np.zeros(mesh.n_dofs) for _ in range(6)]
+    for n in range(6):
+        punc.run_steps(p2, o2, 0.1, 1, first_step=(n == 0), inject=True, seed=5, step_no=n)
+        L.check(lib.pg_get_phi_async(p2.handle, L.dptr(arrs[n])))
+    L.check(lib.pg_synchronize(p2.handle))
+    for n in range(6):
+        assert np.array_equal(arrs[n], ref[n]), n
+    assert not np.array_equal(ref[0], ref[5])
+    a, b = p1.particles(), p2.particles()
+    for k in ("id", "cell", "x", "v"):
+        assert np.array_equal(a[k], b[k]), k
+    p1.close()
+    p2.close()
+
+
 def test_launch_tuning_does_not_change_the_mixed_results(lib, oracle_mod):
     """The mixed form is deterministic: block size, grid size and the
     warp-aggregated deposit give the same particles and charge bit for bit;
