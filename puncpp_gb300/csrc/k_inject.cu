@@ -62,7 +62,13 @@ __global__ void k_inject_count(InjectParams ip, const double *__restrict__ flux_
     counts[idx] = n;
 }
 
-// One warp per injected particle (grid-stride over particles).
+// One warp per 32 injected particles (grid-stride over groups): each lane
+// finds its particle's stream (a binary search over the stream offsets) and
+// loads what the sampling needs, all lanes at once; the warp then samples the
+// group's velocities one particle after another (32 candidates a round, the
+// first accepted one kept by the particle's lane); finally each lane forms
+// its particle's position, walks it from the facet's cell and deposits it.
+// The arithmetic of every particle is the one-particle-at-a-time sequence.
 __global__ void __launch_bounds__(kThreads, 8) k_inject_generate(DevMesh m, DevParticles p, InjectParams ip, const double *__restrict__ pdf_max,
                                   const double *__restrict__ facets, const int64_t *__restrict__ offsets,
                                   int max_steps, int deposit, const double *__restrict__ qsp,
@@ -72,83 +78,105 @@ __global__ void __launch_bounds__(kThreads, 8) k_inject_generate(DevMesh m, DevP
     const int64_t slot_base = ip.counts_dev ? ip.counts_dev[0] : ip.slot_base;
     const int64_t pid_base = ip.counts_dev ? ip.counts_dev[1] : ip.pid_base;
     const uint32_t step = ip.counts_dev ? (uint32_t)ip.counts_dev[2] : ip.step;
+    const bool mixed = p.xf != nullptr;
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     if (warp == 0 && lane == 0) st->inject_total = total;
-    for (int64_t t = warp; t < total; t += nwarps) {
-        // stream of particle t: the last idx with offsets[idx] <= t
-        int lo = 0, hi = total_streams;
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (offsets[mid] <= t) lo = mid; else hi = mid;
+    for (int64_t g0 = warp * 32; g0 < total; g0 += nwarps * 32) {
+        // this lane's particle t and its stream idx: the last idx with
+        // offsets[idx] <= t
+        const int64_t t = g0 + lane;
+        const bool mine = t < total;
+        int idx = 0;
+        if (mine) {
+            int lo = 0, hi = total_streams;
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (offsets[mid] <= t) lo = mid; else hi = mid;
+            }
+            idx = lo;
         }
-        const int idx = lo;
-        const int64_t k = t - offsets[idx];
+        const int64_t k = mine ? t - offsets[idx] : 0;
         const int s = idx / ip.n_facets, j = idx % ip.n_facets;
-        const InjectSpecies &S = ip.sp[s];
         const double *F = facets + 14 * (size_t)j;
-        const bool mixed = p.xf != nullptr;
-        float4 G0 = make_float4(0, 0, 0, 0), G1 = G0, G2 = G0, G3 = G0;
-        if (mixed) {
-            const float4 *G = ip.facets_f + 4 * (size_t)j;
-            G0 = __ldg(G); G1 = __ldg(G + 1); G2 = __ldg(G + 2); G3 = __ldg(G + 3);
-        }
-        const uint32_t c1 = ip.facet_c1 ? ip.facet_c1[j] : (uint32_t)j, c2 = (uint32_t)(s + 8 * (k + 1)), c3 = step;
+        const uint32_t c1 = ip.facet_c1 ? ip.facet_c1[j] : (uint32_t)j, c2 = (uint32_t)(s + 8 * (k + 1));
         const uint64_t seed = ip.facet_seed ? ip.seed + ip.facet_seed[j] : ip.seed;
-        const double pmax = pdf_max[idx];
-        // rejection sampling, 32 candidates per round; each candidate is
-        // screened in FP32 and only undecided ones take the FP64 test
-        FluxBox B;
-        for (int c = 0; c < 3; ++c) { B.lo[c] = S.domain_lo[c]; B.w[c] = S.domain_w[c]; B.vd[c] = S.vd[c]; }
-        B.vth2 = S.vth2;
-        B.factor = S.factor;
-        const FluxBox32 &B32 = ip.sp32[s];
+        const double pmax = mine ? pdf_max[idx] : 0.0;
+        double nx = 0.0, ny = 0.0, nz = 0.0;
         float nx32, ny32, nz32;
-        if (mixed) { nx32 = G2.y; ny32 = G2.z; nz32 = G2.w; }
-        else { nx32 = (float)F[10]; ny32 = (float)F[11]; nz32 = (float)F[12]; }
-        const float pmax32 = (float)pmax;
-        const uint32_t k0 = uint32_t(seed), k1 = uint32_t(seed >> 32);
-        double vx = 0, vy = 0, vz = 0;
-        uint32_t wv0 = 0, wv1 = 0, wv2 = 0, wv3 = 0, wv4 = 0, wv5 = 0;   // the accepted candidate's words
+        if (mixed) {
+            const float4 G2 = __ldg(ip.facets_f + 4 * (size_t)j + 2);
+            nx32 = G2.y; ny32 = G2.z; nz32 = G2.w;
+        }
+        if (mine) { nx = F[10]; ny = F[11]; nz = F[12]; }
+        if (!mixed) { nx32 = (float)nx; ny32 = (float)ny; nz32 = (float)nz; }
+        // rejection sampling of the group's particles in turn; each candidate
+        // is screened in FP32 and only undecided ones take the FP64 test
+        uint32_t wv0 = 0, wv1 = 0, wv2 = 0, wv3 = 0, wv4 = 0, wv5 = 0;   // this lane's accepted candidate
         int found = -1;
-        for (int round = 0; round < kMaxRounds && found < 0; ++round) {
-            const uint32_t cand = (uint32_t)round * 32u + (uint32_t)lane;
-            const Philox4 ra = philox4x32_10(2u + 2u * cand, c1, c2, c3, k0, k1);
-            const Philox4 rb = philox4x32_10(3u + 2u * cand, c1, c2, c3, k0, k1);
-            int dec = flux_screen_fp32(B32, nx32, ny32, nz32, pmax32, ra.v[0], ra.v[2], rb.v[0], rb.v[2]);
-            if (dec < 0) {
-                double t[3];
-                dec = flux_accept_fp64(B, F[10], F[11], F[12], pmax, u01_from(ra.v[0], ra.v[1]),
-                                       u01_from(ra.v[2], ra.v[3]), u01_from(rb.v[0], rb.v[1]),
-                                       u01_from(rb.v[2], rb.v[3]), t) ? 1 : 0;
-            }
-            const unsigned acc = __ballot_sync(0xffffffffu, dec == 1);
-            if (acc) {
-                const int first = __ffs(acc) - 1;
-                found = first;
-                wv0 = __shfl_sync(0xffffffffu, ra.v[0], first);
-                wv1 = __shfl_sync(0xffffffffu, ra.v[1], first);
-                wv2 = __shfl_sync(0xffffffffu, ra.v[2], first);
-                wv3 = __shfl_sync(0xffffffffu, ra.v[3], first);
-                wv4 = __shfl_sync(0xffffffffu, rb.v[0], first);
-                wv5 = __shfl_sync(0xffffffffu, rb.v[1], first);
+        const int n_group = total - g0 < 32 ? (int)(total - g0) : 32;
+        for (int q = 0; q < n_group; ++q) {
+            const int sq = __shfl_sync(0xffffffffu, s, q);
+            const uint32_t qc1 = __shfl_sync(0xffffffffu, c1, q), qc2 = __shfl_sync(0xffffffffu, c2, q);
+            const uint64_t qseed = __shfl_sync(0xffffffffu, seed, q);
+            const double qpmax = __shfl_sync(0xffffffffu, pmax, q);
+            const double qnx = __shfl_sync(0xffffffffu, nx, q), qny = __shfl_sync(0xffffffffu, ny, q);
+            const double qnz = __shfl_sync(0xffffffffu, nz, q);
+            const float qnx32 = __shfl_sync(0xffffffffu, nx32, q), qny32 = __shfl_sync(0xffffffffu, ny32, q);
+            const float qnz32 = __shfl_sync(0xffffffffu, nz32, q);
+            const InjectSpecies &S = ip.sp[sq];
+            FluxBox B;
+            for (int c = 0; c < 3; ++c) { B.lo[c] = S.domain_lo[c]; B.w[c] = S.domain_w[c]; B.vd[c] = S.vd[c]; }
+            B.vth2 = S.vth2;
+            B.factor = S.factor;
+            const FluxBox32 &B32 = ip.sp32[sq];
+            const float pmax32 = (float)qpmax;
+            const uint32_t k0 = uint32_t(qseed), k1 = uint32_t(qseed >> 32);
+            int qfound = -1;
+            for (int round = 0; round < kMaxRounds && qfound < 0; ++round) {
+                const uint32_t cand = (uint32_t)round * 32u + (uint32_t)lane;
+                const Philox4 ra = philox4x32_10(2u + 2u * cand, qc1, qc2, step, k0, k1);
+                const Philox4 rb = philox4x32_10(3u + 2u * cand, qc1, qc2, step, k0, k1);
+                int dec = flux_screen_fp32(B32, qnx32, qny32, qnz32, pmax32, ra.v[0], ra.v[2], rb.v[0], rb.v[2]);
+                if (dec < 0) {
+                    double tv[3];
+                    dec = flux_accept_fp64(B, qnx, qny, qnz, qpmax, u01_from(ra.v[0], ra.v[1]),
+                                           u01_from(ra.v[2], ra.v[3]), u01_from(rb.v[0], rb.v[1]),
+                                           u01_from(rb.v[2], rb.v[3]), tv) ? 1 : 0;
+                }
+                const unsigned acc = __ballot_sync(0xffffffffu, dec == 1);
+                if (acc) {
+                    const int first = __ffs(acc) - 1;
+                    qfound = first;
+                    const uint32_t a0 = __shfl_sync(0xffffffffu, ra.v[0], first);
+                    const uint32_t a1 = __shfl_sync(0xffffffffu, ra.v[1], first);
+                    const uint32_t a2 = __shfl_sync(0xffffffffu, ra.v[2], first);
+                    const uint32_t a3 = __shfl_sync(0xffffffffu, ra.v[3], first);
+                    const uint32_t a4 = __shfl_sync(0xffffffffu, rb.v[0], first);
+                    const uint32_t a5 = __shfl_sync(0xffffffffu, rb.v[1], first);
+                    if (lane == q) { found = first; wv0 = a0; wv1 = a1; wv2 = a2; wv3 = a3; wv4 = a4; wv5 = a5; }
+                }
             }
         }
-        if (lane != 0) continue;
+        if (!mine) continue;
         const int64_t i = slot_base + t;
         p.sp[i] = (uint8_t)s;
         p.pid[i] = pid_base + t;
         if (found < 0) { raise_device_error(st, PG_ERR_ARG, idx); p.cell[i] = kDead; continue; }
+        const uint32_t k0 = uint32_t(seed), k1 = uint32_t(seed >> 32);
         if (mixed) {
             // mixed form: the velocity and the position in FP32 from the same
             // random words (24-bit uniforms), the facet in FP32; the
             // acceptance above is the FP64 decision
+            const FluxBox32 &B32 = ip.sp32[s];
+            const float4 *G = ip.facets_f + 4 * (size_t)j;
+            const float4 G0 = __ldg(G), G1 = __ldg(G + 1), G2 = __ldg(G + 2), G3 = __ldg(G + 3);
             const float vxf = B32.lo[0] + B32.w[0] * u01_24(wv0);
             const float vyf = B32.lo[1] + B32.w[1] * u01_24(wv2);
             const float vzf = B32.lo[2] + B32.w[2] * u01_24(wv4);
-            const Philox4 q0 = philox4x32_10(0u, c1, c2, c3, k0, k1);
-            const Philox4 q1 = philox4x32_10(1u, c1, c2, c3, k0, k1);
+            const Philox4 q0 = philox4x32_10(0u, c1, c2, step, k0, k1);
+            const Philox4 q1 = philox4x32_10(1u, c1, c2, step, k0, k1);
             const float r1 = u01_24(q0.v[0]), r2 = u01_24(q0.v[2]), r = u01_24(q1.v[0]);
             float x = (1.0f - r1) * G0.x + r1 * G0.w;
             float y = (1.0f - r1) * G0.y + r1 * G1.x;
@@ -173,12 +201,13 @@ __global__ void __launch_bounds__(kThreads, 8) k_inject_generate(DevMesh m, DevP
             if (deposit) deposit_fixed(m, c, x, y, z, ip.q_scaled[s], ip.rho_fixed);
             continue;
         }
-        vx = B.lo[0] + B.w[0] * u01_from(wv0, wv1);
-        vy = B.lo[1] + B.w[1] * u01_from(wv2, wv3);
-        vz = B.lo[2] + B.w[2] * u01_from(wv4, wv5);
+        const InjectSpecies &S = ip.sp[s];
+        const double vx = S.domain_lo[0] + S.domain_w[0] * u01_from(wv0, wv1);
+        const double vy = S.domain_lo[1] + S.domain_w[1] * u01_from(wv2, wv3);
+        const double vz = S.domain_lo[2] + S.domain_w[2] * u01_from(wv4, wv5);
         double r1, r2, r, unused;
-        uniforms2(seed, 0u, c1, c2, c3, r1, r2);
-        uniforms2(seed, 1u, c1, c2, c3, r, unused);
+        uniforms2(seed, 0u, c1, c2, step, r1, r2);
+        uniforms2(seed, 1u, c1, c2, step, r, unused);
         double x = (1.0 - r1) * F[1] + r1 * F[4];
         double y = (1.0 - r1) * F[2] + r1 * F[5];
         double z = (1.0 - r1) * F[3] + r1 * F[6];
@@ -231,7 +260,7 @@ void launch_inject_generate(const DevMesh &m, const DevParticles &p, const Injec
                             int64_t max_particles, cudaStream_t st) {
     (void)flux_num;
     if (ip.n_species * ip.n_facets <= 0) return;
-    const int64_t warps = std::max<int64_t>(1, std::min<int64_t>(max_particles, (int64_t)sm_count() * 64));
+    const int64_t warps = std::max<int64_t>(1, std::min<int64_t>((max_particles + 31) / 32, (int64_t)sm_count() * 64));
     const int64_t blocks = (warps * 32 + kThreads - 1) / kThreads;
     count_launches(1);
     k_inject_generate<<<(unsigned)blocks, kThreads, 0, st>>>(m, p, ip, pdf_max, facets, offsets, max_steps, deposit,
