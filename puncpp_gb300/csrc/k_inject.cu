@@ -62,13 +62,15 @@ __global__ void k_inject_count(InjectParams ip, const double *__restrict__ flux_
     counts[idx] = n;
 }
 
-// One warp per 32 injected particles (grid-stride over groups): each lane
-// finds its particle's stream (a binary search over the stream offsets) and
-// loads what the sampling needs, all lanes at once; the warp then samples the
-// group's velocities one particle after another (32 candidates a round, the
-// first accepted one kept by the particle's lane); finally each lane forms
-// its particle's position, walks it from the facet's cell and deposits it.
-// The arithmetic of every particle is the one-particle-at-a-time sequence.
+// One warp per group of G consecutive injected particles (grid-stride over
+// groups; G = the particles per warp of the launch, 1..32, so that small
+// injections still spread over every warp): each of lanes 0..G-1 finds its
+// particle's stream (a binary search over the stream offsets) and loads what
+// the sampling needs, all at once; the warp then samples the group's
+// velocities one particle after another (32 candidates a round, the first
+// accepted one kept by the particle's lane); finally each lane forms its
+// particle's position, walks it from the facet's cell and deposits it. The
+// arithmetic of every particle is the one-particle-at-a-time sequence.
 __global__ void __launch_bounds__(kThreads, 8) k_inject_generate(DevMesh m, DevParticles p, InjectParams ip, const double *__restrict__ pdf_max,
                                   const double *__restrict__ facets, const int64_t *__restrict__ offsets,
                                   int max_steps, int deposit, const double *__restrict__ qsp,
@@ -83,11 +85,13 @@ __global__ void __launch_bounds__(kThreads, 8) k_inject_generate(DevMesh m, DevP
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     if (warp == 0 && lane == 0) st->inject_total = total;
-    for (int64_t g0 = warp * 32; g0 < total; g0 += nwarps * 32) {
+    const int64_t per_warp = (total + nwarps - 1) / nwarps;
+    const int G = per_warp < 1 ? 1 : per_warp > 32 ? 32 : (int)per_warp;
+    for (int64_t g0 = warp * G; g0 < total; g0 += nwarps * G) {
         // this lane's particle t and its stream idx: the last idx with
         // offsets[idx] <= t
         const int64_t t = g0 + lane;
-        const bool mine = t < total;
+        const bool mine = lane < G && t < total;
         int idx = 0;
         if (mine) {
             int lo = 0, hi = total_streams;
@@ -115,7 +119,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_inject_generate(DevMesh m, DevP
         // is screened in FP32 and only undecided ones take the FP64 test
         uint32_t wv0 = 0, wv1 = 0, wv2 = 0, wv3 = 0, wv4 = 0, wv5 = 0;   // this lane's accepted candidate
         int found = -1;
-        const int n_group = total - g0 < 32 ? (int)(total - g0) : 32;
+        const int n_group = total - g0 < G ? (int)(total - g0) : G;
         for (int q = 0; q < n_group; ++q) {
             const int sq = __shfl_sync(0xffffffffu, s, q);
             const uint32_t qc1 = __shfl_sync(0xffffffffu, c1, q), qc2 = __shfl_sync(0xffffffffu, c2, q);
@@ -260,7 +264,7 @@ void launch_inject_generate(const DevMesh &m, const DevParticles &p, const Injec
                             int64_t max_particles, cudaStream_t st) {
     (void)flux_num;
     if (ip.n_species * ip.n_facets <= 0) return;
-    const int64_t warps = std::max<int64_t>(1, std::min<int64_t>((max_particles + 31) / 32, (int64_t)sm_count() * 64));
+    const int64_t warps = std::max<int64_t>(1, std::min<int64_t>(max_particles, (int64_t)sm_count() * 64));
     const int64_t blocks = (warps * 32 + kThreads - 1) / kThreads;
     count_launches(1);
     k_inject_generate<<<(unsigned)blocks, kThreads, 0, st>>>(m, p, ip, pdf_max, facets, offsets, max_steps, deposit,
