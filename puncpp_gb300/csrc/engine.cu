@@ -1355,9 +1355,9 @@ int pg_destroy(pg_sim *s) {
     if (s->copy_stream) {
         cudaStreamSynchronize(s->copy_stream);
         cudaStreamDestroy(s->copy_stream);
-        cudaEventDestroy(s->phi_ready);
-        cudaEventDestroy(s->phi_copied);
     }
+    if (s->phi_ready) cudaEventDestroy(s->phi_ready);
+    if (s->phi_copied) cudaEventDestroy(s->phi_copied);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return PG_OK;
@@ -1971,13 +1971,13 @@ int pg_get_phi(pg_sim *s, double *phi) {
 // written again only after the previous read-back has finished.
 int pg_get_phi_async(pg_sim *s, double *phi) {
     if (!s || !phi) return fail(PG_ERR_ARG, "pg_get_phi_async: NULL argument");
-    if (!s->copy_stream) {
-        PG_CUDA(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
-        PG_CUDA(cudaEventCreateWithFlags(&s->phi_ready, cudaEventDisableTiming));
-        PG_CUDA(cudaEventCreateWithFlags(&s->phi_copied, cudaEventDisableTiming));
+    if (!s->phi_snap) {
         const int rc = dalloc(s, &s->phi_snap, s->ndof);
         if (rc) return rc;
     }
+    if (!s->copy_stream) PG_CUDA(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+    if (!s->phi_ready) PG_CUDA(cudaEventCreateWithFlags(&s->phi_ready, cudaEventDisableTiming));
+    if (!s->phi_copied) PG_CUDA(cudaEventCreateWithFlags(&s->phi_copied, cudaEventDisableTiming));
     if (s->phi_copy_pending) PG_CUDA(cudaStreamWaitEvent(s->stream, s->phi_copied, 0));
     PG_CUDA(cudaMemcpyAsync(s->phi_snap, s->phi, sizeof(double) * s->ndof, cudaMemcpyDeviceToDevice, s->stream));
     PG_CUDA(cudaEventRecord(s->phi_ready, s->stream));
@@ -2707,7 +2707,8 @@ int pg_autotune_amg(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_
     s->profiling = true;
     pg_step_args st = *a;
     int rc = PG_OK;
-    double bt = s->amg_theta, bms = 1e300;
+    const double theta0 = s->amg_theta;
+    double bt = theta0, bms = 1e300;
     for (int c = 0; c < nc && rc == PG_OK; ++c) {
         if ((rc = pg_amg_set_strength(s, cand[c]))) break;
         collect_stages(s);
@@ -2723,7 +2724,12 @@ int pg_autotune_amg(pg_sim *s, const pg_step_args *a, pg_object *objects, int32_
         if (ms < bms) { bms = ms; bt = cand[c]; }
     }
     s->profiling = profiling;
-    if (rc) return rc;
+    if (rc) {
+        // back to the threshold the call started with
+        const std::string msg = pg_last_error();
+        if (pg_amg_set_strength(s, theta0) == PG_OK) return fail(rc, msg);
+        return rc;
+    }
     if ((rc = pg_amg_set_strength(s, bt))) return rc;
     if (best_theta) *best_theta = bt;
     if (best_ms) *best_ms = bms;
