@@ -3,7 +3,10 @@
 //
 // Krylov recurrence in FP32 with the solution, inner products and
 // true-residual replacements in FP64 (as k_pcg_rel), stopping on the FP64
-// true residual ||b - A x|| <= max(rtol ||b||, atol).
+// true residual ||b - A x|| <= max(rtol ||b||, atol).  A replacement before
+// the end of a solve (hierarchies of three or more levels) takes the true
+// residual inside the iteration's own V-cycle; the one at the end is a new
+// pass that restarts the cycle from the true residual.
 //
 // The V-cycle (one weighted-Jacobi sweep from zero before the coarse
 // correction and one after, Galerkin coarse operators, dense coarsest

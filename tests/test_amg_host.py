@@ -241,6 +241,29 @@ def test_collapsed_cycle_equals_the_vcycle(coarse_max, depth, amgd, probe22):
     np.testing.assert_allclose(vcycle_collapsed(levels, cinv, cyc, b), ref, rtol=0, atol=1e-10 * abs(ref).max())
 
 
+def test_strength_threshold_coarsens_less_from_level_one(amgd, probe22):
+    """A strength threshold (the engine's pg_amg_set_strength): the Kuhn
+    Laplacian's couplings are all 1/6 of the diagonal, so level 0's aggregates
+    and level 1 do not change; below that weak couplings are dropped and the
+    coarser levels grow.  The collapsed cycle still equals the textbook
+    V-cycle and the preconditioned CG meets the tolerance in a similar count."""
+    ma, A = probe22
+    b = np.random.default_rng(11).standard_normal(A.shape[0])
+    its = {}
+    sizes = {}
+    for theta in (0.0, 0.05):
+        cyc = {}
+        levels, cinv = hierarchy(amgd, A, theta=theta, theta_factor=1.0, cycle=cyc)
+        sizes[theta] = [L["A"].shape[0] for L in levels]
+        ref = vcycle_textbook(levels, cinv, b)
+        np.testing.assert_allclose(vcycle_collapsed(levels, cinv, cyc, b), ref, rtol=0, atol=1e-10 * abs(ref).max())
+        x, its[theta] = pcg(A, b, lambda r: vcycle(levels, cinv, r), 1e-10)
+        assert np.linalg.norm(b - A @ x) <= 1e-10 * np.linalg.norm(b)
+    assert sizes[0.05][:2] == sizes[0.0][:2], sizes
+    assert sizes[0.05][-1] > sizes[0.0][-1], sizes
+    assert its[0.05] <= its[0.0] + 2, its
+
+
 def test_vcycle_preconditioner_beats_jacobi(amgd, probe):
     ma, A = probe
     levels, cinv = hierarchy(amgd, A)
