@@ -474,7 +474,8 @@ inline std::size_t inject_particles(Population<3> &pop, const std::vector<Specie
 }
 
 // Extensions without a reference counterpart (the C ABI's pg_run_steps,
-// pg_autotune and pg_adjoint_*), with the shim's object conventions.
+// pg_autotune, pg_amg_*, pg_get_phi_async and pg_adjoint_*), with the shim's
+// object conventions.
 
 // n_steps fused steps with the bookkeeping on the device, replaying a
 // captured CUDA graph per step when `graph`; one result per step.
@@ -498,6 +499,26 @@ inline pg_tuning autotune(Population<3> &pop, ObjectVector &objects, const pg_st
     detail::from_c(v, objects);
     return t;
 }
+
+// AMG strength threshold of the Poisson preconditioner: set (rebuilds the
+// hierarchy), or chosen from timed real steps among the candidates ({0, 0.01,
+// 0.02} when empty; the steps advance the simulation), returning the choice.
+inline void set_amg_strength(Population<3> &pop, double theta) { check(pg_amg_set_strength(pop.handle, theta)); }
+inline double autotune_amg(Population<3> &pop, ObjectVector &objects, const pg_step_args &args,
+                           int32_t steps_per_trial = 6, const std::vector<double> &thetas = {}) {
+    auto v = detail::to_c(objects);
+    double best = 0.0, ms = 0.0;
+    check(pg_autotune_amg(pop.handle, &args, v.data(), (int32_t)v.size(), steps_per_trial,
+                          thetas.empty() ? nullptr : thetas.data(), (int32_t)thetas.size(), &best, &ms));
+    detail::from_c(v, objects);
+    return best;
+}
+
+// The potential read back without waiting (pg_get_phi_async): `out` (ndof
+// doubles, page-locked for the copy to overlap the next steps) holds it after
+// synchronize(pop).
+inline void get_phi_async(Population<3> &pop, double *out) { check(pg_get_phi_async(pop.handle, out)); }
+inline void synchronize(Population<3> &pop) { check(pg_synchronize(pop.handle)); }
 
 // Adjoint of K fused FP64 steps: forward (returns ||rho_K - target||^2), then
 // the gradients with respect to the initial velocities and positions (by
